@@ -1,0 +1,357 @@
+"""Generate the golden fixtures from the reference's own NumPy code path.
+
+Run from the repository root in a container that has the reference checkout:
+
+    python tests/golden/make_golden.py [/path/to/reference]
+
+The reference package ``gurugram_flood`` cannot be imported normally here
+(its ``__init__`` needs PyYAML and its engine needs pandas), so bare package
+stubs point at its source directories and only the NumPy-capable modules are
+loaded: ``kernels/triangular_backend.py`` (with ``equations.py``,
+``network_kernels.py``, ``pipe_kernels.py``), ``solver/stabilizers.py`` and
+``domain/production_infiltration_support.py``.  The engine loop
+(``solver/engine.py:219-344``) is restated here on top of those functions.
+
+Dtype discipline follows the reference's CuPy production path: every scalar
+forcing is passed as ``np.float32`` and ``h`` is cast back to float32 after the
+drainage step (the CuPy fused kernels keep the surface state float32 where
+the NumPy drainage path would promote it to float64).
+
+The fixtures are small ``.npz`` files committed next to this script; tests
+read only the fixtures, never the reference.
+"""
+
+from __future__ import annotations
+
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+OUT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "gpu-urban-flood-cupy-jax_gb300"))
+
+
+def import_reference(ref_root: Path):
+    src = ref_root / "HF_CUPY_JAX_COMPLETED_PROJECT" / "reproduction" / "source" / "src" / "gurugram_flood"
+    for name, sub in (("gurugram_flood", ""), ("gurugram_flood.kernels", "kernels"),
+                      ("gurugram_flood.domain", "domain"), ("gurugram_flood.solver", "solver")):
+        mod = types.ModuleType(name)
+        mod.__path__ = [str(src / sub) if sub else str(src)]
+        sys.modules[name] = mod
+    import gurugram_flood.domain.production_infiltration_support as pis
+    import gurugram_flood.kernels.triangular_backend as tb
+    import gurugram_flood.solver.stabilizers as stab
+
+    return tb, stab, pis
+
+
+def topo_arrays(prefix, st):
+    return {
+        f"{prefix}bed": st.bed_elevation_m, f"{prefix}manning": st.manning_n, f"{prefix}area": st.cell_area_m2,
+        f"{prefix}char_len": st.characteristic_length_m, f"{prefix}left": st.edge_left_cell,
+        f"{prefix}right": st.edge_right_cell, f"{prefix}nx": st.edge_normal_x, f"{prefix}ny": st.edge_normal_y,
+        f"{prefix}len": st.edge_length_m, f"{prefix}bcode": st.boundary_code,
+        f"{prefix}active": st.active_mask if st.active_mask is not None else np.ones(st.cell_count, np.float32),
+        f"{prefix}has_active": np.int32(st.active_mask is not None),
+        f"{prefix}has_stage": np.int32(st.has_stage_boundary),
+    }
+
+
+def coupling_arrays(prefix, cp, pp):
+    out = {}
+    for name in ("inlet_cell_index", "inlet_node_index", "node_surface_cell_index", "node_invert_elevation_m",
+                 "node_storage_area_m2", "node_max_depth_m", "inlet_capture_capacity_m3ps",
+                 "inlet_surcharge_capacity_m3ps"):
+        v = getattr(cp, name)
+        if v is not None:
+            out[f"{prefix}{name}"] = np.asarray(v)
+    for name in ("link_from_node_index", "link_to_node_index", "link_length_m", "link_area_m2",
+                 "link_hydraulic_radius_m", "link_manning_n", "link_flow_capacity_m3ps", "outfall_area_m2",
+                 "outfall_coefficient", "outfall_tailwater_head_m", "outfall_flow_capacity_m3ps",
+                 "link_invert_elevation_m", "link_diameter_m", "link_minor_loss_coefficient", "link_geometry_code",
+                 "link_rect_width_m", "link_rect_height_m"):
+        v = getattr(pp, name)
+        if v is not None:
+            out[f"{prefix}{name}"] = np.asarray(v)
+    return out
+
+
+def random_state(rng, n, wet_frac=0.7, hmax=0.6):
+    h = rng.uniform(0.0, hmax, n).astype(np.float32)
+    dry = rng.random(n) > wet_frac
+    h[dry] = 0.0
+    tiny = rng.random(n) < 0.05
+    h[tiny] = np.float32(3e-6)
+    u = rng.uniform(-1.5, 1.5, n).astype(np.float32)
+    v = rng.uniform(-1.5, 1.5, n).astype(np.float32)
+    return h, (h * u).astype(np.float32), (h * v).astype(np.float32)
+
+
+def grid_topology(tb, rng, n=12, mode="outflow", active_frac=0.85):
+    from floodgb.synthetic import grid_mesh
+
+    pts, tris = grid_mesh(n, 10.0 * n, 0.2, rng)
+    cen = pts[tris].mean(axis=1)
+    bed = (0.01 * cen[:, 0] + rng.normal(0, 0.05, len(tris))).astype(np.float32)
+    manning = rng.choice([0.015, 0.035, 0.06], len(tris)).astype(np.float32)
+    active = (rng.random(len(tris)) < active_frac).astype(np.float32)
+    return tb.build_triangular_surface_topology(pts, tris, bed, manning, active, mode), pts, tris
+
+
+def with_mixed_codes(tb, st, rng, stage):
+    code = np.array(st.boundary_code, copy=True)
+    ext = np.flatnonzero(np.asarray(st.edge_right_cell) < 0)
+    code[ext] = rng.choice([0, 1, 2, 3, 4], ext.size)
+    return tb.TriangularSurfaceTopology(
+        **{**st.__dict__, "boundary_code": code.astype(np.int32), "has_stage_boundary": True}
+    )
+
+
+def make_surface_cases(tb, stab):
+    rng = np.random.default_rng(20261203)
+    out = {}
+    cases = []
+    st, pts, tris = grid_topology(tb, rng)
+    out["topo_nodes"] = pts
+    out["topo_triangles"] = tris
+    out["topo_bed"] = np.asarray(st.bed_elevation_m)
+    out["topo_manning"] = np.asarray(st.manning_n)
+    out["topo_active"] = np.asarray(st.active_mask)
+    stage = float(np.mean(st.bed_elevation_m) + 0.25)
+    mixed = with_mixed_codes(tb, st, rng, stage)
+    cases.append(("mixed_scalar", mixed, stage, np.float32(50.0 / 3.6e6), np.float32(10.0 / 3.6e6), 0.7))
+    cases.append(("outflow_percell", st, None,
+                  (rng.uniform(0, 80, st.cell_count) / 3.6e6).astype(np.float32),
+                  (rng.uniform(0, 120, st.cell_count) / 3.6e6).astype(np.float32), 0.25))
+    st2, _, _ = grid_topology(tb, rng, n=10, mode="reflective", active_frac=1.0)
+    st2 = tb.TriangularSurfaceTopology(**{**st2.__dict__, "active_mask": None})
+    cases.append(("reflective_nomask", st2, None, np.float32(0.0), np.float32(0.0), 0.9))
+    st3, _, _ = grid_topology(tb, rng, n=10, mode="transmissive", active_frac=0.9)
+    cases.append(("transmissive_scalar", st3, None, np.float32(20.0 / 3.6e6), np.float32(0.0), 0.05))
+    names = []
+    for name, topo, stg, rain, infil, dt in cases:
+        h, hu, hv = random_state(rng, topo.cell_count)
+        state = tb.TriangularSurfaceState(h, hu, hv)
+        forcing = tb.TriangularSurfaceForcing(rainfall_rate_mps=rain, infiltration_capacity_mps=infil,
+                                              boundary_stage_m=stg)
+        new, diag = tb.step_triangular_surface(state, topo, forcing, dt)
+        assert new.h_m.dtype == np.float32
+        clamped = stab.clamp_velocity(new, 5.0, np)
+        p = f"{name}/"
+        out.update(topo_arrays(p, topo))
+        out[f"{p}stage"] = np.float64(stg if stg is not None else np.nan)
+        out[f"{p}h"], out[f"{p}hu"], out[f"{p}hv"] = h, hu, hv
+        out[f"{p}rain"] = np.asarray(rain)
+        out[f"{p}infil"] = np.asarray(infil)
+        out[f"{p}dt"] = np.float64(dt)
+        out[f"{p}h_out"], out[f"{p}hu_out"], out[f"{p}hv_out"] = new.h_m, new.hu_m2ps, new.hv_m2ps
+        out[f"{p}hu_clamped"], out[f"{p}hv_clamped"] = clamped.hu_m2ps, clamped.hv_m2ps
+        out[f"{p}diag"] = np.array([
+            float(diag.rainfall_input_m3), float(diag.infiltration_loss_m3), float(diag.boundary_net_flux_m3),
+            float(diag.boundary_inflow_m3), float(diag.boundary_outflow_m3), float(diag.final_surface_volume_m3),
+        ])
+        out[f"{p}dt_cfl"] = np.float64(tb.stable_triangular_timestep_s(topo, state, cfl=0.85))
+        names.append(name)
+    out["cases"] = np.array(names)
+    np.savez_compressed(OUT / "surface_cases.npz", **out)
+    return names
+
+
+def tiny_coupled(seed=5):
+    from floodgb.synthetic import make_coupled_city
+
+    t = 700
+    b = 60
+    e = (3 * t + b) // 2
+    return make_coupled_city(n_triangles=t, n_edges=e, n_active=560, n_nodes=90, n_links=104, n_inlets=70,
+                             n_outfalls=3, area_km2=0.25, seed=seed, duration_min=3.0)
+
+
+def make_pipe_cases(tb):
+    rng = np.random.default_rng(77)
+    sc = tiny_coupled()
+    topo = sc.city.topologies
+    st, cp, pp = topo.surface_topology, topo.coupling_topology, topo.pipe_topology
+    out = topo_arrays("mesh/", st)
+    variants = []
+    variants.append(("circular_orifice", pp, "orifice"))
+    variants.append(("circular_weir", pp, "weir_orifice"))
+    variants.append(("circular_capacity", pp, "capacity"))
+    variants.append(("circular_headlimited", pp, "head_limited_capacity"))
+    pre = tb.TriangularPipeNetworkTopology(**{**pp.__dict__, "link_diameter_m": None, "link_minor_loss_coefficient": None})
+    variants.append(("precomputed_orifice", pre, "orifice"))
+    L = pp.link_count
+    geom = np.where(rng.random(L) < 0.4, 2, 1).astype(np.int32)
+    inv = np.minimum(cp.node_invert_elevation_m[pp.link_from_node_index],
+                     cp.node_invert_elevation_m[pp.link_to_node_index]).astype(np.float32) + np.float32(0.05)
+    rect = tb.TriangularPipeNetworkTopology(**{
+        **pp.__dict__, "link_geometry_code": geom, "link_rect_width_m": rng.uniform(0.5, 2.0, L).astype(np.float32),
+        "link_rect_height_m": rng.uniform(0.4, 1.5, L).astype(np.float32), "link_invert_elevation_m": inv,
+        "outfall_flow_capacity_m3ps": np.full(cp.node_count, 0.3, np.float32)})
+    variants.append(("rect_invert_orifice", rect, "orifice"))
+    names = []
+    for name, pipe, rule in variants:
+        h = rng.uniform(0.0, 0.4, st.cell_count).astype(np.float32)
+        h[rng.random(st.cell_count) < 0.3] = 0.0
+        if st.active_mask is not None:
+            h = np.where(st.active_mask > 0.5, h, 0.0).astype(np.float32)
+        V = (cp.node_storage_area_m2.astype(np.float64) * cp.node_max_depth_m.astype(np.float64)
+             * rng.uniform(0.0, 1.3, cp.node_count))
+        Q = rng.uniform(-0.5, 0.5, pipe.link_count)
+        dt = 0.6
+        h_new, state, diag = tb.step_triangular_dynamic_pipe_network(
+            h, st, cp, pipe, tb.TriangularPipeNetworkState(V.copy(), Q.copy()), dt, inlet_capture_rule=rule)
+        p = f"{name}/"
+        out.update(coupling_arrays(p, cp, pipe))
+        out[f"{p}rule"] = np.array(rule)
+        out[f"{p}h"], out[f"{p}V"], out[f"{p}Q"], out[f"{p}dt"] = h, V, Q, np.float64(dt)
+        out[f"{p}h_out"] = np.asarray(h_new, dtype=np.float64)
+        out[f"{p}V_out"] = np.asarray(state.node_volume_m3)
+        out[f"{p}Q_out"] = np.asarray(state.link_flow_m3ps)
+        out[f"{p}diag"] = np.array([
+            float(diag.surface_capture_m3), float(diag.surface_surcharge_m3), float(diag.link_abs_flow_m3),
+            float(diag.outfall_discharge_m3), float(diag.overflow_surcharge_m3), float(diag.unreturned_overflow_m3),
+            float(diag.final_node_volume_m3),
+        ])
+        names.append(name)
+    out["cases"] = np.array(names)
+    np.savez_compressed(OUT / "pipe_cases.npz", **out)
+    return names
+
+
+def reference_run(tb, stab, pis, sc, max_steps, snapshot_interval_s):
+    """engine.py:219-344 restated on the reference's NumPy step functions."""
+
+    from floodgb.config import load_config
+
+    cfg = load_config(None, sc.overrides)
+    s = cfg.solver
+    topo = sc.city.topologies
+    st, cp, pp = topo.surface_topology, topo.coupling_topology, topo.pipe_topology
+    fields = sc.city.infiltration_fields
+    if fields is not None:
+        fields = pis.ProductionInfiltrationFields(
+            rainfall_multiplier=fields.rainfall_multiplier, horton_f0_mps=fields.horton_f0_mps,
+            horton_fc_mps=fields.horton_fc_mps, horton_k_per_s=fields.horton_k_per_s,
+            open_fraction=fields.open_fraction, active_mask=fields.active_mask)
+    mode = cfg.physics.infiltration_mode
+    state = tb.TriangularSurfaceState(np.array(topo.surface_state.h_m, np.float32),
+                                      np.array(topo.surface_state.hu_m2ps, np.float32),
+                                      np.array(topo.surface_state.hv_m2ps, np.float32))
+    pstate = tb.TriangularPipeNetworkState(np.array(topo.pipe_state.node_volume_m3, np.float64),
+                                           np.array(topo.pipe_state.link_flow_m3ps, np.float64))
+    wet = np.zeros(st.cell_count, np.float32)
+    final_t = (s.duration_min if s.duration_min is not None else sc.rainfall.duration_min) * 60.0
+    t = 0.0
+    step = 0
+    cached = None
+    next_snap = 0.0
+    snaps_t, snaps_h, snaps_hu, snaps_hv, snaps_v = [], [], [], [], []
+    cum = np.zeros(6)
+    has_drain = cp.node_count > 0
+    while t < final_t and step < max_steps:
+        if cached is None or step % s.cfl_update_interval_steps == 0:
+            dt = float(tb.stable_triangular_timestep_s(st, state, cfl=s.cfl))
+            cached = dt
+        else:
+            dt = cached * s.cfl_reuse_safety_factor
+        dt = min(dt, s.max_dt_s, final_t - t)
+        dt = max(dt, 1.0e-3)
+        base = sc.rainfall.rate_fn(t)
+        if mode == "production_horton" and fields is not None:
+            rain = pis.rainfall_rate_for_step(xp=np, base_rainfall_rate_mps=base, mode=mode, fields=fields)
+            infil = pis.build_infiltration_capacity_for_step(xp=np, mode=mode, wet_time_s=wet, fields=fields,
+                                                             fallback_capacity_mps=None)
+        else:
+            rain = np.float32(base)
+            infil = np.float32(0.0)
+        forcing = tb.TriangularSurfaceForcing(rainfall_rate_mps=rain, infiltration_capacity_mps=infil)
+        state, sd = tb.step_triangular_surface(state, st, forcing, timestep_s=dt)
+        state = stab.clamp_velocity(state, s.max_speed_mps, np)
+        od = us = 0.0
+        ov = 0.0
+        if has_drain:
+            h, pstate, pd = tb.step_triangular_dynamic_pipe_network(state.h_m, st, cp, pp, pstate, dt)
+            state = tb.TriangularSurfaceState(np.asarray(h, np.float32), state.hu_m2ps, state.hv_m2ps)
+            od, ov, us = float(pd.outfall_discharge_m3), float(pd.overflow_surcharge_m3), float(pd.unreturned_overflow_m3)
+        wet = wet + pis.wet_time_increment_s(xp=np, depth_m=state.h_m, dt_s=dt, min_depth_m=1e-5)
+        cum += [float(sd.rainfall_input_m3), float(sd.infiltration_loss_m3), float(sd.boundary_net_flux_m3), od, ov, us]
+        t += dt
+        step += 1
+        if t >= next_snap or t >= final_t:
+            snaps_t.append(t)
+            snaps_h.append(np.array(state.h_m, np.float32))
+            snaps_hu.append(np.array(state.hu_m2ps, np.float32))
+            snaps_hv.append(np.array(state.hv_m2ps, np.float32))
+            snaps_v.append(np.array(pstate.node_volume_m3, np.float32))
+            next_snap += snapshot_interval_s
+    return dict(step_count=np.int64(step), t_end=np.float64(t), snap_t=np.array(snaps_t), snap_h=np.array(snaps_h),
+                snap_hu=np.array(snaps_hu), snap_hv=np.array(snaps_hv),
+                snap_v=np.array(snaps_v) if has_drain else np.zeros((len(snaps_t), 0), np.float32),
+                ledger=cum, final_V=np.asarray(pstate.node_volume_m3), final_Q=np.asarray(pstate.link_flow_m3ps),
+                wet_time=wet)
+
+
+def scenario_arrays(prefix, sc):
+    """Every input array of a scenario, so tests can rebuild it without the generator."""
+
+    topo = sc.city.topologies
+    out = topo_arrays(prefix + "mesh/", topo.surface_topology)
+    out.update(coupling_arrays(prefix + "net/", topo.coupling_topology, topo.pipe_topology))
+    out[prefix + "h0"] = np.asarray(topo.surface_state.h_m, np.float32)
+    out[prefix + "hu0"] = np.asarray(topo.surface_state.hu_m2ps, np.float32)
+    out[prefix + "hv0"] = np.asarray(topo.surface_state.hv_m2ps, np.float32)
+    out[prefix + "V0"] = np.asarray(topo.pipe_state.node_volume_m3, np.float64)
+    out[prefix + "Q0"] = np.asarray(topo.pipe_state.link_flow_m3ps, np.float64)
+    out[prefix + "centroids"] = np.asarray(sc.city.mesh.centroids_xy)
+    f = sc.city.infiltration_fields
+    if f is not None:
+        out[prefix + "rain_mult"] = f.rainfall_multiplier
+        out[prefix + "f0"] = f.horton_f0_mps
+        out[prefix + "fc"] = f.horton_fc_mps
+        out[prefix + "k"] = f.horton_k_per_s
+    r = sc.rainfall
+    out[prefix + "hyeto"] = np.stack([r.start_min, r.end_min, r.intensity_mmhr])
+    out[prefix + "overrides"] = np.array(repr(sorted(sc.overrides.items())))
+    return out
+
+
+def make_run_cases(tb, stab, pis):
+    from floodgb.synthetic import make_grid_city
+
+    out = {}
+    sc = tiny_coupled(seed=9)
+    sc.overrides["solver.snapshot_interval_min"] = 0.5
+    sc.overrides["solver.duration_min"] = 3.0
+    # a wetter start so drainage, Horton decay and the clamp all act
+    st = sc.city.topologies.surface_topology
+    rng = np.random.default_rng(11)
+    h0 = np.where(st.active_mask > 0.5, rng.uniform(0, 0.3, st.cell_count), 0).astype(np.float32)
+    topo = sc.city.topologies
+    topo.surface_state = tb.TriangularSurfaceState(h0, np.zeros_like(h0), np.zeros_like(h0))
+    out.update(scenario_arrays("coupled/", sc))
+    res = reference_run(tb, stab, pis, sc, max_steps=400, snapshot_interval_s=30.0)
+    out.update({f"coupled/{k}": v for k, v in res.items()})
+    gsc = make_grid_city(n=20, size_m=200.0, seed=4, rain_mmhr=80.0, duration_min=4.0)
+    gsc.overrides["solver.snapshot_interval_min"] = 1.0
+    out.update(scenario_arrays("grid/", gsc))
+    res = reference_run(tb, stab, pis, gsc, max_steps=100000, snapshot_interval_s=60.0)
+    out.update({f"grid/{k}": v for k, v in res.items()})
+    np.savez_compressed(OUT / "run_cases.npz", **out)
+
+
+def main():
+    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    tb, stab, pis = import_reference(ref)
+    print("surface:", make_surface_cases(tb, stab))
+    print("pipe:", make_pipe_cases(tb))
+    make_run_cases(tb, stab, pis)
+    for f in sorted(OUT.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()
