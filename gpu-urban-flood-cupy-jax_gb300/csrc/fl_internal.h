@@ -1,0 +1,186 @@
+// Internal layout and control structures shared by the host runtime
+// (fl_solver.cpp, fl_plan.cpp) and the kernels (fl_surface.cu, fl_drainage.cu).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace fl {
+
+// ---------------------------------------------------------------------------
+// Per-cell "slot" words.  A triangle has up to three edges; slot k of cell c
+// describes the k-th edge in the reference's cell_edge_indices order (edges
+// the cell is left of, ascending, then edges it is right of, ascending).
+//   bits  0..26  other cell (renumbered index), NO_CELL for an exterior edge
+//   bit   27     other cell is active
+//   bits 28..30  the edge's boundary_code + 1 (0 = interior code -1)
+//   bit   31     this cell is the edge's right cell
+// SLOT_NONE marks an unused slot.
+// ---------------------------------------------------------------------------
+constexpr uint32_t SLOT_NONE = 0xFFFFFFFFu;
+constexpr uint32_t IDX_MASK = 0x07FFFFFFu;
+constexpr uint32_t NO_CELL = 0x07FFFFFFu;
+constexpr uint32_t OTHER_ACTIVE_BIT = 1u << 27;
+constexpr int CODE_SHIFT = 28;
+constexpr uint32_t RIGHT_BIT = 1u << 31;
+constexpr int64_t MAX_CELLS = 0x07FFFFFE;
+
+// topo[c].w bits
+constexpr uint32_t CELL_ACTIVE = 1u;
+constexpr uint32_t CELL_COUPLED = 2u;       // drainage writes this cell's final depth
+constexpr uint32_t CELL_STAGE_LEDGER = 4u;  // inactive cell left of an exterior stage edge
+
+// Per-step control, double-buffered by launch slot.  Written by the planner
+// (one thread) of the previous launch, read by every kernel of the step.
+struct StepCtrl {
+    double t0;        // simulated time at the start of the step
+    double dt;        // float64 step length (the reference's Python float dt)
+    float dt_f;       // float32(dt): what the kernels multiply by
+    float dtg_f;      // float32(dt * g): the Manning term's Python-float product
+    float rain_f;     // float32(base rainfall rate at t0)
+    float pad0;
+    int32_t active;   // 0: the step is a no-op
+    int32_t parity;   // state buffer holding the input state
+    int32_t snap_slot;     // >= 0: the step's end state is snapshot slot k
+    int32_t check_finite;  // check the input depth for non-finite values
+    int32_t phases;
+    int32_t pad1;
+    int64_t step;     // index of this step (0-based)
+};
+
+// Run control: advanced only by the planner.
+struct RunCtrl {
+    double t;             // time at the start of the next step to plan
+    double cached_dt;     // float64 of the last CFL minimum; < 0 before the first
+    double next_snap_t;
+    double final_t;
+    double stop_t;        // fl_run pause target
+    double max_dt, safety, snap_interval, g;
+    double last_dt;
+    int64_t step;         // steps planned (active)
+    int64_t max_step;     // planner stops at this step count
+    int64_t cfl_evals, cfl_reused;
+    int64_t error_step;
+    int32_t parity;       // buffer holding the latest state
+    int32_t snap_count, max_snaps;
+    int32_t error;        // sticky FL_E_* code (written with atomicCAS)
+    int32_t cfl_interval, finite_interval;
+    int32_t hyeto_n;
+    int32_t pad;
+};
+
+struct HyetoView {
+    const double *start_s, *end_s, *rate;
+    int32_t n;
+};
+
+// Ledger slots of the per-block running sums.
+constexpr int SURF_TERMS = 4;   // rain, infil, boundary in, boundary out
+constexpr int D1_TERMS = 2;     // capture, surcharge
+constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer|
+
+struct SurfArgs {
+    const uint4 *topo;
+    const float4 *g0, *g1, *g2;   // {nx, ny, len, manning}, {.., area}, {.., 0}
+    const float4 *horton;         // {f0, fc, k, rain multiplier} (kind 1)
+    float *wet;                   // wet time (kind 1)
+    float4 *state0, *state1;      // {h, hu, hv, bed}
+    StepCtrl *ctrl;
+    RunCtrl *run;
+    HyetoView hy;
+    double *ledger;               // [gridDim.x * SURF_TERMS]
+    float *snap_h, *snap_hu, *snap_hv;
+    double *snap_t;
+    int32_t C;
+    int32_t forcing_kind;
+    float infil_scalar;
+    float g, half_g, md, vmax, stage;
+    int32_t has_stage;
+};
+
+struct DtArgs {
+    const float4 *state0, *state1;
+    const float *char_len;
+    StepCtrl *ctrl;
+    RunCtrl *run;
+    HyetoView hy;
+    float *partial;               // [gridDim.x]
+    unsigned int *counter;
+    double *snap_t;
+    int32_t C;
+    float cfl, g, md;
+    double *dt_out;               // optional: fl_stable_timestep result
+};
+
+struct D1Args {
+    // inlets sorted by (renumbered) cell
+    const int32_t *in_cell, *in_node, *in_kcell;
+    const float4 *in_par;         // {bed - invert offset, capture cap * 1, surcharge cap, unused}
+    const int32_t *kcell_cell, *kcell_start;   // inlet cells and their inlet ranges
+    const int32_t *node_in_start, *node_in_list;
+    const float *node_area;
+    const float4 *g1;             // cell area in .w
+    const float4 *state0, *state1;
+    float *hc_out;                // depth of each inlet cell after the exchange
+    const float2 *Va;             // node volume (float-float) before
+    float2 *Vb;                   // after the exchange
+    StepCtrl *ctrl;
+    double *ledger;               // [gridDim.x * D1_TERMS]
+    int32_t K, N;
+    int32_t rule;
+    float coef_area;              // float32(Cd * A_orifice)
+    float weir_coef_perim;        // float32(Cw * perimeter) for weir_orifice
+    float g2;                     // 2 g (float32)
+};
+
+struct D2Args {
+    const int32_t *grp_cell, *grp_kcell, *grp_start, *grp_nodes;
+    const int32_t *node_link_start, *node_link_list;
+    const int32_t *link_from, *link_to;
+    const float4 *lk0;            // {length, from-to invert difference, depth offset, manning n}
+    const float4 *lk1;            // {diameter (0: none), area, hydraulic radius, minor loss}
+    const float4 *lk2;            // {flow capacity (inf: none), rect width, rect height, geometry code}
+    const float4 *nd0;            // {storage area, outfall head offset, Cd*A outfall, outfall capacity}
+    const float *nd_capv;         // storage area * max(max depth, 0)
+    const float4 *g1;
+    float4 *state0, *state1;
+    const float *hc_out;
+    const float2 *Vb;             // after the inlet exchange
+    float2 *Va;                   // final
+    float *Q0, *Q1;               // link flow, ping-pong with the state parity
+    float *wet;
+    float *snap_h, *snap_v;
+    StepCtrl *ctrl;
+    double *ledger;               // [gridDim.x * D2_TERMS]
+    int32_t G, C, N;
+    int32_t forcing_kind;
+    float g, md, wave_speed;
+};
+
+// Host-side renumbered layout (fl_plan.cpp).
+struct HostLayout {
+    int32_t C = 0, E = 0, N = 0, L = 0, I = 0, K = 0, G = 0;
+    std::vector<int32_t> perm;        // perm[new] = reference cell
+    std::vector<int32_t> inv;         // inv[reference] = new
+    std::vector<uint4> topo;
+    std::vector<float4> g0, g1, g2;
+    std::vector<float> char_len;
+    std::vector<float> bed;
+    int64_t slots_used = 0;
+    // drainage
+    std::vector<int32_t> in_cell, in_node, in_kcell, in_order; // in_order[new inlet] = reference inlet
+    std::vector<float4> in_par;
+    std::vector<int32_t> kcell_cell, kcell_start;
+    std::vector<int32_t> node_in_start, node_in_list;
+    std::vector<float> node_area, nd_capv;
+    std::vector<float4> nd0;
+    std::vector<int32_t> grp_cell, grp_kcell, grp_start, grp_nodes;
+    std::vector<int32_t> node_link_start, node_link_list;
+    std::vector<int32_t> link_from, link_to;
+    std::vector<float4> lk0, lk1, lk2;
+    int32_t max_inlets_per_cell = 0;
+};
+
+}  // namespace fl

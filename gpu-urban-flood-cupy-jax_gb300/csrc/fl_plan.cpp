@@ -1,0 +1,355 @@
+// Host-side layout builder: validates the reference-layout inputs, renumbers
+// cells along a Hilbert curve of their centroids, packs each cell's three
+// edges into slot words + float4 geometry, and builds the CSR tables the
+// drainage kernels gather over.  Pure C++ (no CUDA calls), so it also runs
+// through fl_plan_check on machines without a GPU.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <limits>
+#include <numeric>
+#include <string>
+
+#include "../../include/floodgb.h"
+#include "fl_internal.h"
+
+namespace fl {
+
+int set_error(int code, const char *fmt, ...);
+
+namespace {
+
+// Hilbert index of (x, y) on a 2^16 x 2^16 grid.
+uint64_t hilbert_d(uint32_t x, uint32_t y) {
+    const uint32_t n = 1u << 16;
+    uint64_t d = 0;
+    for (uint32_t s = n / 2; s > 0; s /= 2) {
+        const uint32_t rx = (x & s) > 0;
+        const uint32_t ry = (y & s) > 0;
+        d += (uint64_t)s * (uint64_t)s * ((3 * rx) ^ ry);
+        if (ry == 0) {
+            if (rx == 1) {
+                x = s - 1 - x;
+                y = s - 1 - y;
+            }
+            std::swap(x, y);
+        }
+    }
+    return d;
+}
+
+float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+
+}  // namespace
+
+int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) {
+    const int64_t C = m.cell_count, E = m.edge_count;
+    if (C <= 0 || E <= 0) return set_error(FL_E_INVALID, "mesh needs cell_count > 0 and edge_count > 0");
+    if (C > MAX_CELLS) return set_error(FL_E_INVALID, "mesh has %lld cells; the limit is %lld", (long long)C, (long long)MAX_CELLS);
+    if (!m.bed_elevation_m || !m.manning_n || !m.cell_area_m2 || !m.characteristic_length_m || !m.edge_left_cell ||
+        !m.edge_right_cell || !m.boundary_code || !m.edge_normal_x || !m.edge_normal_y || !m.edge_length_m)
+        return set_error(FL_E_INVALID, "mesh descriptor has a NULL required array");
+    L.C = (int32_t)C;
+    L.E = (int32_t)E;
+    std::vector<uint8_t> active(C, 1);
+    if (m.active_mask) {
+        for (int64_t c = 0; c < C; ++c) {
+            const float a = m.active_mask[c];
+            if (a != 0.0f && a != 1.0f)
+                return set_error(FL_E_UNSUPPORTED, "active_mask must hold 0/1 values (cell %lld has %g)", (long long)c, (double)a);
+            active[c] = a > 0.5f;
+        }
+    }
+    // incidences: left ones (ascending edge), then right ones (ascending edge)
+    std::vector<uint8_t> count(C, 0);
+    std::vector<int32_t> inc(C * 3, -1);
+    std::vector<uint8_t> inc_right(C * 3, 0);
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int64_t e = 0; e < E; ++e) {
+            const int32_t l = m.edge_left_cell[e], r = m.edge_right_cell[e];
+            if (pass == 0) {
+                if (l < 0 || l >= C) return set_error(FL_E_INVALID, "edge_left_cell[%lld] = %d is out of range", (long long)e, l);
+                if (r < -1 || r >= C) return set_error(FL_E_INVALID, "edge_right_cell[%lld] = %d is out of range", (long long)e, r);
+                if (r == l) return set_error(FL_E_INVALID, "edge %lld has the same left and right cell", (long long)e);
+                const int32_t code = m.boundary_code[e];
+                if (code < -1 || code > 4) return set_error(FL_E_INVALID, "Unsupported triangular boundary code %d on edge %lld.", code, (long long)e);
+                if (!(m.edge_length_m[e] > 0.0f)) return set_error(FL_E_INVALID, "edge %lld has a non-positive length", (long long)e);
+            }
+            const int32_t c = pass == 0 ? l : r;
+            if (c < 0) continue;
+            if (count[c] >= 3)
+                return set_error(FL_E_INVALID, "triangular topology contains a cell with more than three edges (cell %d)", c);
+            inc[c * 3 + count[c]] = (int32_t)e;
+            inc_right[c * 3 + count[c]] = (uint8_t)pass;
+            count[c]++;
+        }
+    }
+    for (int64_t c = 0; c < C; ++c) {
+        if (!(m.cell_area_m2[c] > 0.0f)) return set_error(FL_E_INVALID, "cell %lld has a non-positive area", (long long)c);
+    }
+
+    // renumbering
+    L.perm.resize(C);
+    std::iota(L.perm.begin(), L.perm.end(), 0);
+    if (m.centroid_x && m.centroid_y) {
+        double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
+        for (int64_t c = 0; c < C; ++c) {
+            xmin = std::min(xmin, (double)m.centroid_x[c]);
+            xmax = std::max(xmax, (double)m.centroid_x[c]);
+            ymin = std::min(ymin, (double)m.centroid_y[c]);
+            ymax = std::max(ymax, (double)m.centroid_y[c]);
+        }
+        const double span = std::max(std::max(xmax - xmin, ymax - ymin), 1e-9);
+        std::vector<uint64_t> key(C);
+        for (int64_t c = 0; c < C; ++c) {
+            const double fx = (m.centroid_x[c] - xmin) / span, fy = (m.centroid_y[c] - ymin) / span;
+            const uint32_t qx = (uint32_t)std::min(65535.0, std::max(0.0, fx * 65535.0));
+            const uint32_t qy = (uint32_t)std::min(65535.0, std::max(0.0, fy * 65535.0));
+            key[c] = hilbert_d(qx, qy);
+        }
+        std::stable_sort(L.perm.begin(), L.perm.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+    }
+    L.inv.resize(C);
+    for (int64_t i = 0; i < C; ++i) L.inv[L.perm[i]] = (int32_t)i;
+
+    // coupled cells (drainage finishes their depth)
+    std::vector<uint8_t> coupled(C, 0);
+    if (d) {
+        for (int32_t i = 0; i < d->inlet_count; ++i) {
+            const int32_t c = d->inlet_cell_index[i];
+            if (c >= 0 && c < C) coupled[c] = 1;
+        }
+        for (int32_t n = 0; n < d->node_count; ++n) {
+            const int32_t c = d->node_surface_cell_index[n];
+            if (c >= 0 && c < C) coupled[c] = 1;
+        }
+    }
+
+    L.topo.resize(C);
+    L.g0.resize(C);
+    L.g1.resize(C);
+    L.g2.resize(C);
+    L.char_len.resize(C);
+    L.bed.resize(C);
+    L.slots_used = 0;
+    for (int64_t i = 0; i < C; ++i) {
+        const int32_t c = L.perm[i];
+        uint32_t w[3] = {SLOT_NONE, SLOT_NONE, SLOT_NONE};
+        float4 g[3] = {f4(0, 0, 0, 0), f4(0, 0, 0, 0), f4(0, 0, 0, 0)};
+        bool stage_ledger = false;
+        for (int k = 0; k < count[c]; ++k) {
+            const int32_t e = inc[c * 3 + k];
+            const bool is_right = inc_right[c * 3 + k] != 0;
+            const int32_t other_ref = is_right ? m.edge_left_cell[e] : m.edge_right_cell[e];
+            uint32_t word = 0;
+            if (other_ref < 0) {
+                word = NO_CELL;
+            } else {
+                word = (uint32_t)L.inv[other_ref];
+                if (active[other_ref]) word |= OTHER_ACTIVE_BIT;
+            }
+            word |= (uint32_t)(m.boundary_code[e] + 1) << CODE_SHIFT;
+            if (is_right) word |= RIGHT_BIT;
+            w[k] = word;
+            g[k] = f4(m.edge_normal_x[e], m.edge_normal_y[e], m.edge_length_m[e], 0.0f);
+            if (!active[c] && !is_right && other_ref < 0 && m.boundary_code[e] == 3 && m.has_stage_boundary)
+                stage_ledger = true;
+            L.slots_used++;
+        }
+        uint32_t info = 0;
+        if (active[c]) info |= CELL_ACTIVE;
+        if (coupled[c]) info |= CELL_COUPLED;
+        if (stage_ledger) info |= CELL_STAGE_LEDGER;
+        L.topo[i] = make_uint4(w[0], w[1], w[2], info);
+        g[0].w = m.manning_n[c];
+        g[1].w = m.cell_area_m2[c];
+        g[2].w = 0.0f;
+        L.g0[i] = g[0];
+        L.g1[i] = g[1];
+        L.g2[i] = g[2];
+        L.char_len[i] = m.characteristic_length_m[c];
+        L.bed[i] = m.bed_elevation_m[c];
+    }
+    return FL_OK;
+}
+
+int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L) {
+    const int32_t N = d.node_count, NL = d.link_count, I = d.inlet_count, C = L.C;
+    if (N < 0 || NL < 0 || I < 0) return set_error(FL_E_INVALID, "negative drainage counts");
+    if (N == 0 && (NL > 0 || I > 0)) return set_error(FL_E_INVALID, "links or inlets need nodes");
+    L.N = N;
+    L.L = NL;
+    L.I = I;
+    if (N == 0) return FL_OK;
+    if (!d.node_surface_cell_index || !d.node_invert_elevation_m || !d.node_storage_area_m2 || !d.node_max_depth_m)
+        return set_error(FL_E_INVALID, "drainage descriptor has a NULL required node array");
+    if (I > 0 && (!d.inlet_cell_index || !d.inlet_node_index))
+        return set_error(FL_E_INVALID, "drainage descriptor has a NULL inlet index array");
+    if (NL > 0 && (!d.link_from_node_index || !d.link_to_node_index || !d.link_length_m || !d.link_area_m2 ||
+                   !d.link_hydraulic_radius_m || !d.link_manning_n))
+        return set_error(FL_E_INVALID, "drainage descriptor has a NULL required link array");
+    if (d.inlet_capture_rule < 0 || d.inlet_capture_rule > 3)
+        return set_error(FL_E_INVALID, "inlet_capture_rule must be 'orifice', 'weir_orifice', 'capacity', or 'head_limited_capacity'.");
+    for (int32_t n = 0; n < N; ++n) {
+        const int32_t c = d.node_surface_cell_index[n];
+        if (c >= C) return set_error(FL_E_INVALID, "node_surface_cell_index[%d] = %d is out of range", n, c);
+    }
+    const float INF = std::numeric_limits<float>::infinity();
+
+    // inlets sorted by renumbered cell (stable in reference order)
+    std::vector<int32_t> order(I);
+    std::iota(order.begin(), order.end(), 0);
+    for (int32_t i = 0; i < I; ++i) {
+        const int32_t c = d.inlet_cell_index[i], n = d.inlet_node_index[i];
+        if (c < 0 || c >= C) return set_error(FL_E_INVALID, "inlet_cell_index[%d] = %d is out of range", i, c);
+        if (n < 0 || n >= N) return set_error(FL_E_INVALID, "inlet_node_index[%d] = %d is out of range", i, n);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+        return L.inv[d.inlet_cell_index[a]] < L.inv[d.inlet_cell_index[b]];
+    });
+    L.in_order = order;
+    L.in_cell.resize(I);
+    L.in_node.resize(I);
+    L.in_kcell.resize(I);
+    L.in_par.resize(I);
+    L.kcell_cell.clear();
+    L.kcell_start.clear();
+    L.max_inlets_per_cell = 0;
+    for (int32_t j = 0; j < I; ++j) {
+        const int32_t i = order[j];
+        const int32_t cref = d.inlet_cell_index[i], n = d.inlet_node_index[i];
+        const int32_t c = L.inv[cref];
+        if (L.kcell_cell.empty() || L.kcell_cell.back() != c) {
+            L.kcell_cell.push_back(c);
+            L.kcell_start.push_back(j);
+        }
+        L.in_cell[j] = c;
+        L.in_node[j] = n;
+        L.in_kcell[j] = (int32_t)L.kcell_cell.size() - 1;
+        const double off = (double)m.bed_elevation_m[cref] - (double)d.node_invert_elevation_m[n];
+        const float capc = d.inlet_capture_capacity_m3ps ? std::max(d.inlet_capture_capacity_m3ps[i], 0.0f) : INF;
+        const float surc = d.inlet_surcharge_capacity_m3ps ? std::max(d.inlet_surcharge_capacity_m3ps[i], 0.0f) : INF;
+        L.in_par[j] = f4((float)off, capc, surc, 0.0f);
+    }
+    L.kcell_start.push_back(I);
+    L.K = (int32_t)L.kcell_cell.size();
+    for (int32_t k = 0; k < L.K; ++k)
+        L.max_inlets_per_cell = std::max(L.max_inlets_per_cell, L.kcell_start[k + 1] - L.kcell_start[k]);
+
+    // inlets per node (CSR over the sorted inlet order)
+    L.node_in_start.assign(N + 1, 0);
+    for (int32_t j = 0; j < I; ++j) L.node_in_start[L.in_node[j] + 1]++;
+    for (int32_t n = 0; n < N; ++n) L.node_in_start[n + 1] += L.node_in_start[n];
+    L.node_in_list.assign(I, 0);
+    {
+        std::vector<int32_t> fill(L.node_in_start.begin(), L.node_in_start.end() - 1);
+        for (int32_t j = 0; j < I; ++j) L.node_in_list[fill[L.in_node[j]]++] = j;
+    }
+
+    // node parameters
+    const bool has_outfall = d.outfall_area_m2 && d.outfall_coefficient && d.outfall_tailwater_head_m;
+    L.node_area.resize(N);
+    L.nd0.resize(N);
+    L.nd_capv.resize(N);
+    for (int32_t n = 0; n < N; ++n) {
+        const float A = d.node_storage_area_m2[n];
+        L.node_area[n] = A;
+        float off = 0.0f, ca = 0.0f, cap = INF;
+        if (has_outfall) {
+            off = (float)((double)d.node_invert_elevation_m[n] - (double)d.outfall_tailwater_head_m[n]);
+            ca = d.outfall_coefficient[n] * d.outfall_area_m2[n];
+            if (d.outfall_flow_capacity_m3ps) cap = std::max(d.outfall_flow_capacity_m3ps[n], 0.0f);
+        }
+        L.nd0[n] = f4(A, off, ca, cap);
+        L.nd_capv[n] = (float)((double)A * (double)std::max(d.node_max_depth_m[n], 0.0f));
+    }
+
+    // drainage groups: each coupled cell with the nodes that overflow into it,
+    // then orphan nodes (no surface cell)
+    std::vector<int32_t> node_cell_new(N, -1);
+    for (int32_t n = 0; n < N; ++n) {
+        const int32_t c = d.node_surface_cell_index[n];
+        node_cell_new[n] = c >= 0 ? L.inv[c] : -1;
+    }
+    std::vector<int32_t> nodes_by_cell(N);
+    std::iota(nodes_by_cell.begin(), nodes_by_cell.end(), 0);
+    std::stable_sort(nodes_by_cell.begin(), nodes_by_cell.end(), [&](int32_t a, int32_t b) {
+        const int32_t ca = node_cell_new[a] < 0 ? std::numeric_limits<int32_t>::max() : node_cell_new[a];
+        const int32_t cb = node_cell_new[b] < 0 ? std::numeric_limits<int32_t>::max() : node_cell_new[b];
+        return ca < cb;
+    });
+    L.grp_cell.clear();
+    L.grp_kcell.clear();
+    L.grp_start.clear();
+    L.grp_nodes.clear();
+    size_t ni = 0;   // cursor into nodes_by_cell
+    size_t ki = 0;   // cursor into kcell_cell (sorted)
+    while (true) {
+        int32_t next_node_cell = std::numeric_limits<int32_t>::max();
+        if (ni < nodes_by_cell.size() && node_cell_new[nodes_by_cell[ni]] >= 0) next_node_cell = node_cell_new[nodes_by_cell[ni]];
+        const int32_t next_k_cell = ki < L.kcell_cell.size() ? L.kcell_cell[ki] : std::numeric_limits<int32_t>::max();
+        const int32_t c = std::min(next_node_cell, next_k_cell);
+        if (c == std::numeric_limits<int32_t>::max()) break;
+        L.grp_cell.push_back(c);
+        L.grp_kcell.push_back(next_k_cell == c ? (int32_t)ki : -1);
+        if (next_k_cell == c) ++ki;
+        L.grp_start.push_back((int32_t)L.grp_nodes.size());
+        while (ni < nodes_by_cell.size() && node_cell_new[nodes_by_cell[ni]] == c) L.grp_nodes.push_back(nodes_by_cell[ni++]);
+    }
+    for (; ni < nodes_by_cell.size(); ++ni) {  // orphans
+        L.grp_cell.push_back(-1);
+        L.grp_kcell.push_back(-1);
+        L.grp_start.push_back((int32_t)L.grp_nodes.size());
+        L.grp_nodes.push_back(nodes_by_cell[ni]);
+    }
+    L.grp_start.push_back((int32_t)L.grp_nodes.size());
+    L.G = (int32_t)L.grp_cell.size();
+
+    // links
+    L.link_from.resize(NL);
+    L.link_to.resize(NL);
+    L.lk0.resize(NL);
+    L.lk1.resize(NL);
+    L.lk2.resize(NL);
+    L.node_link_start.assign(N + 1, 0);
+    const bool rect = d.link_geometry_code && d.link_rect_width_m && d.link_rect_height_m;
+    for (int32_t l = 0; l < NL; ++l) {
+        const int32_t f = d.link_from_node_index[l], t = d.link_to_node_index[l];
+        if (f < 0 || f >= N || t < 0 || t >= N)
+            return set_error(FL_E_INVALID, "link %d has a node index out of range", l);
+        L.link_from[l] = f;
+        L.link_to[l] = t;
+        const double invf = d.node_invert_elevation_m[f], invt = d.node_invert_elevation_m[t];
+        const double inv = d.link_invert_elevation_m ? (double)d.link_invert_elevation_m[l] : std::min(invf, invt);
+        L.lk0[l] = f4(d.link_length_m[l], (float)(invf - invt), (float)(0.5 * (invf + invt) - inv),
+                      std::max(d.link_manning_n[l], 0.0f));
+        const float km = d.link_minor_loss_coefficient ? std::max(d.link_minor_loss_coefficient[l], 0.0f) : 0.0f;
+        L.lk1[l] = f4(d.link_diameter_m ? d.link_diameter_m[l] : 0.0f, d.link_area_m2[l], d.link_hydraulic_radius_m[l], km);
+        int flags = 0;
+        if (d.link_diameter_m) flags |= 1;
+        float W = 0.0f, H = 0.0f;
+        if (rect && d.link_geometry_code[l] == 2) {
+            flags |= 2;
+            W = d.link_rect_width_m[l];
+            H = d.link_rect_height_m[l];
+        }
+        const float capq = d.link_flow_capacity_m3ps ? std::max(d.link_flow_capacity_m3ps[l], 0.0f) : INF;
+        L.lk2[l] = f4(capq, W, H, (float)flags);
+        L.node_link_start[f + 1]++;
+        if (t != f) L.node_link_start[t + 1]++;
+    }
+    for (int32_t n = 0; n < N; ++n) L.node_link_start[n + 1] += L.node_link_start[n];
+    L.node_link_list.assign(L.node_link_start[N], 0);
+    {
+        std::vector<int32_t> fill(L.node_link_start.begin(), L.node_link_start.end() - 1);
+        for (int32_t l = 0; l < NL; ++l) {
+            const int32_t f = L.link_from[l], t = L.link_to[l];
+            L.node_link_list[fill[f]++] = l;
+            if (t != f) L.node_link_list[fill[t]++] = l;
+        }
+    }
+    return FL_OK;
+}
+
+}  // namespace fl

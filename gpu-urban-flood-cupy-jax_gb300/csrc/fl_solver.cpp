@@ -1,0 +1,924 @@
+// Solver runtime behind the C ABI (include/floodgb.h): device memory, the
+// device-resident adaptive step loop as captured CUDA-graph chunks, state and
+// snapshot transfer, the ledger, and error reporting.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/floodgb.h"
+#include "fl_internal.h"
+
+namespace fl {
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_error;
+static std::atomic<int64_t> g_launches{0};
+
+int set_error(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L);
+int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L);
+
+// kernel launchers (fl_surface.cu / fl_drainage.cu)
+cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, cudaStream_t stream);
+int surface_blocks(int32_t C);
+cudaError_t launch_dt(const DtArgs &a, int blocks, int slot, int plan, cudaStream_t stream);
+cudaError_t launch_replan(RunCtrl *run, double *snap_t, HyetoView hy, StepCtrl *ctrl, int slot, cudaStream_t stream);
+cudaError_t launch_finite(const float4 *s0, const float4 *s1, RunCtrl *run, int32_t C, cudaStream_t stream);
+cudaError_t launch_load_state(float4 *state, const float *h, const float *hu, const float *hv, const float *bed,
+                              const int32_t *perm, int32_t C, int mask, cudaStream_t stream);
+cudaError_t launch_store_state(const float4 *state, float *h, float *hu, float *hv, const int32_t *perm, int32_t C,
+                               cudaStream_t stream);
+cudaError_t launch_permute_f32(const float *src, float *dst, const int32_t *perm, int32_t C, int to_reference,
+                               cudaStream_t stream);
+cudaError_t launch_f64_to_ff(const double *src, float2 *dst, int32_t n, cudaStream_t stream);
+cudaError_t launch_ff_to_f64(const float2 *src, double *dst, int32_t n, cudaStream_t stream);
+cudaError_t launch_f64_to_f32(const double *src, float *dst, int32_t n, cudaStream_t stream);
+cudaError_t launch_f32_to_f64(const float *src, double *dst, int32_t n, cudaStream_t stream);
+cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *g1, const float2 *V, RunCtrl *run,
+                           int32_t C, int32_t N, double *out2, cudaStream_t stream);
+cudaError_t launch_inlets(const D1Args &a, int slot, cudaStream_t stream);
+cudaError_t launch_network(const D2Args &a, int slot, cudaStream_t stream);
+int inlet_blocks(int32_t K, int32_t N);
+int network_blocks(int32_t G);
+
+}  // namespace fl
+
+using namespace fl;
+
+#define FL_CUDA(call)                                                                              \
+    do {                                                                                           \
+        cudaError_t _e = (call);                                                                   \
+        if (_e != cudaSuccess) return set_error(FL_E_CUDA, "%s: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+
+struct FlSolver {
+    int device = 0;
+    int32_t C = 0, N = 0, NL = 0, I = 0, K = 0, G = 0;
+    int kind = 0;
+    FlParams params{};
+    int dt_blocks = 0, surf_blocks = 0, d1_blocks = 0, d2_blocks = 0;
+    int chunk = 32;
+    std::vector<void *> allocs;
+    // device
+    int32_t *perm = nullptr;
+    std::vector<int32_t> perm_h;
+    float *bed = nullptr;
+    float4 *state[2] = {nullptr, nullptr};
+    float2 *Va = nullptr, *Vb = nullptr;
+    float *Q[2] = {nullptr, nullptr};
+    float *wet = nullptr;
+    StepCtrl *ctrl = nullptr;
+    RunCtrl *run = nullptr;
+    double *snap_t = nullptr;
+    float *snap_h = nullptr, *snap_hu = nullptr, *snap_hv = nullptr, *snap_v = nullptr;
+    double *led_s = nullptr, *led_1 = nullptr, *led_2 = nullptr;
+    double *dt_out = nullptr, *vol_out = nullptr;
+    float *stage_f[3] = {nullptr, nullptr, nullptr};
+    double *stage_d = nullptr;
+    SurfArgs sa{};
+    DtArgs da{};
+    D1Args d1{};
+    D2Args d2{};
+    HyetoView hy{};
+    // host
+    RunCtrl *run_h = nullptr;   // pinned mirror
+    RunCtrl *poll_h = nullptr;  // pinned, 2 slots
+    int slot = 0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    bool has_drain() const { return N > 0; }
+    int launches_per_step() const { return 1 + (has_drain() ? 2 : 0); }
+
+    template <class T>
+    int alloc(T **p, size_t count) {
+        if (count == 0) count = 1;
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, sizeof(T) * count);
+        if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * count, cudaGetErrorString(e));
+        allocs.push_back(q);
+        *p = (T *)q;
+        return FL_OK;
+    }
+    template <class T>
+    int upload(T **p, const std::vector<T> &v) {
+        int rc = alloc(p, v.size());
+        if (rc) return rc;
+        if (!v.empty()) FL_CUDA(cudaMemcpy(*p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+        return FL_OK;
+    }
+};
+
+static int sync_run(FlSolver *s, cudaStream_t st) {
+    FL_CUDA(cudaMemcpyAsync(s->run_h, s->run, sizeof(RunCtrl), cudaMemcpyDeviceToHost, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    return FL_OK;
+}
+
+static int push_run(FlSolver *s, cudaStream_t st) {
+    FL_CUDA(cudaMemcpyAsync(s->run, s->run_h, sizeof(RunCtrl), cudaMemcpyHostToDevice, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    return FL_OK;
+}
+
+// One step: [CFL reduction + plan] surface [inlets network]
+static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStream_t st) {
+    if (eval) {
+        FL_CUDA(launch_dt(s->da, s->dt_blocks, slot, 1, st));
+        g_launches++;
+    }
+    FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, st));
+    g_launches++;
+    if (s->has_drain()) {
+        FL_CUDA(launch_inlets(s->d1, slot, st));
+        FL_CUDA(launch_network(s->d2, slot, st));
+        g_launches += 2;
+    }
+    return FL_OK;
+}
+
+static int capture_graph(FlSolver *s) {
+    if (s->graph) return FL_OK;
+    cudaGraph_t g = nullptr;
+    FL_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const int interval = s->params.cfl_update_interval_steps;
+    int rc = FL_OK;
+    for (int j = 0; j < s->chunk && rc == FL_OK; ++j) {
+        const bool eval = (j % interval) == 0;
+        const bool next_eval = ((j + 1) % interval) == 0;
+        rc = launch_step(s, j & 1, eval, !next_eval, s->cap_stream);
+    }
+    cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+    if (rc != FL_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_error(FL_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_error(FL_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    // the launches above were captured, not executed
+    g_launches -= (int64_t)s->chunk * s->launches_per_step() + (s->chunk + interval - 1) / interval;
+    return FL_OK;
+}
+
+static int error_code_message(FlSolver *s) {
+    const RunCtrl &r = *s->run_h;
+    if (r.error == FL_E_NONFINITE)
+        return set_error(FL_E_NONFINITE,
+                         "Non-finite depth detected at step %lld (t=%.1f min). Lower solver.cfl_update_interval_steps "
+                         "or solver.cfl_reuse_safety_factor.",
+                         (long long)r.error_step, r.t / 60.0);
+    if (r.error == FL_E_SNAPSHOTS) return set_error(FL_E_SNAPSHOTS, "more than %d snapshots requested", r.max_snaps);
+    if (r.error == FL_E_INVALID) return set_error(FL_E_INVALID, "No finite cells are available for timestep calculation.");
+    if (r.error) return set_error(r.error, "device error %d at step %lld", r.error, (long long)r.error_step);
+    return FL_OK;
+}
+
+extern "C" {
+
+FL_API int fl_abi_version(void) { return FLOODGB_ABI_VERSION; }
+
+FL_API const char *fl_last_error(void) { return g_error.c_str(); }
+
+FL_API int64_t fl_launch_count(void) { return g_launches.load(); }
+
+FL_API int fl_device_count(int32_t *count) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) n = 0;
+    if (count) *count = n;
+    return FL_OK;
+}
+
+FL_API int fl_plan_check(const FlMeshDesc *mesh, const FlDrainDesc *drain, int64_t *stats, int32_t *perm_out) {
+    if (!mesh) return set_error(FL_E_INVALID, "mesh descriptor is NULL");
+    HostLayout L;
+    int rc = build_mesh_layout(*mesh, drain, L);
+    if (rc) return rc;
+    if (drain) {
+        rc = build_drain_layout(*mesh, *drain, L);
+        if (rc) return rc;
+    }
+    if (stats) {
+        stats[0] = L.C;
+        stats[1] = L.E;
+        stats[2] = L.slots_used;
+        stats[3] = L.K;
+        stats[4] = L.N;
+        stats[5] = L.L;
+        stats[6] = L.G;
+        stats[7] = L.max_inlets_per_cell;
+    }
+    if (perm_out) memcpy(perm_out, L.perm.data(), sizeof(int32_t) * L.perm.size());
+    return FL_OK;
+}
+
+FL_API void fl_destroy(FlSolver *s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    for (auto &e : s->ev)
+        if (e) cudaEventDestroy(e);
+    if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    for (void *p : s->allocs) cudaFree(p);
+    if (s->run_h) cudaFreeHost(s->run_h);
+    if (s->poll_h) cudaFreeHost(s->poll_h);
+    delete s;
+}
+
+static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcing,
+                       const FlParams *params, int32_t device, FlSolver *s) {
+    if (!mesh || !forcing || !params) return set_error(FL_E_INVALID, "fl_create needs mesh, forcing and params");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return set_error(FL_E_NO_DEVICE, "no CUDA device is visible; CPU fallback is disabled");
+    if (device < 0 || device >= ndev) return set_error(FL_E_NO_DEVICE, "device %d is not visible (%d devices)", device, ndev);
+    const FlParams &p = *params;
+    if (!(p.cfl > 0.0 && p.cfl <= 1.0)) return set_error(FL_E_INVALID, "solver.cfl must be in (0, 1]");
+    if (p.cfl_update_interval_steps < 1) return set_error(FL_E_INVALID, "cfl_update_interval_steps must be >= 1");
+    if (!(p.max_dt_s > 0.0)) return set_error(FL_E_INVALID, "max_dt_s must be positive");
+    if (!(p.duration_s > 0.0)) return set_error(FL_E_INVALID, "Simulation duration must be positive");
+    if (!(p.snapshot_interval_s > 0.0)) return set_error(FL_E_INVALID, "snapshot_interval_s must be positive");
+    if (p.max_snapshots < 1) return set_error(FL_E_INVALID, "max_snapshots must be >= 1");
+    if (forcing->kind != 0 && forcing->kind != 1) return set_error(FL_E_INVALID, "forcing kind must be 0 or 1");
+    if (forcing->kind == 1 && (!forcing->rain_multiplier || !forcing->horton_f0_mps || !forcing->horton_fc_mps ||
+                               !forcing->horton_k_per_s))
+        return set_error(FL_E_INVALID, "per-cell forcing needs rain_multiplier and Horton f0/fc/k arrays");
+    if (forcing->hyetograph_count < 0 || (forcing->hyetograph_count > 0 &&
+                                          (!forcing->hyeto_start_s || !forcing->hyeto_end_s || !forcing->hyeto_rate_mps)))
+        return set_error(FL_E_INVALID, "hyetograph arrays are missing");
+    s->device = device;
+    FL_CUDA(cudaSetDevice(device));
+    s->params = p;
+    s->kind = forcing->kind;
+
+    HostLayout L;
+    int rc = build_mesh_layout(*mesh, drain, L);
+    if (rc) return rc;
+    const bool with_drain = drain && drain->node_count > 0;
+    if (with_drain) {
+        rc = build_drain_layout(*mesh, *drain, L);
+        if (rc) return rc;
+    }
+    s->C = L.C;
+    s->perm_h = L.perm;
+    s->N = L.N;
+    s->NL = L.L;
+    s->I = L.I;
+    s->K = L.K;
+    s->G = L.G;
+    const int32_t C = s->C;
+
+    // static surface layout
+    uint4 *topo;
+    float4 *g0, *g1, *g2;
+    float *char_len;
+    if ((rc = s->upload(&topo, L.topo)) || (rc = s->upload(&g0, L.g0)) || (rc = s->upload(&g1, L.g1)) ||
+        (rc = s->upload(&g2, L.g2)) || (rc = s->upload(&char_len, L.char_len)) || (rc = s->upload(&s->bed, L.bed)) ||
+        (rc = s->upload(&s->perm, L.perm)))
+        return rc;
+    float4 *horton = nullptr;
+    if (s->kind == 1) {
+        std::vector<float4> hz(C);
+        for (int32_t i = 0; i < C; ++i) {
+            const int32_t r = L.perm[i];
+            hz[i] = make_float4(forcing->horton_f0_mps[r], forcing->horton_fc_mps[r], forcing->horton_k_per_s[r],
+                                forcing->rain_multiplier[r]);
+        }
+        if ((rc = s->upload(&horton, hz))) return rc;
+    }
+    if ((rc = s->alloc(&s->wet, C))) return rc;
+    FL_CUDA(cudaMemset(s->wet, 0, sizeof(float) * C));
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = s->alloc(&s->state[b], C))) return rc;
+    }
+    {
+        std::vector<float4> st0(C);
+        for (int32_t i = 0; i < C; ++i) st0[i] = make_float4(0.0f, 0.0f, 0.0f, L.bed[i]);
+        FL_CUDA(cudaMemcpy(s->state[0], st0.data(), sizeof(float4) * C, cudaMemcpyHostToDevice));
+        FL_CUDA(cudaMemcpy(s->state[1], st0.data(), sizeof(float4) * C, cudaMemcpyHostToDevice));
+    }
+    if ((rc = s->alloc(&s->ctrl, 2)) || (rc = s->alloc(&s->run, 1)) || (rc = s->alloc(&s->snap_t, p.max_snapshots)))
+        return rc;
+    FL_CUDA(cudaMemset(s->ctrl, 0, sizeof(StepCtrl) * 2));
+    const size_t snap_cells = (size_t)p.max_snapshots * (size_t)C;
+    if ((rc = s->alloc(&s->snap_h, snap_cells)) || (rc = s->alloc(&s->snap_hu, snap_cells)) ||
+        (rc = s->alloc(&s->snap_hv, snap_cells)) || (rc = s->alloc(&s->snap_v, (size_t)p.max_snapshots * (s->N > 0 ? s->N : 1))))
+        return rc;
+    // hyetograph
+    const int nh = forcing->hyetograph_count;
+    double *hy = nullptr;
+    if ((rc = s->alloc(&hy, 3 * (size_t)(nh > 0 ? nh : 1)))) return rc;
+    if (nh > 0) {
+        FL_CUDA(cudaMemcpy(hy, forcing->hyeto_start_s, sizeof(double) * nh, cudaMemcpyHostToDevice));
+        FL_CUDA(cudaMemcpy(hy + nh, forcing->hyeto_end_s, sizeof(double) * nh, cudaMemcpyHostToDevice));
+        FL_CUDA(cudaMemcpy(hy + 2 * nh, forcing->hyeto_rate_mps, sizeof(double) * nh, cudaMemcpyHostToDevice));
+    }
+    s->hy.start_s = hy;
+    s->hy.end_s = hy + nh;
+    s->hy.rate = hy + 2 * nh;
+    s->hy.n = nh;
+    // scratch
+    s->surf_blocks = surface_blocks(C);
+    int sms = 0;
+    FL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    s->dt_blocks = std::max(1, std::min(sms * 4, (C + 255) / 256));
+    float *dt_partial;
+    unsigned int *counter;
+    if ((rc = s->alloc(&dt_partial, s->dt_blocks)) || (rc = s->alloc(&counter, 1)) || (rc = s->alloc(&s->dt_out, 1)) ||
+        (rc = s->alloc(&s->vol_out, 2)) || (rc = s->alloc(&s->led_s, (size_t)s->surf_blocks * SURF_TERMS)))
+        return rc;
+    FL_CUDA(cudaMemset(counter, 0, sizeof(unsigned int)));
+    for (int b = 0; b < 3; ++b)
+        if ((rc = s->alloc(&s->stage_f[b], C))) return rc;
+    const size_t nd = std::max<size_t>((size_t)std::max(s->N, s->NL), 1);
+    if ((rc = s->alloc(&s->stage_d, nd))) return rc;
+
+    // drainage
+    if (with_drain) {
+        int32_t *in_cell, *in_node, *in_kcell, *kcell_cell, *kcell_start, *node_in_start, *node_in_list;
+        float4 *in_par, *nd0, *lk0, *lk1, *lk2;
+        float *node_area, *nd_capv;
+        int32_t *grp_cell, *grp_kcell, *grp_start, *grp_nodes, *nls, *nll, *lf, *lt;
+        if ((rc = s->upload(&in_cell, L.in_cell)) || (rc = s->upload(&in_node, L.in_node)) ||
+            (rc = s->upload(&in_kcell, L.in_kcell)) || (rc = s->upload(&in_par, L.in_par)) ||
+            (rc = s->upload(&kcell_cell, L.kcell_cell)) || (rc = s->upload(&kcell_start, L.kcell_start)) ||
+            (rc = s->upload(&node_in_start, L.node_in_start)) || (rc = s->upload(&node_in_list, L.node_in_list)) ||
+            (rc = s->upload(&node_area, L.node_area)) || (rc = s->upload(&nd0, L.nd0)) ||
+            (rc = s->upload(&nd_capv, L.nd_capv)) || (rc = s->upload(&grp_cell, L.grp_cell)) ||
+            (rc = s->upload(&grp_kcell, L.grp_kcell)) || (rc = s->upload(&grp_start, L.grp_start)) ||
+            (rc = s->upload(&grp_nodes, L.grp_nodes)) || (rc = s->upload(&nls, L.node_link_start)) ||
+            (rc = s->upload(&nll, L.node_link_list)) || (rc = s->upload(&lf, L.link_from)) ||
+            (rc = s->upload(&lt, L.link_to)) || (rc = s->upload(&lk0, L.lk0)) || (rc = s->upload(&lk1, L.lk1)) ||
+            (rc = s->upload(&lk2, L.lk2)))
+            return rc;
+        float *hc_out;
+        if ((rc = s->alloc(&s->Va, s->N)) || (rc = s->alloc(&s->Vb, s->N)) || (rc = s->alloc(&s->Q[0], s->NL)) ||
+            (rc = s->alloc(&s->Q[1], s->NL)) || (rc = s->alloc(&hc_out, s->K)))
+            return rc;
+        FL_CUDA(cudaMemset(s->Va, 0, sizeof(float2) * s->N));
+        FL_CUDA(cudaMemset(s->Vb, 0, sizeof(float2) * s->N));
+        FL_CUDA(cudaMemset(s->Q[0], 0, sizeof(float) * std::max(s->NL, 1)));
+        FL_CUDA(cudaMemset(s->Q[1], 0, sizeof(float) * std::max(s->NL, 1)));
+        s->d1_blocks = inlet_blocks(s->K, s->N);
+        s->d2_blocks = network_blocks(s->G);
+        if ((rc = s->alloc(&s->led_1, (size_t)s->d1_blocks * D1_TERMS)) ||
+            (rc = s->alloc(&s->led_2, (size_t)s->d2_blocks * D2_TERMS)))
+            return rc;
+        D1Args &a = s->d1;
+        a.in_cell = in_cell;
+        a.in_node = in_node;
+        a.in_kcell = in_kcell;
+        a.in_par = in_par;
+        a.kcell_cell = kcell_cell;
+        a.kcell_start = kcell_start;
+        a.node_in_start = node_in_start;
+        a.node_in_list = node_in_list;
+        a.node_area = node_area;
+        a.g1 = g1;
+        a.state0 = s->state[0];
+        a.state1 = s->state[1];
+        a.hc_out = hc_out;
+        a.Va = s->Va;
+        a.Vb = s->Vb;
+        a.ctrl = s->ctrl;
+        a.ledger = s->led_1;
+        a.K = s->K;
+        a.N = s->N;
+        a.rule = drain->inlet_capture_rule;
+        a.coef_area = drain->inlet_orifice_coefficient * drain->inlet_orifice_area_m2;
+        const float eq = sqrtf(4.0f * 3.14159265358979323846f * std::max(drain->inlet_orifice_area_m2, 0.0f));
+        const float perim = drain->inlet_weir_perimeter_m > 0.0f ? drain->inlet_weir_perimeter_m : eq;
+        a.weir_coef_perim = drain->inlet_weir_coefficient * std::max(perim, 0.0f);
+        a.g2 = (float)(2.0 * (double)(float)p.gravity_mps2);
+        D2Args &b = s->d2;
+        b.grp_cell = grp_cell;
+        b.grp_kcell = grp_kcell;
+        b.grp_start = grp_start;
+        b.grp_nodes = grp_nodes;
+        b.node_link_start = nls;
+        b.node_link_list = nll;
+        b.link_from = lf;
+        b.link_to = lt;
+        b.lk0 = lk0;
+        b.lk1 = lk1;
+        b.lk2 = lk2;
+        b.nd0 = nd0;
+        b.nd_capv = nd_capv;
+        b.g1 = g1;
+        b.state0 = s->state[0];
+        b.state1 = s->state[1];
+        b.hc_out = hc_out;
+        b.Vb = s->Vb;
+        b.Va = s->Va;
+        b.Q0 = s->Q[0];
+        b.Q1 = s->Q[1];
+        b.wet = s->wet;
+        b.snap_h = s->snap_h;
+        b.snap_v = s->snap_v;
+        b.ctrl = s->ctrl;
+        b.ledger = s->led_2;
+        b.G = s->G;
+        b.C = C;
+        b.N = s->N;
+        b.forcing_kind = s->kind;
+        b.g = (float)p.gravity_mps2;
+        b.md = (float)p.min_depth_m;
+        b.wave_speed = drain->pressurized_wave_speed_mps;
+    }
+    SurfArgs &a = s->sa;
+    a.topo = topo;
+    a.g0 = g0;
+    a.g1 = g1;
+    a.g2 = g2;
+    a.horton = horton;
+    a.wet = s->wet;
+    a.state0 = s->state[0];
+    a.state1 = s->state[1];
+    a.ctrl = s->ctrl;
+    a.run = s->run;
+    a.hy = s->hy;
+    a.ledger = s->led_s;
+    a.snap_h = s->snap_h;
+    a.snap_hu = s->snap_hu;
+    a.snap_hv = s->snap_hv;
+    a.snap_t = s->snap_t;
+    a.C = C;
+    a.forcing_kind = s->kind;
+    a.infil_scalar = forcing->infiltration_mps;
+    a.g = (float)p.gravity_mps2;
+    a.half_g = (float)(0.5 * p.gravity_mps2);
+    a.md = (float)p.min_depth_m;
+    a.vmax = (float)p.max_speed_mps;
+    a.stage = mesh->has_stage_boundary ? mesh->boundary_stage_m : 0.0f;
+    a.has_stage = mesh->has_stage_boundary;
+    DtArgs &d = s->da;
+    d.state0 = s->state[0];
+    d.state1 = s->state[1];
+    d.char_len = char_len;
+    d.ctrl = s->ctrl;
+    d.run = s->run;
+    d.hy = s->hy;
+    d.partial = dt_partial;
+    d.counter = counter;
+    d.snap_t = s->snap_t;
+    d.C = C;
+    d.cfl = (float)p.cfl;
+    d.g = (float)p.gravity_mps2;
+    d.md = (float)p.min_depth_m;
+    d.dt_out = nullptr;
+
+    // host side
+    FL_CUDA(cudaHostAlloc((void **)&s->run_h, sizeof(RunCtrl), cudaHostAllocDefault));
+    FL_CUDA(cudaHostAlloc((void **)&s->poll_h, 2 * sizeof(RunCtrl), cudaHostAllocDefault));
+    memset(s->run_h, 0, sizeof(RunCtrl));
+    FL_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+    FL_CUDA(cudaEventCreateWithFlags(&s->ev[0], cudaEventDisableTiming));
+    FL_CUDA(cudaEventCreateWithFlags(&s->ev[1], cudaEventDisableTiming));
+    const int interval = p.cfl_update_interval_steps;
+    s->chunk = interval % 2 == 0 ? interval : 2 * interval;
+    while (s->chunk < 16) s->chunk *= 2;  // short CFL cycles: several per graph
+    FL_CUDA(cudaDeviceSynchronize());
+    return fl_reset_clock(s, nullptr);
+}
+
+FL_API int fl_create(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcing,
+                     const FlParams *params, int32_t device, FlSolver **out) {
+    if (!out) return set_error(FL_E_INVALID, "out is NULL");
+    *out = nullptr;
+    FlSolver *s = new (std::nothrow) FlSolver();
+    if (!s) return set_error(FL_E_NOMEM, "out of host memory");
+    int rc = create_impl(mesh, drain, forcing, params, device, s);
+    if (rc != FL_OK) {
+        std::string msg = g_error;
+        fl_destroy(s);
+        g_error = msg;
+        return rc;
+    }
+    *out = s;
+    return FL_OK;
+}
+
+FL_API int fl_reset_clock(FlSolver *s, void *stream) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    const int32_t parity = s->run_h ? s->run_h->parity : 0;
+    RunCtrl r;
+    memset(&r, 0, sizeof(r));
+    r.t = 0.0;
+    r.cached_dt = -1.0;
+    r.next_snap_t = 0.0;
+    r.final_t = s->params.duration_s;
+    r.stop_t = 0.0;
+    r.max_dt = s->params.max_dt_s;
+    r.safety = s->params.cfl_reuse_safety_factor;
+    r.snap_interval = s->params.snapshot_interval_s;
+    r.g = s->params.gravity_mps2;
+    r.last_dt = 0.0;
+    r.step = 0;
+    r.max_step = std::numeric_limits<int64_t>::max();
+    r.parity = parity;
+    r.snap_count = 0;
+    r.max_snaps = s->params.max_snapshots;
+    r.error = 0;
+    r.cfl_interval = s->params.cfl_update_interval_steps;
+    r.finite_interval = s->params.finite_check_interval_steps;
+    r.hyeto_n = s->hy.n;
+    *s->run_h = r;
+    FL_CUDA(cudaMemcpyAsync(s->run, s->run_h, sizeof(RunCtrl), cudaMemcpyHostToDevice, st));
+    FL_CUDA(cudaMemsetAsync(s->ctrl, 0, sizeof(StepCtrl) * 2, st));
+    FL_CUDA(cudaMemsetAsync(s->wet, 0, sizeof(float) * (size_t)s->C, st));
+    FL_CUDA(cudaMemsetAsync(s->led_s, 0, sizeof(double) * (size_t)s->surf_blocks * SURF_TERMS, st));
+    if (s->has_drain()) {
+        FL_CUDA(cudaMemsetAsync(s->led_1, 0, sizeof(double) * (size_t)s->d1_blocks * D1_TERMS, st));
+        FL_CUDA(cudaMemsetAsync(s->led_2, 0, sizeof(double) * (size_t)s->d2_blocks * D2_TERMS, st));
+    }
+    FL_CUDA(cudaStreamSynchronize(st));
+    s->slot = 0;
+    return FL_OK;
+}
+
+FL_API int fl_set_state(FlSolver *s, const float *h, const float *hu, const float *hv, const double *node_volume,
+                        const double *link_flow, const float *wet_time, int32_t mem, void *stream) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    int rc = sync_run(s, st);
+    if (rc) return rc;
+    const int32_t C = s->C;
+    const cudaMemcpyKind k = mem == FL_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const float *src[3] = {h, hu, hv};
+    int mask = 0;
+    for (int b = 0; b < 3; ++b) {
+        if (!src[b]) continue;
+        FL_CUDA(cudaMemcpyAsync(s->stage_f[b], src[b], sizeof(float) * C, k, st));
+        mask |= 1 << b;
+    }
+    if (mask) {
+        FL_CUDA(launch_load_state(s->state[s->run_h->parity], s->stage_f[0], s->stage_f[1], s->stage_f[2], s->bed,
+                                  s->perm, C, mask, st));
+    }
+    if (wet_time) {
+        FL_CUDA(cudaMemcpyAsync(s->stage_f[0], wet_time, sizeof(float) * C, k, st));
+        FL_CUDA(launch_permute_f32(s->stage_f[0], s->wet, s->perm, C, 0, st));
+    }
+    if (node_volume && s->N > 0) {
+        FL_CUDA(cudaMemcpyAsync(s->stage_d, node_volume, sizeof(double) * s->N, k, st));
+        FL_CUDA(launch_f64_to_ff(s->stage_d, s->Va, s->N, st));
+    }
+    if (link_flow && s->NL > 0) {
+        FL_CUDA(cudaStreamSynchronize(st));
+        FL_CUDA(cudaMemcpyAsync(s->stage_d, link_flow, sizeof(double) * s->NL, k, st));
+        FL_CUDA(launch_f64_to_f32(s->stage_d, s->Q[s->run_h->parity], s->NL, st));
+    }
+    g_launches += (mask ? 1 : 0) + (wet_time ? 1 : 0) + (node_volume && s->N ? 1 : 0) + (link_flow && s->NL ? 1 : 0);
+    FL_CUDA(cudaStreamSynchronize(st));
+    return FL_OK;
+}
+
+FL_API int fl_get_state(FlSolver *s, float *h, float *hu, float *hv, double *node_volume, double *link_flow,
+                        float *wet_time, int32_t mem, void *stream) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    int rc = sync_run(s, st);
+    if (rc) return rc;
+    const int32_t C = s->C;
+    const cudaMemcpyKind k = mem == FL_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (h || hu || hv) {
+        FL_CUDA(launch_store_state(s->state[s->run_h->parity], h ? s->stage_f[0] : nullptr, hu ? s->stage_f[1] : nullptr,
+                                   hv ? s->stage_f[2] : nullptr, s->perm, C, st));
+        if (h) FL_CUDA(cudaMemcpyAsync(h, s->stage_f[0], sizeof(float) * C, k, st));
+        if (hu) FL_CUDA(cudaMemcpyAsync(hu, s->stage_f[1], sizeof(float) * C, k, st));
+        if (hv) FL_CUDA(cudaMemcpyAsync(hv, s->stage_f[2], sizeof(float) * C, k, st));
+        FL_CUDA(cudaStreamSynchronize(st));
+    }
+    if (wet_time) {
+        FL_CUDA(launch_permute_f32(s->wet, s->stage_f[0], s->perm, C, 1, st));
+        FL_CUDA(cudaMemcpyAsync(wet_time, s->stage_f[0], sizeof(float) * C, k, st));
+        FL_CUDA(cudaStreamSynchronize(st));
+    }
+    if (node_volume && s->N > 0) {
+        FL_CUDA(launch_ff_to_f64(s->Va, s->stage_d, s->N, st));
+        FL_CUDA(cudaMemcpyAsync(node_volume, s->stage_d, sizeof(double) * s->N, k, st));
+        FL_CUDA(cudaStreamSynchronize(st));
+    }
+    if (link_flow && s->NL > 0) {
+        FL_CUDA(launch_f32_to_f64(s->Q[s->run_h->parity], s->stage_d, s->NL, st));
+        FL_CUDA(cudaMemcpyAsync(link_flow, s->stage_d, sizeof(double) * s->NL, k, st));
+        FL_CUDA(cudaStreamSynchronize(st));
+    }
+    return FL_OK;
+}
+
+FL_API int fl_run(FlSolver *s, double t_target_s, int64_t max_steps, void *stream) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    int rc = sync_run(s, st);
+    if (rc) return rc;
+    if (s->run_h->error) return error_code_message(s);
+    RunCtrl &r = *s->run_h;
+    const double stop = std::min(t_target_s, r.final_t);
+    const int64_t start_step = r.step;
+    r.stop_t = stop;
+    r.max_step = max_steps > 0 ? start_step + max_steps : std::numeric_limits<int64_t>::max();
+    if ((rc = push_run(s, st))) return rc;
+    if (!(r.t < stop)) return FL_OK;
+    const int interval = s->params.cfl_update_interval_steps;
+    // the next launch re-plans from the run state
+    FL_CUDA(cudaMemsetAsync(&s->ctrl[s->slot], 0, sizeof(StepCtrl), st));
+    int64_t hs = start_step;
+    if (hs % interval != 0) {
+        FL_CUDA(launch_replan(s->run, s->snap_t, s->hy, s->ctrl, s->slot, st));
+        g_launches++;
+    }
+    while (hs % interval != 0) {  // unaligned prefix: single steps
+        const bool next_eval = (hs + 1) % interval == 0;
+        if ((rc = launch_step(s, s->slot, false, !next_eval, st))) return rc;
+        s->slot ^= 1;
+        ++hs;
+    }
+    if ((rc = capture_graph(s))) return rc;
+    // graph chunks, polling progress one chunk behind
+    int64_t launched = 0;
+    int64_t last_step = -1;
+    int stalled = 0;
+    const int per_chunk = s->chunk * s->launches_per_step() + (s->chunk + interval - 1) / interval;
+    while (true) {
+        FL_CUDA(cudaGraphLaunch(s->graph, st));
+        g_launches += per_chunk;
+        FL_CUDA(cudaMemcpyAsync(&s->poll_h[launched & 1], s->run, sizeof(RunCtrl), cudaMemcpyDeviceToHost, st));
+        FL_CUDA(cudaEventRecord(s->ev[launched & 1], st));
+        ++launched;
+        if (launched >= 2) {
+            FL_CUDA(cudaEventSynchronize(s->ev[launched & 1]));
+            const RunCtrl &p = s->poll_h[launched & 1];
+            if (p.error || !(p.t < stop) || p.step >= r.max_step) break;
+            // every chunk of an unfinished run advances the step count
+            stalled = (p.step == last_step) ? stalled + 1 : 0;
+            last_step = p.step;
+            if (stalled >= 3) {
+                FL_CUDA(cudaStreamSynchronize(st));
+                return set_error(FL_E_CUDA, "device loop stopped advancing at step %lld (t=%.3f s)",
+                                 (long long)p.step, p.t);
+            }
+        }
+    }
+    s->slot = 0;
+    if ((rc = sync_run(s, st))) return rc;
+    const RunCtrl &e = *s->run_h;
+    if (!e.error && e.finite_interval > 0 && e.step > 0 && e.step % e.finite_interval == 0) {
+        FL_CUDA(launch_finite(s->state[0], s->state[1], s->run, s->C, st));
+        g_launches++;
+        if ((rc = sync_run(s, st))) return rc;
+    }
+    if (s->run_h->error) return error_code_message(s);
+    if (s->run_h->t < stop) return set_error(FL_E_STEP_CAP, "step cap reached at t=%.3f s (target %.3f s)", s->run_h->t, stop);
+    return FL_OK;
+}
+
+FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mps, void *stream) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    if (!(dt_s > 0.0)) return set_error(FL_E_INVALID, "timestep_s must be positive.");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    int rc = sync_run(s, st);
+    if (rc) return rc;
+    RunCtrl &r = *s->run_h;
+    StepCtrl c;
+    memset(&c, 0, sizeof(c));
+    c.t0 = r.t;
+    c.dt = dt_s;
+    c.dt_f = (float)dt_s;
+    c.dtg_f = (float)(dt_s * s->params.gravity_mps2);
+    c.rain_f = (float)rain_rate_mps;
+    c.active = 1;
+    c.parity = r.parity;
+    c.snap_slot = -1;
+    c.check_finite = 0;
+    c.phases = phases;
+    c.step = r.step;
+    r.t += dt_s;
+    r.step += 1;
+    r.parity ^= 1;
+    r.last_dt = dt_s;
+    FL_CUDA(cudaMemcpyAsync(&s->ctrl[s->slot], &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, st));
+    FL_CUDA(cudaMemcpyAsync(s->run, s->run_h, sizeof(RunCtrl), cudaMemcpyHostToDevice, st));
+    FL_CUDA(launch_surface(s->sa, s->kind, s->slot, 0, st));
+    g_launches++;
+    if (s->has_drain() && (phases & FL_PHASE_DRAINAGE)) {
+        FL_CUDA(launch_inlets(s->d1, s->slot, st));
+        FL_CUDA(launch_network(s->d2, s->slot, st));
+        g_launches += 2;
+    } else if (s->has_drain()) {
+        // no drainage this step: carry link flow to the other parity buffer
+        FL_CUDA(cudaMemcpyAsync(s->Q[r.parity], s->Q[c.parity], sizeof(float) * std::max(s->NL, 1),
+                                cudaMemcpyDeviceToDevice, st));
+    }
+    s->slot ^= 1;
+    FL_CUDA(cudaStreamSynchronize(st));
+    FL_CUDA(cudaGetLastError());
+    return FL_OK;
+}
+
+FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *stream, double *ms_per_launch) {
+    if (!s || !ms_per_launch || reps < 1) return set_error(FL_E_INVALID, "bad fl_time_kernel arguments");
+    if ((kernel == 1 || kernel == 2) && !s->has_drain()) return set_error(FL_E_INVALID, "solver has no drainage");
+    if (kernel < 0 || kernel > 3) return set_error(FL_E_INVALID, "kernel must be 0..3");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    int rc = sync_run(s, st);
+    if (rc) return rc;
+    const RunCtrl &r = *s->run_h;
+    StepCtrl c;
+    memset(&c, 0, sizeof(c));
+    const double dt = r.last_dt > 0.0 ? r.last_dt : 0.1;
+    c.t0 = r.t;
+    c.dt = dt;
+    c.dt_f = (float)dt;
+    c.dtg_f = (float)(dt * s->params.gravity_mps2);
+    c.active = 1;
+    c.parity = r.parity;
+    c.snap_slot = -1;
+    c.phases = FL_PHASE_ALL;
+    c.step = r.step;
+    FL_CUDA(cudaMemcpyAsync(&s->ctrl[0], &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, st));
+    auto launch = [&]() -> int {
+        switch (kernel) {
+            case 0: FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, st)); break;
+            case 1: FL_CUDA(launch_inlets(s->d1, 0, st)); break;
+            case 2: FL_CUDA(launch_network(s->d2, 0, st)); break;
+            default: {
+                DtArgs a = s->da;
+                a.dt_out = s->dt_out;
+                FL_CUDA(launch_dt(a, s->dt_blocks, 0, 0, st));
+            }
+        }
+        g_launches++;
+        return FL_OK;
+    };
+    if ((rc = launch())) return rc;  // warm-up
+    cudaEvent_t e0, e1;
+    FL_CUDA(cudaEventCreate(&e0));
+    FL_CUDA(cudaEventCreate(&e1));
+    FL_CUDA(cudaEventRecord(e0, st));
+    for (int i = 0; i < reps && rc == FL_OK; ++i) rc = launch();
+    FL_CUDA(cudaEventRecord(e1, st));
+    FL_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    *ms_per_launch = (double)ms / reps;
+    return FL_OK;
+}
+
+FL_API int fl_stable_timestep(FlSolver *s, double *dt_s, void *stream) {
+    if (!s || !dt_s) return set_error(FL_E_INVALID, "solver or output is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    DtArgs a = s->da;
+    a.dt_out = s->dt_out;
+    FL_CUDA(launch_dt(a, s->dt_blocks, 0, 0, st));
+    g_launches++;
+    double v = -1.0;
+    FL_CUDA(cudaMemcpyAsync(&v, s->dt_out, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    if (!(v > 0.0)) return set_error(FL_E_INVALID, "No finite cells are available for timestep calculation.");
+    *dt_s = v;
+    return FL_OK;
+}
+
+FL_API int fl_update_forcing(FlSolver *s, const float *rain_multiplier, const float *f0, const float *fc,
+                             const float *k, float infiltration_mps) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    FL_CUDA(cudaSetDevice(s->device));
+    if (s->kind == 0) {
+        if (s->sa.infil_scalar != infiltration_mps) {
+            s->sa.infil_scalar = infiltration_mps;
+            if (s->graph) {  // the graph holds the kernel arguments by value
+                cudaGraphExecDestroy(s->graph);
+                s->graph = nullptr;
+            }
+        }
+        return FL_OK;
+    }
+    const int32_t C = s->C;
+    std::vector<float4> hz(C);
+    FL_CUDA(cudaMemcpy(hz.data(), s->sa.horton, sizeof(float4) * C, cudaMemcpyDeviceToHost));
+    for (int32_t i = 0; i < C; ++i) {
+        const int32_t r = s->perm_h[i];
+        if (f0) hz[i].x = f0[r];
+        if (fc) hz[i].y = fc[r];
+        if (k) hz[i].z = k[r];
+        if (rain_multiplier) hz[i].w = rain_multiplier[r];
+    }
+    FL_CUDA(cudaMemcpy((void *)s->sa.horton, hz.data(), sizeof(float4) * C, cudaMemcpyHostToDevice));
+    return FL_OK;
+}
+
+FL_API int fl_get_progress(FlSolver *s, FlProgress *out, void *stream) {
+    if (!s || !out) return set_error(FL_E_INVALID, "solver or output is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    int rc = sync_run(s, st);
+    if (rc) return rc;
+    const RunCtrl &r = *s->run_h;
+    out->t_s = r.t;
+    out->step_count = r.step;
+    out->cfl_eval_count = r.cfl_evals;
+    out->cfl_reused_count = r.cfl_reused;
+    out->snapshot_count = r.snap_count;
+    out->error = r.error;
+    out->error_step = r.error_step;
+    out->last_dt_s = r.last_dt;
+    return FL_OK;
+}
+
+static void sum_blocks(const std::vector<double> &v, int terms, double *out) {
+    for (int j = 0; j < terms; ++j) out[j] = 0.0;
+    const size_t blocks = v.size() / terms;
+    for (size_t b = 0; b < blocks; ++b)
+        for (int j = 0; j < terms; ++j) out[j] += v[b * terms + j];
+}
+
+FL_API int fl_read_ledger(FlSolver *s, double *out, int32_t n, void *stream) {
+    if (!s || !out) return set_error(FL_E_INVALID, "solver or output is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    double all[FL_LEDGER_COUNT] = {0};
+    std::vector<double> v((size_t)s->surf_blocks * SURF_TERMS);
+    FL_CUDA(cudaMemcpyAsync(v.data(), s->led_s, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    sum_blocks(v, SURF_TERMS, all + FL_LEDGER_RAINFALL);
+    if (s->has_drain()) {
+        std::vector<double> v1((size_t)s->d1_blocks * D1_TERMS), v2((size_t)s->d2_blocks * D2_TERMS);
+        FL_CUDA(cudaMemcpyAsync(v1.data(), s->led_1, sizeof(double) * v1.size(), cudaMemcpyDeviceToHost, st));
+        FL_CUDA(cudaMemcpyAsync(v2.data(), s->led_2, sizeof(double) * v2.size(), cudaMemcpyDeviceToHost, st));
+        FL_CUDA(cudaStreamSynchronize(st));
+        sum_blocks(v1, D1_TERMS, all + FL_LEDGER_CAPTURE);
+        sum_blocks(v2, D2_TERMS, all + FL_LEDGER_OUTFALL);
+    }
+    FL_CUDA(cudaMemsetAsync(s->vol_out, 0, 2 * sizeof(double), st));
+    FL_CUDA(launch_volumes(s->state[0], s->state[1], s->sa.g1, s->Va, s->run, s->C, s->N, s->vol_out, st));
+    g_launches++;
+    FL_CUDA(cudaMemcpyAsync(all + FL_LEDGER_SURFACE_VOLUME, s->vol_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < n && i < FL_LEDGER_COUNT; ++i) out[i] = all[i];
+    return FL_OK;
+}
+
+FL_API int fl_get_snapshots(FlSolver *s, int32_t first, int32_t count, double *times_s, float *h, float *hu,
+                            float *hv, float *node_volume, int32_t mem, void *stream) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    int rc = sync_run(s, st);
+    if (rc) return rc;
+    if (first < 0 || count < 0 || first + count > s->run_h->snap_count)
+        return set_error(FL_E_INVALID, "snapshots [%d, %d) requested, %d available", first, first + count,
+                         s->run_h->snap_count);
+    const cudaMemcpyKind k = mem == FL_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const size_t C = (size_t)s->C;
+    if (times_s) {
+        FL_CUDA(cudaMemcpyAsync(times_s, s->snap_t + first, sizeof(double) * count, cudaMemcpyDeviceToHost, st));
+    }
+    float *src[3] = {s->snap_h, s->snap_hu, s->snap_hv};
+    float *dst[3] = {h, hu, hv};
+    for (int b = 0; b < 3; ++b) {
+        if (!dst[b]) continue;
+        for (int32_t i = 0; i < count; ++i) {
+            FL_CUDA(launch_permute_f32(src[b] + (size_t)(first + i) * C, s->stage_f[0], s->perm, s->C, 1, st));
+            FL_CUDA(cudaMemcpyAsync(dst[b] + (size_t)i * C, s->stage_f[0], sizeof(float) * C, k, st));
+            FL_CUDA(cudaStreamSynchronize(st));
+        }
+    }
+    if (node_volume && s->N > 0 && count > 0) {
+        FL_CUDA(cudaMemcpyAsync(node_volume, s->snap_v + (size_t)first * s->N, sizeof(float) * (size_t)count * s->N, k, st));
+    }
+    FL_CUDA(cudaStreamSynchronize(st));
+    return FL_OK;
+}
+
+}  // extern "C"

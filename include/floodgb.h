@@ -1,0 +1,225 @@
+/*
+ * floodgb -- C ABI of the GB300 (sm_103a) flood step library (libfloodgb.so).
+ *
+ * The library replaces the reference's CuPy fused-kernel dispatch for the
+ * explicit finite-volume flood step (arsanjeevk/gpu-urban-flood-cupy-jax,
+ * package gurugram_flood).  Each entry point below names the reference
+ * interface it stands in for.  All signatures use plain pointers and sizes;
+ * arrays are given in the reference's layout and cell order (the library
+ * renumbers internally and converts back on output).
+ *
+ * Return codes: FL_OK (0) or a negative FL_E_* code; fl_last_error() gives
+ * the message of the most recent failure on the calling thread.
+ *
+ * Threading: a solver is used from one host thread at a time; every call
+ * takes the CUDA stream it runs on (NULL = the legacy default stream).
+ */
+#ifndef FLOODGB_H
+#define FLOODGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FL_API __attribute__((visibility("default")))
+
+#define FLOODGB_ABI_VERSION 1
+
+enum {
+    FL_OK = 0,
+    FL_E_INVALID = -1,     /* bad argument, shape or index (reference: ValueError) */
+    FL_E_CUDA = -2,        /* CUDA runtime failure */
+    FL_E_NO_DEVICE = -3,   /* no usable CUDA device (reference: BackendUnavailableError) */
+    FL_E_NONFINITE = -4,   /* non-finite depth at a check step (reference: SimulationError) */
+    FL_E_STEP_CAP = -5,    /* the step cap ended fl_run before the target time */
+    FL_E_NOMEM = -6,       /* host or device allocation failed */
+    FL_E_UNSUPPORTED = -7, /* input uses a reference feature this library does not implement */
+    FL_E_SNAPSHOTS = -8    /* more snapshots than FlParams.max_snapshots */
+};
+
+/* Step phases for fl_step (a bit set). */
+enum {
+    FL_PHASE_SURFACE = 1,  /* fluxes, cell update + Manning, rain and infiltration */
+    FL_PHASE_CLAMP = 2,    /* velocity clamp */
+    FL_PHASE_DRAINAGE = 4, /* inlet exchange, links, outfalls, overflow return */
+    FL_PHASE_ALL = 7
+};
+
+/* Memory kind of caller buffers in state / snapshot transfers. */
+enum { FL_MEM_HOST = 0, FL_MEM_DEVICE = 1 };
+
+/* Inlet capture rules (reference: inlet_capture_rule strings). */
+enum { FL_CAPTURE_CAPACITY = 0, FL_CAPTURE_HEAD_LIMITED = 1, FL_CAPTURE_ORIFICE = 2, FL_CAPTURE_WEIR_ORIFICE = 3 };
+
+/* Surface mesh: the fields of TriangularSurfaceTopology
+ * (gurugram_flood/kernels/triangular_backend.py:58-90), host pointers. */
+typedef struct {
+    int32_t cell_count, edge_count;
+    const float *bed_elevation_m, *manning_n, *cell_area_m2, *characteristic_length_m;
+    const float *active_mask; /* NULL: every cell active; values must be 0 or 1 */
+    const int32_t *edge_left_cell, *edge_right_cell, *boundary_code;
+    const float *edge_normal_x, *edge_normal_y, *edge_length_m;
+    const float *centroid_x, *centroid_y; /* optional: enable space-filling-curve renumbering */
+    int32_t has_stage_boundary;
+    float boundary_stage_m;
+} FlMeshDesc;
+
+/* Drainage: TriangularNodeCouplingTopology (:130-154) and
+ * TriangularPipeNetworkTopology (:172-200), host pointers; optional arrays
+ * may be NULL exactly where the reference allows None. */
+typedef struct {
+    int32_t node_count, link_count, inlet_count;
+    const int32_t *inlet_cell_index, *inlet_node_index, *node_surface_cell_index;
+    const float *node_invert_elevation_m, *node_storage_area_m2, *node_max_depth_m;
+    const float *inlet_capture_capacity_m3ps, *inlet_surcharge_capacity_m3ps;
+    const int32_t *link_from_node_index, *link_to_node_index;
+    const float *link_length_m, *link_area_m2, *link_hydraulic_radius_m, *link_manning_n;
+    const float *link_flow_capacity_m3ps, *link_invert_elevation_m, *link_diameter_m;
+    const float *link_minor_loss_coefficient;
+    const int32_t *link_geometry_code;
+    const float *link_rect_width_m, *link_rect_height_m;
+    const float *outfall_area_m2, *outfall_coefficient, *outfall_tailwater_head_m;
+    const float *outfall_flow_capacity_m3ps;
+    float pressurized_wave_speed_mps;
+    int32_t inlet_capture_rule;
+    float inlet_orifice_area_m2, inlet_orifice_coefficient, inlet_weir_perimeter_m, inlet_weir_coefficient;
+} FlDrainDesc;
+
+/* Forcing: kind 0 = uniform (scalar rain from the hyetograph, scalar
+ * infiltration capacity); kind 1 = per cell (rain = rate x multiplier,
+ * Horton capacity fc + (f0 - fc) exp(-k wet_time)); reference
+ * production_infiltration_support.py:96-138. */
+typedef struct {
+    int32_t kind;
+    const float *rain_multiplier, *horton_f0_mps, *horton_fc_mps, *horton_k_per_s;
+    float infiltration_mps;
+    int32_t hyetograph_count;
+    const double *hyeto_start_s, *hyeto_end_s, *hyeto_rate_mps;
+} FlForcingDesc;
+
+/* Solver knobs: SolverConfig (gurugram_flood/config.py:84-100). */
+typedef struct {
+    double gravity_mps2, min_depth_m;
+    double cfl;
+    int32_t cfl_update_interval_steps;
+    double cfl_reuse_safety_factor;
+    double max_dt_s, max_speed_mps;
+    int32_t finite_check_interval_steps;
+    double duration_s, snapshot_interval_s;
+    int32_t max_snapshots;
+} FlParams;
+
+typedef struct {
+    double t_s;
+    int64_t step_count, cfl_eval_count, cfl_reused_count;
+    int32_t snapshot_count;
+    int32_t error;      /* 0 or an FL_E_* code */
+    int64_t error_step; /* step count at the failed check */
+    double last_dt_s;
+} FlProgress;
+
+/* Ledger terms (cumulative m^3, float64): the keys of engine.py's `cum`
+ * (engine.py:197-207) plus the diagnostics the pipe step returns. */
+enum {
+    FL_LEDGER_RAINFALL = 0,
+    FL_LEDGER_INFILTRATION,
+    FL_LEDGER_BOUNDARY_IN,
+    FL_LEDGER_BOUNDARY_OUT,
+    FL_LEDGER_CAPTURE,
+    FL_LEDGER_SURCHARGE,
+    FL_LEDGER_OUTFALL,
+    FL_LEDGER_OVERFLOW,
+    FL_LEDGER_UNRETURNED,
+    FL_LEDGER_LINK_ABS,
+    FL_LEDGER_SURFACE_VOLUME, /* current sum(h * area) */
+    FL_LEDGER_NODE_VOLUME,    /* current sum(node volume) */
+    FL_LEDGER_COUNT
+};
+
+typedef struct FlSolver FlSolver;
+
+/* Library version and last error message (thread-local). */
+FL_API int fl_abi_version(void);
+FL_API const char *fl_last_error(void);
+
+/* Number of visible CUDA devices (0 on a machine without a GPU). */
+FL_API int fl_device_count(int32_t *count);
+
+/* Build the device layout and upload the static inputs.  Replaces the
+ * upload + cell_edge_indices build of triangular_topology_to_backend,
+ * triangular_node_coupling_to_backend and triangular_pipe_network_to_backend
+ * (triangular_backend.py:329-475) and the per-run setup of run_simulation
+ * (gurugram_flood/solver/engine.py:137-161).  drain may be NULL. */
+FL_API int fl_create(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcing,
+                     const FlParams *params, int32_t device, FlSolver **out);
+FL_API void fl_destroy(FlSolver *solver);
+
+/* State transfer in reference order: TriangularSurfaceState,
+ * TriangularPipeNetworkState (:49-55, :203-208) and the Horton wet time.
+ * Any pointer may be NULL to leave that field unchanged / unread. */
+FL_API int fl_set_state(FlSolver *solver, const float *h, const float *hu, const float *hv,
+                        const double *node_volume, const double *link_flow, const float *wet_time,
+                        int32_t mem, void *stream);
+FL_API int fl_get_state(FlSolver *solver, float *h, float *hu, float *hv, double *node_volume,
+                        double *link_flow, float *wet_time, int32_t mem, void *stream);
+
+/* Rewind the clock: t = 0, no cached CFL dt, ledger, snapshots and Horton
+ * wet time cleared (the start of run_simulation's loop, engine.py:186-215). */
+FL_API int fl_reset_clock(FlSolver *solver, void *stream);
+
+/* Advance the adaptive loop of run_simulation (engine.py:219-344) until the
+ * simulated time reaches min(t_target_s, duration) or max_steps more steps
+ * ran (FL_E_STEP_CAP).  The loop runs on the device as CUDA-graph chunks of
+ * cfl_update_interval_steps steps; the host only polls progress. */
+FL_API int fl_run(FlSolver *solver, double t_target_s, int64_t max_steps, void *stream);
+
+/* One step with an explicit dt and a phase set: step_triangular_surface
+ * (triangular_backend.py:478-528) for FL_PHASE_SURFACE, clamp_velocity
+ * (stabilizers.py:8-27) for FL_PHASE_CLAMP, step_triangular_dynamic_pipe_network
+ * (triangular_backend.py:665-830) for FL_PHASE_DRAINAGE.  rain_rate_mps is
+ * the base rainfall rate for the step (multiplied per cell in kind 1). */
+FL_API int fl_step(FlSolver *solver, double dt_s, int32_t phases, double rain_rate_mps, void *stream);
+
+/* stable_triangular_timestep_s (triangular_backend.py:955-972) on the current
+ * state, with the configured cfl. */
+FL_API int fl_stable_timestep(FlSolver *solver, double *dt_s, void *stream);
+
+/* Replace the per-cell forcing fields (kind 1: reference-order arrays, any
+ * may be NULL to keep it) or the scalar infiltration capacity (kind 0).
+ * The reference passes forcing per step (TriangularSurfaceForcing,
+ * triangular_backend.py:93-101); the run loop derives it from these fields. */
+FL_API int fl_update_forcing(FlSolver *solver, const float *rain_multiplier, const float *horton_f0_mps,
+                             const float *horton_fc_mps, const float *horton_k_per_s, float infiltration_mps);
+
+FL_API int fl_get_progress(FlSolver *solver, FlProgress *out, void *stream);
+
+/* Cumulative ledger, FL_LEDGER_COUNT doubles (n may be smaller). */
+FL_API int fl_read_ledger(FlSolver *solver, double *out, int32_t n, void *stream);
+
+/* Snapshots [first, first+count) of depth, hu, hv (count x cell_count, reference
+ * order) and node volume (count x node_count, float32 as engine.py:321 stores
+ * it); times in seconds.  Any output pointer may be NULL. */
+FL_API int fl_get_snapshots(FlSolver *solver, int32_t first, int32_t count, double *times_s, float *h,
+                            float *hu, float *hv, float *node_volume, int32_t mem, void *stream);
+
+/* Host-only layout check (no GPU needed): builds the renumbered layout and
+ * reports its sizes.  stats[0..7] = cells, edges, slots used, inlet cells,
+ * nodes, links, drainage groups, max inlets per cell. */
+FL_API int fl_plan_check(const FlMeshDesc *mesh, const FlDrainDesc *drain, int64_t *stats, int32_t *perm_out);
+
+/* Time `reps` back-to-back launches of one kernel of a step (0 surface,
+ * 1 inlet exchange, 2 pipe network, 3 CFL reduction) between CUDA events on
+ * `stream`, at the solver's current state and last dt; the clock is not
+ * advanced but the state buffers are overwritten (reset before the next run).
+ * No reference counterpart: it is the measurement hook for the roofline. */
+FL_API int fl_time_kernel(FlSolver *solver, int32_t kernel, int32_t reps, void *stream, double *ms_per_launch);
+
+/* Number of kernel launches the library has issued in this process. */
+FL_API int64_t fl_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
