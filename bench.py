@@ -49,6 +49,10 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--profile", choices=["loop", "kernels"], default=None,
+                   help="ncu helper: open a profiler range around 64 solver steps of a wet run (loop) or "
+                        "around 3 isolated launches of each step kernel (kernels); prints nothing else")
+    p.add_argument("--profile-start-s", type=float, default=900.0)
     return p.parse_args()
 
 
@@ -336,8 +340,46 @@ def our_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_arm(args):
+    """Small, bounded workloads for ncu (use with --profile-from-start off)."""
+
+    import torch
+
+    from floodgb import native
+    from floodgb.build import build_library
+    from floodgb.config import load_config
+    from floodgb.exceptions import SimulationError
+    from floodgb.solver import solver_for_city
+    from floodgb.synthetic import production_workload
+
+    build_library()
+    native.load()
+    sc = production_workload()
+    cfg = load_config(None, sc.overrides)
+    solver = solver_for_city(sc.city, sc.rainfall, cfg)
+    solver.run(args.profile_start_s)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    if args.profile == "loop":
+        try:
+            solver.run(max_steps=64)
+        except SimulationError:
+            pass  # the step cap ends the slice
+    else:
+        for k in range(4):
+            solver.time_kernel(k, reps=3)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    p = solver.progress()
+    print(json.dumps({"profile": args.profile, "t_s": p.t_s, "steps": p.step_count}))
+    solver.close()
+
+
 def main():
     args = parse_args()
+    if args.profile:
+        profile_arm(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
     else:

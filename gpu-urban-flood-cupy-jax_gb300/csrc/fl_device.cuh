@@ -106,6 +106,7 @@ __device__ __forceinline__ float ff_val(float2 a) { return a.x + a.y; }
 // a + b with the error of the leading sum kept in the low word (TwoSum).
 __device__ __forceinline__ float2 ff_add(float2 a, float b) {
     const float s = a.x + b;
+    if (!isfinite(s)) return make_float2(s, 0.0f);
     const float bb = s - a.x;
     const float err = (a.x - (s - bb)) + (b - bb);
     const float lo = a.y + err;

@@ -156,7 +156,8 @@ def clamp_velocity(state: TriangularSurfaceState, max_speed_mps: float, xp=np,
         speed = np.sqrt(hu ** 2 + hv ** 2) / np.maximum(h, np.float32(1.0e-8))
         scale = np.minimum(np.float32(1.0), np.float32(max_speed_mps) / np.maximum(speed, np.float32(1.0e-12)))
         return TriangularSurfaceState(h, hu * scale, hv * scale)
-    s = _surface_solver(topology, None, False, max_speed=float(max_speed_mps))
+    stage = 0.0 if topology.has_stage_boundary else None  # the stage does not enter the clamp
+    s = _surface_solver(topology, stage, False, max_speed=float(max_speed_mps))
     s.set_state(state.h_m, state.hu_m2ps, state.hv_m2ps)
     s.reset_clock()
     s.step(1.0, N.FL_PHASE_CLAMP, 0.0)
@@ -168,7 +169,8 @@ def stable_triangular_timestep_s(topology: TriangularSurfaceTopology, state: Tri
                                  cfl: float = 0.45, gravity_mps2: float = 9.80665, min_depth_m: float = 1.0e-5) -> float:
     """Global CFL dt: min over cells of cfl * l / (|u| + sqrt(g h))."""
 
-    s = _surface_solver(topology, None, False, cfl=float(cfl))
+    stage = 0.0 if topology.has_stage_boundary else None  # the stage does not enter the CFL dt
+    s = _surface_solver(topology, stage, False, cfl=float(cfl))
     s.set_state(state.h_m, state.hu_m2ps, state.hv_m2ps)
     return s.stable_timestep()
 

@@ -44,18 +44,23 @@ def hyetograph_arrays(event: RainfallEvent) -> tuple[np.ndarray, np.ndarray, np.
     return start_s, end_s, rate
 
 
-def make_rate_fn(start_min, end_min, intensity_mmhr) -> Callable[[float], float]:
-    start_s = np.asarray(start_min, dtype=float) * 60.0
-    end_s = np.asarray(end_min, dtype=float) * 60.0
-    rate_mps = np.asarray(intensity_mmhr, dtype=float) / 1000.0 / 3600.0
+class HyetographRate:
+    """Callable ``t_s -> rainfall rate (m/s)`` of a hyetograph table."""
 
-    def rate(t_s: float) -> float:
-        idx = int(np.searchsorted(end_s, t_s, side="right"))
-        if idx >= len(rate_mps) or t_s < start_s[idx]:
+    def __init__(self, start_min, end_min, intensity_mmhr):
+        self.start_s = np.asarray(start_min, dtype=float) * 60.0
+        self.end_s = np.asarray(end_min, dtype=float) * 60.0
+        self.rate_mps = np.asarray(intensity_mmhr, dtype=float) / 1000.0 / 3600.0
+
+    def __call__(self, t_s: float) -> float:
+        idx = int(np.searchsorted(self.end_s, t_s, side="right"))
+        if idx >= len(self.rate_mps) or t_s < self.start_s[idx]:
             return 0.0
-        return float(rate_mps[idx])
+        return float(self.rate_mps[idx])
 
-    return rate
+
+def make_rate_fn(start_min, end_min, intensity_mmhr) -> Callable[[float], float]:
+    return HyetographRate(start_min, end_min, intensity_mmhr)
 
 
 def rainfall_event(start_min, end_min, intensity_mmhr, source: str = "synthetic") -> RainfallEvent:

@@ -39,7 +39,9 @@ def gates(depth, ref_depth, area, valid, threshold=0.05):
     r = ref_depth.astype(np.float64)[valid]
     rmse = float(np.sqrt(np.mean((d - r) ** 2)))
     wet_c, wet_r = d >= threshold, r >= threshold
-    csi = float((wet_c & wet_r).sum() / max(int((wet_c | wet_r).sum()), 1))
+    union = int((wet_c | wet_r).sum())
+    # nothing wet in either field yet: the extents agree
+    csi = float((wet_c & wet_r).sum() / union) if union else 1.0
     vc = float(np.sum(depth.astype(np.float64) * area))
     vr = float(np.sum(ref_depth.astype(np.float64) * area))
     return rmse, csi, (vc - vr) / max(abs(vr), 1.0)
@@ -214,16 +216,30 @@ def test_runs_are_bitwise_reproducible():
 
 
 def test_nonfinite_depth_raises_simulation_error():
+    # Fault injected on the host: an isolated storage node holding an infinite
+    # volume overflows into its surface cell, whose depth becomes +inf at the
+    # end of step 1; the finite check (every step here) must stop the run.
+    # (A non-finite initial depth cannot be used: like the reference's CUDA
+    # kernels, the depth update clips max(h, 0), which maps NaN to 0.)
+    from floodgb.topology import TriangularNodeCouplingTopology, TriangularPipeNetworkTopology
+
     sc = make_grid_city(n=20, size_m=200.0, seed=1, duration_min=30.0)
     topo = sc.city.topologies
-    h0 = np.zeros(topo.surface_topology.cell_count, np.float32)
-    h0[7] = np.inf  # an unbounded depth poisons the neighbourhood
-    topo.surface_state = TriangularSurfaceState(h0, np.zeros_like(h0), np.zeros_like(h0))
-    cfg = load_config(None, {**sc.overrides, "solver.finite_check_interval_steps": 10})
+    zi, zf = np.zeros(0, np.int32), np.zeros(0, np.float32)
+    topo.coupling_topology = TriangularNodeCouplingTopology(
+        inlet_cell_index=zi, inlet_node_index=zi, node_surface_cell_index=np.array([57], np.int32),
+        node_invert_elevation_m=np.array([-2.0], np.float32), node_storage_area_m2=np.array([1.0], np.float32),
+        node_max_depth_m=np.array([1.0], np.float32))
+    topo.pipe_topology = TriangularPipeNetworkTopology(
+        link_from_node_index=zi, link_to_node_index=zi, link_length_m=zf, link_area_m2=zf,
+        link_hydraulic_radius_m=zf, link_manning_n=zf)
+    topo.pipe_state = TriangularPipeNetworkState(np.array([np.inf]), np.zeros(0))
+    cfg = load_config(None, {**sc.overrides, "solver.finite_check_interval_steps": 1})
     s = solver_for_city(sc.city, sc.rainfall, cfg)
     try:
         with pytest.raises(SimulationError, match="Non-finite depth"):
             s.run()
+        assert s.progress().step_count <= 3
     finally:
         s.close()
 
