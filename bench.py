@@ -51,7 +51,7 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--profile", choices=["loop", "kernels"], default=None,
                    help="ncu helper: open a profiler range around 64 solver steps of a wet run (loop) or "
-                        "around 3 isolated launches of each step kernel (kernels); prints nothing else")
+                        "around 2 isolated launches of each step kernel (kernels); prints nothing else")
     p.add_argument("--profile-start-s", type=float, default=900.0)
     return p.parse_args()
 
@@ -367,7 +367,7 @@ def profile_arm(args):
             pass  # the step cap ends the slice
     else:
         for k in range(4):
-            solver.time_kernel(k, reps=3)
+            solver.time_kernel(k, reps=1)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     p = solver.progress()
