@@ -1,9 +1,7 @@
 // Device helpers: Riemann flux, float-float volume arithmetic, the step
-// planner and block reductions.  The translation units that include this
-// header are compiled with -fmad=false so every float32 expression rounds
-// exactly as written (and as the reference's elementwise NumPy/CuPy
-// operations round), and so that a flux evaluated by both cells of an edge,
-// or a request evaluated by both ends of a coupling, is bit-identical.
+// planner and warp reductions.  The drainage translation unit is compiled
+// with -fmad=false so that a request or transfer evaluated at several call
+// sites (both ends of a coupling, both ends of a link) is bit-identical.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -23,59 +21,52 @@ struct EdgeFlux {
     float huR, hvR;   // momentum flux seen by the right cell
 };
 
-// HLL normal flux of the shallow-water equations on the reconstructed
-// states (reference equations.py:20-81).
-__device__ __forceinline__ void hll(float h_left, float hu_left, float hv_left, float h_right,
-                                    float hu_right, float hv_right, float nx, float ny, float g,
-                                    float half_g, float md, float &fh, float &fhu, float &fhv) {
-    const float h_l = fmax32(h_left, 0.0f), h_r = fmax32(h_right, 0.0f);
-    const bool wet_l = h_l > md, wet_r = h_r > md;
-    const float u_l = wet_l ? hu_left / fmax32(h_l, md) : 0.0f;
-    const float v_l = wet_l ? hv_left / fmax32(h_l, md) : 0.0f;
-    const float u_r = wet_r ? hu_right / fmax32(h_r, md) : 0.0f;
-    const float v_r = wet_r ? hv_right / fmax32(h_r, md) : 0.0f;
-    const float un_l = u_l * nx + v_l * ny;
-    const float un_r = u_r * nx + v_r * ny;
-    const float c_l = sqrtf(g * h_l), c_r = sqrtf(g * h_r);
-    const float p_l = half_g * h_l * h_l, p_r = half_g * h_r * h_r;
-    const float fhl = h_l * un_l, fhul = hu_left * un_l + p_l * nx, fhvl = hv_left * un_l + p_l * ny;
-    const float fhr = h_r * un_r, fhur = hu_right * un_r + p_r * nx, fhvr = hv_right * un_r + p_r * ny;
-    const float sl = fmin32(un_l - c_l, un_r - c_r);
-    const float sr = fmax32(un_l + c_l, un_r + c_r);
-    if (!(wet_l || wet_r)) {
-        fh = 0.0f; fhu = 0.0f; fhv = 0.0f;
-        return;
-    }
-    if (sl >= 0.0f) {
-        fh = fhl; fhu = fhul; fhv = fhvl;
-    } else if (sr <= 0.0f) {
-        fh = fhr; fhu = fhur; fhv = fhvr;
-    } else {
-        const float denom = (fabsf(sr - sl) > 1.0e-12f) ? (sr - sl) : 1.0f;
-        const float slsr = sl * sr;
-        fh = (sr * fhl - sl * fhr + slsr * (h_r - h_l)) / denom;
-        fhu = (sr * fhul - sl * fhur + slsr * (hu_right - hu_left)) / denom;
-        fhv = (sr * fhvl - sl * fhvr + slsr * (hv_right - hv_left)) / denom;
-    }
-}
+// Approximate reciprocal (MUFU) and square root: the surface kernel's flux
+// arithmetic is instruction-bound, and these keep it within a few ulp of the
+// correctly rounded operations the reference uses.
+__device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ float fsqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
 
-// Hydrostatic-reconstruction flux pair (reference equations.py:84-152):
-// both cells of an edge call this with the same (left, right) arguments and
-// get bit-identical results.
+// Hydrostatic-reconstruction flux pair with the HLL Riemann solver on the
+// reconstructed states (reference equations.py:20-152).  Same algebra as the
+// reference with three rewrites that do not change the value beyond rounding:
+// a velocity is a product with one reciprocal of the depth; the HLL velocity
+// of a reconstructed state (hu* / h* with hu* = u h*) is u itself; and the
+// three HLL branches are evaluated and selected without branching.  Both
+// cells of an edge call this with the edge's own (left, right) order at a
+// single call site, so they get bit-identical results.
 __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, float zL, float hR,
                                             float huR, float hvR, float zR, float nx, float ny,
                                             float g, float half_g, float md) {
     const float h_l = fmax32(hL, 0.0f), h_r = fmax32(hR, 0.0f);
-    const float eta_l = h_l + zL, eta_r = h_r + zR;
     const float zs = fmax32(zL, zR);
-    const float hls = fmax32(eta_l - zs, 0.0f), hrs = fmax32(eta_r - zs, 0.0f);
-    const bool wl = h_l > md, wr = h_r > md;
-    const float u_l = wl ? huL / fmax32(h_l, md) : 0.0f;
-    const float v_l = wl ? hvL / fmax32(h_l, md) : 0.0f;
-    const float u_r = wr ? huR / fmax32(h_r, md) : 0.0f;
-    const float v_r = wr ? hvR / fmax32(h_r, md) : 0.0f;
-    float fh, fhu, fhv;
-    hll(hls, u_l * hls, v_l * hls, hrs, u_r * hrs, v_r * hrs, nx, ny, g, half_g, md, fh, fhu, fhv);
+    const float hls = fmax32(h_l + zL - zs, 0.0f), hrs = fmax32(h_r + zR - zs, 0.0f);
+    const float il = h_l > md ? rcp(h_l) : 0.0f;
+    const float ir = h_r > md ? rcp(h_r) : 0.0f;
+    const float u_l = huL * il, v_l = hvL * il, u_r = huR * ir, v_r = hvR * ir;
+    const bool wl = hls > md, wr = hrs > md;
+    const float un_l = wl ? u_l * nx + v_l * ny : 0.0f;
+    const float un_r = wr ? u_r * nx + v_r * ny : 0.0f;
+    const float c_l = fsqrt(g * hls), c_r = fsqrt(g * hrs);
+    const float p_l = half_g * hls * hls, p_r = half_g * hrs * hrs;
+    const float hul = u_l * hls, hvl = v_l * hls, hur = u_r * hrs, hvr = v_r * hrs;
+    const float fhl = hls * un_l, fhul = hul * un_l + p_l * nx, fhvl = hvl * un_l + p_l * ny;
+    const float fhr = hrs * un_r, fhur = hur * un_r + p_r * nx, fhvr = hvr * un_r + p_r * ny;
+    const float sl = fmin32(un_l - c_l, un_r - c_r);
+    const float sr = fmax32(un_l + c_l, un_r + c_r);
+    const float d = sr - sl;
+    const float inv = fabsf(d) > 1.0e-12f ? rcp(d) : 1.0f;
+    const float slsr = sl * sr;
+    const float mh = (sr * fhl - sl * fhr + slsr * (hrs - hls)) * inv;
+    const float mhu = (sr * fhul - sl * fhur + slsr * (hur - hul)) * inv;
+    const float mhv = (sr * fhvl - sl * fhvr + slsr * (hvr - hvl)) * inv;
+    const bool left = sl >= 0.0f, right = sr <= 0.0f, dry = !(wl || wr);
+    float fh = left ? fhl : (right ? fhr : mh);
+    float fhu = left ? fhul : (right ? fhur : mhu);
+    float fhv = left ? fhvl : (right ? fhvr : mhv);
+    fh = dry ? 0.0f : fh;
+    fhu = dry ? 0.0f : fhu;
+    fhv = dry ? 0.0f : fhv;
     const float pcl = half_g * (h_l * h_l - hls * hls);
     const float pcr = half_g * (h_r * h_r - hrs * hrs);
     EdgeFlux f;
@@ -86,6 +77,13 @@ __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, floa
     f.hvR = fhv + pcr * ny;
     return f;
 }
+
+// Correctly rounded, never-contracted float32 operations for the parts whose
+// results are compared bit-for-bit with the reference (CFL dt, velocity clamp).
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
 
 // Ghost right state of a non-active-interior edge (reference
 // triangular_backend.py:1294-1327): reflective for codes 0/2, fixed stage
@@ -201,30 +199,17 @@ static __device__ __noinline__ void plan_step(RunCtrl *run, double *snap_t, cons
 }
 
 // --------------------------------------------------------------- reductions
+// Per-warp running ledger: lane 0 adds the warp's float32 sums into the
+// warp's own float64 slots (no block barrier; slot = global warp index).
 template <int NT>
-__device__ __forceinline__ void block_add_ledger(const float (&v)[NT], double *ledger) {
-    __shared__ float red[32][NT];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float x[NT];
+__device__ __forceinline__ void warp_add_ledger(const float (&v)[NT], double *ledger) {
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 #pragma unroll
     for (int j = 0; j < NT; ++j) {
-        x[j] = v[j];
+        float x = v[j];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x[j] += __shfl_down_sync(0xffffffffu, x[j], o);
-    }
-    if (lane == 0) {
-#pragma unroll
-        for (int j = 0; j < NT; ++j) red[warp][j] = x[j];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-        for (int j = 0; j < NT; ++j) {
-            double acc = 0.0;
-            for (int w = 0; w < nw; ++w) acc += (double)red[w][j];
-            ledger[(size_t)blockIdx.x * NT + j] += acc;
-        }
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) ledger[(size_t)warp * NT + j] += (double)x;
     }
 }
 

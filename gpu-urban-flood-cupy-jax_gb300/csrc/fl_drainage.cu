@@ -12,13 +12,16 @@
 // conserved exactly as in the reference and runs are reproducible.
 //
 // Two launches per step:
-//   k_inlets  one thread per inlet cell (depth after the exchange) and one per
-//             node (volume after the exchange)              [reference :52-177]
+//   k_inlets  one thread per inlet cell (depth after the exchange), one per
+//             node (volume after the exchange)               [reference :52-177]
+//             and one per link: the semi-implicit link update from the two
+//             end volumes after the exchange (recomputed with the node
+//             threads' own code, so bit-identical)         [pipe network :39-139]
 //   k_network one thread per drainage group = a surface cell together with
-//             the nodes that overflow into it (or an orphan node): link
-//             momentum update with donor limiting, node continuity, outfall,
+//             the nodes that overflow into it (or an orphan node): donor
+//             limiting of the link transfers, node continuity, outfall,
 //             overflow return and the cell's final depth      [reference
-//             pipe network :39-211, overflow :179-207]
+//             pipe network :141-211, overflow :179-207]
 //
 // Heads are carried as depth relative to a static per-link / per-inlet datum
 // offset (bed - invert, invert_from - invert_to, ...), so float32 keeps
@@ -89,6 +92,76 @@ __device__ __forceinline__ float node_surcharge_factor(const D1Args &a, const fl
     return fmin32(1.0f, fmax32(ff_val(V), 0.0f) / fmax32(sum, 1.0e-12f));
 }
 
+// Node volume after the inlet exchange (float-float), reference apply kernel
+// :133-177 plus the node-side sum.
+__device__ __forceinline__ float2 node_after_inlets(const D1Args &a, const float4 *hs, int n, float dt) {
+    const float2 V = ff_clamp0(a.Va[n]);
+    const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
+    if (j0 == j1) return V;
+    const float An = a.node_area[n];
+    const float surf = node_surcharge_factor(a, hs, n, dt);
+    float dv = 0.0f;
+    for (int j = j0; j < j1; ++j) {
+        const int i = a.node_in_list[j];
+        const Req r = inlet_request(a, i, hs[a.in_cell[i]].x, V, An, dt);
+        const float cap = r.cap * cell_capture_factor(a, hs, a.in_kcell[i], dt);
+        const float sur = r.sur * surf;
+        dv += cap - sur;
+    }
+    return ff_add(V, dv);
+}
+
+// Semi-implicit Saint-Venant link update with circular/Preissmann or
+// rectangular geometry (reference pipe_link_flow_kernel :39-139); returns the
+// signed transfer volume of the step.  Heads enter as end depths plus the
+// link's static datum offsets.
+__device__ __forceinline__ float link_transfer(float4 k0, float4 k1, float4 k2, float df, float dtn, float q,
+                                               float g, float wave_speed, float dt) {
+    const float depth = fmax32(0.5f * (df + dtn) + k0.z, 0.0f);
+    const int flags = (int)k2.w;
+    float area, radius;
+    if (flags & 1) {
+        const float dia = fmax32(k1.x, 1.0e-12f);
+        const float rg = 0.5f * dia;
+        const float od = fmin32(depth, dia);
+        const float ratio = fmax32(fmin32((rg - od) / rg, 1.0f), -1.0f);
+        const float theta = 2.0f * acosf(ratio);
+        const float oa = 0.5f * rg * rg * (theta - sinf(theta));
+        const float fa = 0.25f * 3.14159265358979323846f * dia * dia;
+        const bool full = depth >= dia;
+        const float ca = full ? fa : oa;
+        const float cp = full ? 3.14159265358979323846f * dia : rg * theta;
+        const float sw = g * fa / fmax32(wave_speed * wave_speed, 1.0e-12f);
+        const float pd = fmax32(depth - dia, 0.0f);
+        area = ca + sw * pd;
+        radius = ca / fmax32(cp, 1.0e-12f);
+    } else {
+        area = k1.y;
+        radius = k1.z;
+    }
+    if (flags & 2) {
+        const float od = fmin32(fmax32(depth, 0.0f), fmax32(k2.z, 1.0e-6f));
+        const float oa = fmax32(k2.y, 1.0e-6f) * od;
+        const float op = fmax32(k2.y + 2.0f * od, 1.0e-12f);
+        area = oa;
+        radius = oa / op;
+    }
+    const float len = fmax32(k0.x, 1.0e-6f);
+    const float sa = fmax32(area, 1.0e-12f);
+    const float sr = fmax32(radius, 1.0e-12f);
+    const float slope = (k0.y + (df - dtn)) / len;
+    const float fric = g * k0.w * k0.w * fabsf(q) / (powf(sr, 4.0f / 3.0f) * sa);
+    const float minor = k1.w * fabsf(q) / (2.0f * len * sa);
+    const float num = q + g * sa * dt * slope;
+    float up = num / (1.0f + dt * (fric + minor));
+    up = fmin32(fmax32(up, -k2.x), k2.x);
+    return up * dt;
+}
+
+__device__ __forceinline__ float node_depth(float2 V, float A) {
+    return fmax32(ff_val(ff_clamp0(V)), 0.0f) / fmax32(A, 1.0e-12f);
+}
+
 __global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a, int slot) {
     wait_for_previous_grid();
     const StepCtrl s = a.ctrl[slot];
@@ -117,93 +190,26 @@ __global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a
         a.hc_out[k] = h + dh;
     } else if (t < a.K + a.N) {
         const int n = t - a.K;
-        const float2 V = ff_clamp0(a.Va[n]);
-        const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
-        if (j0 == j1) {
-            a.Vb[n] = V;
-        } else {
-            const float An = a.node_area[n];
-            const float surf = node_surcharge_factor(a, hs, n, dt);
-            float dv = 0.0f;
-            for (int j = j0; j < j1; ++j) {
-                const int i = a.node_in_list[j];
-                const Req r = inlet_request(a, i, hs[a.in_cell[i]].x, V, An, dt);
-                const float cap = r.cap * cell_capture_factor(a, hs, a.in_kcell[i], dt);
-                const float sur = r.sur * surf;
-                dv += cap - sur;
-            }
-            a.Vb[n] = ff_add(V, dv);
-        }
+        a.Vb[n] = node_after_inlets(a, hs, n, dt);
+    } else if (t < a.K + a.N + a.L) {
+        const int l = t - a.K - a.N;
+        const int f = a.link_from[l], to = a.link_to[l];
+        const float df = node_depth(node_after_inlets(a, hs, f, dt), a.node_area[f]);
+        const float dtn = node_depth(node_after_inlets(a, hs, to, dt), a.node_area[to]);
+        const float *Qin = s.parity ? a.Q1 : a.Q0;
+        a.T[l] = link_transfer(a.lk0[l], a.lk1[l], a.lk2[l], df, dtn, Qin[l], a.g, a.wave_speed, dt);
     }
-    block_add_ledger<D1_TERMS>(led, a.ledger);
-}
-
-// --------------------------------------------------------------- links
-
-struct Transfer {
-    float t;      // signed transfer volume this step (m^3)
-    int donor;
-};
-
-// Semi-implicit Saint-Venant link update with circular/Preissmann or
-// rectangular geometry (reference pipe_link_flow_kernel :39-139).
-__device__ __forceinline__ Transfer link_transfer(const D2Args &a, const float *Qin, int l, float dt) {
-    const int f = a.link_from[l], to = a.link_to[l];
-    const float4 k0 = a.lk0[l], k1 = a.lk1[l], k2 = a.lk2[l];
-    const float Af = a.nd0[f].x, At = a.nd0[to].x;
-    const float df = fmax32(ff_val(ff_clamp0(a.Vb[f])), 0.0f) / fmax32(Af, 1.0e-12f);
-    const float dtn = fmax32(ff_val(ff_clamp0(a.Vb[to])), 0.0f) / fmax32(At, 1.0e-12f);
-    const float depth = fmax32(0.5f * (df + dtn) + k0.z, 0.0f);
-    const int flags = (int)k2.w;
-    float area, radius;
-    if (flags & 1) {
-        const float dia = fmax32(k1.x, 1.0e-12f);
-        const float rg = 0.5f * dia;
-        const float od = fmin32(depth, dia);
-        const float ratio = fmax32(fmin32((rg - od) / rg, 1.0f), -1.0f);
-        const float theta = 2.0f * acosf(ratio);
-        const float oa = 0.5f * rg * rg * (theta - sinf(theta));
-        const float fa = 0.25f * 3.14159265358979323846f * dia * dia;
-        const bool full = depth >= dia;
-        const float ca = full ? fa : oa;
-        const float cp = full ? 3.14159265358979323846f * dia : rg * theta;
-        const float sw = a.g * fa / fmax32(a.wave_speed * a.wave_speed, 1.0e-12f);
-        const float pd = fmax32(depth - dia, 0.0f);
-        area = ca + sw * pd;
-        radius = ca / fmax32(cp, 1.0e-12f);
-    } else {
-        area = k1.y;
-        radius = k1.z;
-    }
-    if (flags & 2) {
-        const float od = fmin32(fmax32(depth, 0.0f), fmax32(k2.z, 1.0e-6f));
-        const float oa = fmax32(k2.y, 1.0e-6f) * od;
-        const float op = fmax32(k2.y + 2.0f * od, 1.0e-12f);
-        area = oa;
-        radius = oa / op;
-    }
-    const float len = fmax32(k0.x, 1.0e-6f);
-    const float sa = fmax32(area, 1.0e-12f);
-    const float sr = fmax32(radius, 1.0e-12f);
-    const float q = Qin[l];
-    const float slope = (k0.y + (df - dtn)) / len;
-    const float fric = a.g * k0.w * k0.w * fabsf(q) / (powf(sr, 4.0f / 3.0f) * sa);
-    const float minor = k1.w * fabsf(q) / (2.0f * len * sa);
-    const float num = q + a.g * sa * dt * slope;
-    float up = num / (1.0f + dt * (fric + minor));
-    up = fmin32(fmax32(up, -k2.x), k2.x);
-    Transfer r;
-    r.t = up * dt;
-    r.donor = r.t >= 0.0f ? f : to;
-    return r;
+    warp_add_ledger<D1_TERMS>(led, a.ledger);
 }
 
 // Sum of |transfer| over the links whose donor is node d.
-__device__ __forceinline__ float donor_request(const D2Args &a, const float *Qin, int d, float dt) {
+__device__ __forceinline__ float donor_request(const D2Args &a, int d) {
     float sum = 0.0f;
     for (int j = a.node_link_start[d]; j < a.node_link_start[d + 1]; ++j) {
-        const Transfer tr = link_transfer(a, Qin, a.node_link_list[j], dt);
-        if (tr.donor == d) sum += fabsf(tr.t);
+        const int l = a.node_link_list[j];
+        const float t = a.T[l];
+        const int donor = t >= 0.0f ? a.link_from[l] : a.link_to[l];
+        if (donor == d) sum += fabsf(t);
     }
     return sum;
 }
@@ -213,7 +219,6 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args 
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
     float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
-    const float *Qin = s.parity ? a.Q1 : a.Q0;
     float *Qout = s.parity ? a.Q0 : a.Q1;
     const float dt = s.dt_f;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -232,33 +237,28 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args 
             const float2 Vp = ff_clamp0(a.Vb[n]);
             const float Vpf = fmax32(ff_val(Vp), 0.0f);
             const int j0 = a.node_link_start[n], j1 = a.node_link_start[n + 1];
-            // donor request of this node
-            float own = 0.0f;
-            for (int j = j0; j < j1; ++j) {
-                const Transfer tr = link_transfer(a, Qin, a.node_link_list[j], dt);
-                if (tr.donor == n) own += fabsf(tr.t);
-            }
+            const float own = donor_request(a, n);
             float dv = 0.0f;
             for (int j = j0; j < j1; ++j) {
                 const int l = a.node_link_list[j];
-                const Transfer tr = link_transfer(a, Qin, l, dt);
+                const float t = a.T[l];
+                const int from = a.link_from[l], to = a.link_to[l];
+                const int d = t >= 0.0f ? from : to;
                 float factor;
-                if (tr.donor == n) {
+                if (d == n) {
                     factor = fmin32(1.0f, Vpf / fmax32(own, 1.0e-12f));
                 } else {
-                    const int d = tr.donor;
                     const float Vd = fmax32(ff_val(ff_clamp0(a.Vb[d])), 0.0f);
-                    factor = fmin32(1.0f, Vd / fmax32(donor_request(a, Qin, d, dt), 1.0e-12f));
+                    factor = fmin32(1.0f, Vd / fmax32(donor_request(a, d), 1.0e-12f));
                 }
-                const float lim = fabsf(tr.t) * factor;
-                const int from = a.link_from[l];
-                const float sgn = (tr.donor == from) ? lim : -lim;
+                const float lim = fabsf(t) * factor;
+                const float sgn = (d == from) ? lim : -lim;
                 if (from == n) {
                     dv -= sgn;
                     Qout[l] = sgn / fmax32(dt, 1.0e-12f);
                     led[3] += lim;
                 }
-                if (a.link_to[l] == n) dv += sgn;
+                if (to == n) dv += sgn;
             }
             float2 V = ff_clamp0(ff_add(Vp, dv));
             // outfall (reference pipe_outfall_kernel :176-211)
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args 
             if (s.snap_slot >= 0) a.snap_h[(size_t)s.snap_slot * (size_t)a.C + c] = hf;
         }
     }
-    block_add_ledger<D2_TERMS>(led, a.ledger);
+    warp_add_ledger<D2_TERMS>(led, a.ledger);
 }
 
 static cudaError_t launch_pdl2(const void *func, dim3 grid, dim3 block, void **args, cudaStream_t stream) {
@@ -308,12 +308,12 @@ static cudaError_t launch_pdl2(const void *func, dim3 grid, dim3 block, void **a
     return cudaLaunchKernelExC(&cfg, func, args);
 }
 
-int inlet_blocks(int32_t K, int32_t N) { return (K + N + 127) / 128 > 0 ? (K + N + 127) / 128 : 1; }
+int inlet_blocks(int32_t K, int32_t N, int32_t L) { return (K + N + L + 127) / 128 > 0 ? (K + N + L + 127) / 128 : 1; }
 int network_blocks(int32_t G) { return (G + 127) / 128 > 0 ? (G + 127) / 128 : 1; }
 
 cudaError_t launch_inlets(const D1Args &a, int slot, cudaStream_t stream) {
     void *args[] = {(void *)&a, (void *)&slot};
-    return launch_pdl2((const void *)k_inlets, dim3(inlet_blocks(a.K, a.N)), dim3(128), args, stream);
+    return launch_pdl2((const void *)k_inlets, dim3(inlet_blocks(a.K, a.N, a.L)), dim3(128), args, stream);
 }
 
 cudaError_t launch_network(const D2Args &a, int slot, cudaStream_t stream) {

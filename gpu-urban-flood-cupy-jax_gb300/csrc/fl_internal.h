@@ -76,7 +76,7 @@ struct HyetoView {
     int32_t n;
 };
 
-// Ledger slots of the per-block running sums.
+// Ledger slots of the per-warp running sums.
 constexpr int SURF_TERMS = 4;   // rain, infil, boundary in, boundary out
 constexpr int D1_TERMS = 2;     // capture, surcharge
 constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer|
@@ -90,7 +90,7 @@ struct SurfArgs {
     StepCtrl *ctrl;
     RunCtrl *run;
     HyetoView hy;
-    double *ledger;               // [gridDim.x * SURF_TERMS]
+    double *ledger;               // [warps * SURF_TERMS]
     float *snap_h, *snap_hu, *snap_hv;
     double *snap_t;
     int32_t C;
@@ -126,10 +126,16 @@ struct D1Args {
     float *hc_out;                // depth of each inlet cell after the exchange
     const float2 *Va;             // node volume (float-float) before
     float2 *Vb;                   // after the exchange
+    // links: the transfer volume of each link this step
+    const int32_t *link_from, *link_to;
+    const float4 *lk0, *lk1, *lk2;
+    const float *Q0, *Q1;         // link flow, ping-pong with the state parity
+    float *T;
     StepCtrl *ctrl;
-    double *ledger;               // [gridDim.x * D1_TERMS]
-    int32_t K, N;
+    double *ledger;               // [warps * D1_TERMS]
+    int32_t K, N, L;
     int32_t rule;
+    float g, wave_speed;
     float coef_area;              // float32(Cd * A_orifice)
     float weir_coef_perim;        // float32(Cw * perimeter) for weir_orifice
     float g2;                     // 2 g (float32)
@@ -149,11 +155,12 @@ struct D2Args {
     const float *hc_out;
     const float2 *Vb;             // after the inlet exchange
     float2 *Va;                   // final
+    const float *T;               // link transfer volumes (k_inlets)
     float *Q0, *Q1;               // link flow, ping-pong with the state parity
     float *wet;
     float *snap_h, *snap_v;
     StepCtrl *ctrl;
-    double *ledger;               // [gridDim.x * D2_TERMS]
+    double *ledger;               // [warps * D2_TERMS]
     int32_t G, C, N;
     int32_t forcing_kind;
     float g, md, wave_speed;

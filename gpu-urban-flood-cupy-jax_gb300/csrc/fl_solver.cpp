@@ -55,7 +55,7 @@ cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *g1,
                            int32_t C, int32_t N, double *out2, cudaStream_t stream);
 cudaError_t launch_inlets(const D1Args &a, int slot, cudaStream_t stream);
 cudaError_t launch_network(const D2Args &a, int slot, cudaStream_t stream);
-int inlet_blocks(int32_t K, int32_t N);
+int inlet_blocks(int32_t K, int32_t N, int32_t L);
 int network_blocks(int32_t G);
 
 }  // namespace fl
@@ -344,7 +344,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     float *dt_partial;
     unsigned int *counter;
     if ((rc = s->alloc(&dt_partial, s->dt_blocks)) || (rc = s->alloc(&counter, 1)) || (rc = s->alloc(&s->dt_out, 1)) ||
-        (rc = s->alloc(&s->vol_out, 2)) || (rc = s->alloc(&s->led_s, (size_t)s->surf_blocks * SURF_TERMS)))
+        (rc = s->alloc(&s->vol_out, 2)) || (rc = s->alloc(&s->led_s, (size_t)s->surf_blocks * 8 * SURF_TERMS)))
         return rc;
     FL_CUDA(cudaMemset(counter, 0, sizeof(unsigned int)));
     for (int b = 0; b < 3; ++b)
@@ -378,11 +378,14 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         FL_CUDA(cudaMemset(s->Vb, 0, sizeof(float2) * s->N));
         FL_CUDA(cudaMemset(s->Q[0], 0, sizeof(float) * std::max(s->NL, 1)));
         FL_CUDA(cudaMemset(s->Q[1], 0, sizeof(float) * std::max(s->NL, 1)));
-        s->d1_blocks = inlet_blocks(s->K, s->N);
+        s->d1_blocks = inlet_blocks(s->K, s->N, s->NL);
         s->d2_blocks = network_blocks(s->G);
-        if ((rc = s->alloc(&s->led_1, (size_t)s->d1_blocks * D1_TERMS)) ||
-            (rc = s->alloc(&s->led_2, (size_t)s->d2_blocks * D2_TERMS)))
+        float *T;
+        if ((rc = s->alloc(&s->led_1, (size_t)s->d1_blocks * 4 * D1_TERMS)) ||
+            (rc = s->alloc(&s->led_2, (size_t)s->d2_blocks * 4 * D2_TERMS)) || (rc = s->alloc(&T, s->NL)))
             return rc;
+        s->d1.T = T;
+        s->d2.T = T;
         D1Args &a = s->d1;
         a.in_cell = in_cell;
         a.in_node = in_node;
@@ -403,6 +406,16 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         a.ledger = s->led_1;
         a.K = s->K;
         a.N = s->N;
+        a.link_from = lf;
+        a.link_to = lt;
+        a.lk0 = lk0;
+        a.lk1 = lk1;
+        a.lk2 = lk2;
+        a.Q0 = s->Q[0];
+        a.Q1 = s->Q[1];
+        a.L = s->NL;
+        a.g = (float)p.gravity_mps2;
+        a.wave_speed = drain->pressurized_wave_speed_mps;
         a.rule = drain->inlet_capture_rule;
         a.coef_area = drain->inlet_orifice_coefficient * drain->inlet_orifice_area_m2;
         const float eq = sqrtf(4.0f * 3.14159265358979323846f * std::max(drain->inlet_orifice_area_m2, 0.0f));
@@ -547,10 +560,10 @@ FL_API int fl_reset_clock(FlSolver *s, void *stream) {
     FL_CUDA(cudaMemcpyAsync(s->run, s->run_h, sizeof(RunCtrl), cudaMemcpyHostToDevice, st));
     FL_CUDA(cudaMemsetAsync(s->ctrl, 0, sizeof(StepCtrl) * 2, st));
     FL_CUDA(cudaMemsetAsync(s->wet, 0, sizeof(float) * (size_t)s->C, st));
-    FL_CUDA(cudaMemsetAsync(s->led_s, 0, sizeof(double) * (size_t)s->surf_blocks * SURF_TERMS, st));
+    FL_CUDA(cudaMemsetAsync(s->led_s, 0, sizeof(double) * (size_t)s->surf_blocks * 8 * SURF_TERMS, st));
     if (s->has_drain()) {
-        FL_CUDA(cudaMemsetAsync(s->led_1, 0, sizeof(double) * (size_t)s->d1_blocks * D1_TERMS, st));
-        FL_CUDA(cudaMemsetAsync(s->led_2, 0, sizeof(double) * (size_t)s->d2_blocks * D2_TERMS, st));
+        FL_CUDA(cudaMemsetAsync(s->led_1, 0, sizeof(double) * (size_t)s->d1_blocks * 4 * D1_TERMS, st));
+        FL_CUDA(cudaMemsetAsync(s->led_2, 0, sizeof(double) * (size_t)s->d2_blocks * 4 * D2_TERMS, st));
     }
     FL_CUDA(cudaStreamSynchronize(st));
     s->slot = 0;
@@ -868,12 +881,12 @@ FL_API int fl_read_ledger(FlSolver *s, double *out, int32_t n, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
     double all[FL_LEDGER_COUNT] = {0};
-    std::vector<double> v((size_t)s->surf_blocks * SURF_TERMS);
+    std::vector<double> v((size_t)s->surf_blocks * 8 * SURF_TERMS);
     FL_CUDA(cudaMemcpyAsync(v.data(), s->led_s, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, st));
     FL_CUDA(cudaStreamSynchronize(st));
     sum_blocks(v, SURF_TERMS, all + FL_LEDGER_RAINFALL);
     if (s->has_drain()) {
-        std::vector<double> v1((size_t)s->d1_blocks * D1_TERMS), v2((size_t)s->d2_blocks * D2_TERMS);
+        std::vector<double> v1((size_t)s->d1_blocks * 4 * D1_TERMS), v2((size_t)s->d2_blocks * 4 * D2_TERMS);
         FL_CUDA(cudaMemcpyAsync(v1.data(), s->led_1, sizeof(double) * v1.size(), cudaMemcpyDeviceToHost, st));
         FL_CUDA(cudaMemcpyAsync(v2.data(), s->led_2, sizeof(double) * v2.size(), cudaMemcpyDeviceToHost, st));
         FL_CUDA(cudaStreamSynchronize(st));

@@ -12,6 +12,12 @@
 // stays exactly conservative without atomics; summation order per cell is
 // fixed, so runs are bitwise reproducible.
 //
+// The flux arithmetic uses reciprocal-based division and fast exp/log (the
+// kernel is instruction-bound); values stay within a few ulp of the
+// reference's correctly rounded float32 operations.  The velocity clamp and
+// the CFL dt use correctly rounded, uncontracted operations and match the
+// reference bit-for-bit.
+//
 // k_dt: the global CFL minimum (equations.py:155-178) as a warp-shuffle and
 // single-pass grid reduction; the last block to finish plans the step.
 #include "fl_device.cuh"
@@ -42,28 +48,40 @@ __global__ void __launch_bounds__(256) k_surface(const __grid_constant__ SurfArg
         const float dt = s.dt_f;
         const float md = a.md;
         float hn = 0.0f, hun = 0.0f, hvn = 0.0f;
+        const bool act = (tp.w & CELL_ACTIVE) != 0;
         if (!do_surface) {
             hn = st.x; hun = st.y; hvn = st.z;
-        } else if (tp.w & CELL_ACTIVE) {
+        } else if (act || (tp.w & CELL_STAGE_LEDGER)) {
+            // An inactive cell only evaluates its exterior stage edges: the
+            // reference counts their flux in the boundary ledger and then
+            // zeroes the cell.
+            const float4 own = act ? st : make_float4(0.0f, 0.0f, 0.0f, st.w);
             float L0 = 0.0f, L1 = 0.0f, L2 = 0.0f, R0 = 0.0f, R1 = 0.0f, R2 = 0.0f;
             float bin = 0.0f, bout = 0.0f;
-            const float4 gk[3] = {a.g0[c], a.g1[c], a.g2[c]};
-            const uint32_t wk[3] = {tp.x, tp.y, tp.z};
-#pragma unroll
+            const float4 g0 = a.g0[c], g1 = a.g1[c], g2 = a.g2[c];
+            // one flux code path for all three edges (not unrolled): both cells
+            // of an edge run the identical instruction sequence
+#pragma unroll 1
             for (int k = 0; k < 3; ++k) {
-                const uint32_t w = wk[k];
+                const uint32_t w = k == 0 ? tp.x : (k == 1 ? tp.y : tp.z);
+                const float4 gk = k == 0 ? g0 : (k == 1 ? g1 : g2);
                 if (w == SLOT_NONE) continue;
                 const uint32_t other = w & IDX_MASK;
                 const bool interior = other != NO_CELL;
                 const bool oact = (w & OTHER_ACTIVE_BIT) != 0;
+                const bool is_right = (w & RIGHT_BIT) != 0;
                 const int raw = (int)((w >> CODE_SHIFT) & 7u) - 1;
-                const float nx = gk[k].x, ny = gk[k].y, len = gk[k].z;
-                if (!(w & RIGHT_BIT)) {
-                    // this cell is the edge's left cell (and active)
-                    const bool ai = interior && oact;
-                    const int code = (interior && !oact) ? 0 : raw;
-                    const float4 r = ai ? in[other] : ghost_state(st.x, st.y, st.z, st.w, nx, ny, code, a.stage);
-                    EdgeFlux f = hr_flux(st.x, st.y, st.z, st.w, r.x, r.y, r.z, r.w, nx, ny, a.g, a.half_g, md);
+                const bool ai = interior && oact;
+                if (is_right && !ai) continue;  // the reference adds nothing here
+                if (!act && (is_right || interior || raw != 3)) continue;
+                const int code = (interior && !oact) ? 0 : raw;
+                const float nx = gk.x, ny = gk.y, len = gk.z;
+                // the edge's left and right states in the reference's orientation
+                const float4 o = ai ? in[other] : ghost_state(own.x, own.y, own.z, own.w, nx, ny, code, a.stage);
+                const float4 L = is_right ? o : own;
+                const float4 R = is_right ? own : o;
+                EdgeFlux f = hr_flux(L.x, L.y, L.z, L.w, R.x, R.y, R.z, R.w, nx, ny, a.g, a.half_g, md);
+                if (!is_right) {
                     if (!interior && code == 4 && f.h < 0.0f) {
                         f.h = 0.0f; f.huL = 0.0f; f.hvL = 0.0f;
                     }
@@ -75,86 +93,66 @@ __global__ void __launch_bounds__(256) k_surface(const __grid_constant__ SurfArg
                         bin += fmax32(-b, 0.0f);
                         bout += fmax32(b, 0.0f);
                     }
-                } else if (oact) {
-                    // this cell is the right cell of an active interior edge
-                    const float4 l = in[other];
-                    const EdgeFlux f = hr_flux(l.x, l.y, l.z, l.w, st.x, st.y, st.z, st.w, nx, ny, a.g, a.half_g, md);
+                } else {
                     R0 = R0 + f.h * len;
                     R1 = R1 + f.huR * len;
                     R2 = R2 + f.hvR * len;
                 }
             }
-            const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
-            const float area = gk[1].w;
-            hn = fmax32(st.x + dt * d0 / area, 0.0f);
-            hun = st.y + dt * d1 / area;
-            hvn = st.z + dt * d2 / area;
-            // semi-implicit Manning damping
-            const bool wet = hn > md;
-            const float hs = fmax32(hn, md);
-            const float uu = hun / hs, vv = hvn / hs;
-            const float speed = sqrtf(uu * uu + vv * vv);
-            const float n = gk[0].w;
-            const float damping = 1.0f + s.dtg_f * (n * n) * speed / powf(hs, 4.0f / 3.0f);
-            hun = wet ? hun / damping : 0.0f;
-            hvn = wet ? hvn / damping : 0.0f;
-            // rainfall, infiltration, momentum rescale, dry zeroing
-            float rain, infil;
-            if (KIND == 1) {
-                const float4 hz = a.horton[c];
-                rain = s.rain_f * hz.w;
-                infil = hz.y + (hz.x - hz.y) * expf(-hz.z * a.wet[c]);
-            } else {
-                rain = s.rain_f;
-                infil = a.infil_scalar;
-            }
-            const float rd = fmax32(rain, 0.0f) * dt;
-            const float h1 = hn + rd;
-            const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
-            const float h2 = h1 - id;
-            const float scale = (h1 > md) ? h2 / fmax32(h1, md) : 0.0f;
-            hun = hun * scale;
-            hvn = hvn * scale;
-            const bool wet2 = h2 > md;
-            hn = h2;
-            hun = wet2 ? hun : 0.0f;
-            hvn = wet2 ? hvn : 0.0f;
-            led[0] = rd * area;
-            led[1] = id * area;
             led[2] = bin;
             led[3] = bout;
-        } else if (tp.w & CELL_STAGE_LEDGER) {
-            // An inactive cell's exterior stage edges still move water in the
-            // reference's boundary ledger (the inactive cell is then zeroed).
-            float bin = 0.0f, bout = 0.0f;
-            const float4 gk[3] = {a.g0[c], a.g1[c], a.g2[c]};
-            const uint32_t wk[3] = {tp.x, tp.y, tp.z};
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const uint32_t w = wk[k];
-                if (w == SLOT_NONE || (w & RIGHT_BIT) || (w & IDX_MASK) != NO_CELL) continue;
-                const int raw = (int)((w >> CODE_SHIFT) & 7u) - 1;
-                if (raw != 3) continue;
-                const float4 r = ghost_state(0.0f, 0.0f, 0.0f, st.w, gk[k].x, gk[k].y, 3, a.stage);
-                const EdgeFlux f = hr_flux(0.0f, 0.0f, 0.0f, st.w, r.x, r.y, r.z, r.w, gk[k].x, gk[k].y, a.g, a.half_g, md);
-                const float b = f.h * gk[k].z * dt;
-                bin += fmax32(-b, 0.0f);
-                bout += fmax32(b, 0.0f);
+            if (act) {
+                const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
+                const float area = g1.w;
+                const float ia = rcp(area);
+                hn = fmax32(st.x + dt * d0 * ia, 0.0f);
+                hun = st.y + dt * d1 * ia;
+                hvn = st.z + dt * d2 * ia;
+                // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
+                const bool wet = hn > md;
+                const float hs = fmax32(hn, md);
+                const float ih = rcp(hs);
+                const float uu = hun * ih, vv = hvn * ih;
+                const float speed = fsqrt(uu * uu + vv * vv);
+                const float n = g0.w;
+                const float h43 = __expf(1.3333334f * __logf(hs));
+                const float damping = 1.0f + s.dtg_f * (n * n) * speed * rcp(h43);
+                const float idamp = rcp(damping);
+                hun = wet ? hun * idamp : 0.0f;
+                hvn = wet ? hvn * idamp : 0.0f;
+                // rainfall, infiltration, momentum rescale, dry zeroing
+                float rain, infil;
+                if (KIND == 1) {
+                    const float4 hz = a.horton[c];
+                    rain = s.rain_f * hz.w;
+                    infil = hz.y + (hz.x - hz.y) * __expf(-hz.z * a.wet[c]);
+                } else {
+                    rain = s.rain_f;
+                    infil = a.infil_scalar;
+                }
+                const float rd = fmax32(rain, 0.0f) * dt;
+                const float h1 = hn + rd;
+                const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
+                const float h2 = h1 - id;
+                const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
+                const bool wet2 = h2 > md;
+                hn = h2;
+                hun = wet2 ? hun * scale : 0.0f;
+                hvn = wet2 ? hvn * scale : 0.0f;
+                led[0] = rd * area;
+                led[1] = id * area;
             }
-            led[2] = bin;
-            led[3] = bout;
         }
         if (s.phases & FL_PHASE_CLAMP) {
-            const float speed = sqrtf(hun * hun + hvn * hvn) / fmax32(hn, 1.0e-8f);
-            const float scale = fmin32(1.0f, a.vmax / fmax32(speed, 1.0e-12f));
-            hun = hun * scale;
-            hvn = hvn * scale;
+            // velocity clamp, rounded exactly as the reference computes it
+            const float speed = xdiv(xsqrt(xadd(xmul(hun, hun), xmul(hvn, hvn))), fmax32(hn, 1.0e-8f));
+            const float scale = fmin32(1.0f, xdiv(a.vmax, fmax32(speed, 1.0e-12f)));
+            hun = xmul(hun, scale);
+            hvn = xmul(hvn, scale);
         }
         out[c] = make_float4(hn, hun, hvn, st.w);
         const bool final_here = !(drain_finishes && (tp.w & CELL_COUPLED));
-        if (do_surface && final_here) {
-            if (KIND == 1) a.wet[c] = a.wet[c] + dt * (float)(hn > md);
-        }
+        if (KIND == 1 && do_surface && final_here) a.wet[c] = a.wet[c] + dt * (float)(hn > md);
         if (s.snap_slot >= 0) {
             const size_t o = (size_t)s.snap_slot * (size_t)a.C + (size_t)c;
             if (final_here) a.snap_h[o] = hn;
@@ -162,7 +160,7 @@ __global__ void __launch_bounds__(256) k_surface(const __grid_constant__ SurfArg
             a.snap_hv[o] = hvn;
         }
     }
-    block_add_ledger<SURF_TERMS>(led, a.ledger);
+    warp_add_ledger<SURF_TERMS>(led, a.ledger);
 }
 
 template __global__ void k_surface<0>(const __grid_constant__ SurfArgs, int, int);
@@ -174,11 +172,12 @@ __global__ void __launch_bounds__(256) k_dt(const __grid_constant__ DtArgs a, in
     const float4 *__restrict__ st = a.run->parity ? a.state1 : a.state0;
     float best = CUDART_INF_F;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.C; c += gridDim.x * blockDim.x) {
+        // rounded exactly as the reference's float32 expression
         const float4 v = st[c];
         const float hs = fmax32(v.x, a.md);
-        const float u = v.y / hs, w = v.z / hs;
-        const float speed = sqrtf(u * u + w * w) + sqrtf(a.g * hs);
-        const float local = a.cfl * a.char_len[c] / fmax32(speed, 1.0e-12f);
+        const float u = xdiv(v.y, hs), w = xdiv(v.z, hs);
+        const float speed = xadd(xsqrt(xadd(xmul(u, u), xmul(w, w))), xsqrt(xmul(a.g, hs)));
+        const float local = xdiv(xmul(a.cfl, a.char_len[c]), fmax32(speed, 1.0e-12f));
         if (isfinite(local) && local < best) best = local;
     }
 #pragma unroll

@@ -1,8 +1,8 @@
 """Build ``libfloodgb.so`` (the CUDA kernels + C ABI) in-tree with nvcc.
 
-Kernels are compiled for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``)
-with ``-fmad=false`` (see ``csrc/fl_device.cuh``); host sources are compiled by
-g++.  Objects go to ``gpu-urban-flood-cupy-jax_gb300/_build`` and the library to
+Kernels are compiled for sm_103a only (``-gencode arch=compute_103a,code=sm_103a``);
+the drainage translation unit with ``-fmad=false`` (see ``csrc/fl_device.cuh``);
+host sources are compiled by g++.  Objects go to ``gpu-urban-flood-cupy-jax_gb300/_build`` and the library to
 ``floodgb/_lib``.  Translation units compile in parallel; an up-to-date
 library is not rebuilt.
 """
@@ -61,7 +61,10 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     jobs = []
     for src in cu:
         obj = BUILD / (src.stem + ".o")
-        cmd = [nvcc, "-c", str(src), "-o", str(obj), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
+        # the drainage kernels evaluate the same request/transfer at several call
+        # sites and rely on uncontracted arithmetic for bit-identical results
+        fmad = "-fmad=false" if src.stem == "fl_drainage" else "-fmad=true"
+        cmd = [nvcc, "-c", str(src), "-o", str(obj), *ARCH, "-O3", "-lineinfo", "-std=c++17", fmad,
                "-Xcompiler", "-fPIC,-fvisibility=hidden", "-Xptxas", "-v" if verbose else "-O3", *inc]
         jobs.append((obj, cmd))
     for src in cpp:
