@@ -116,6 +116,40 @@ __device__ __forceinline__ float2 ff_clamp0(float2 a) {
     return (a.x + a.y < 0.0f) ? make_float2(0.0f, 0.0f) : a;
 }
 
+// --------------------------------------------------------------- inlets
+// Requested capture and surcharge volume of inlet i for one step (reference
+// inlet_exchange_request_kernel, triangular_inlet_exchange_cuda_kernels.py:52-131).
+// The head difference is (bed - invert) + h - V/A: a static datum offset plus
+// two small depths, exact in float32 at any elevation.
+__device__ __forceinline__ float2 inlet_request(const InletReqView &v, int i, float h_cell, float2 Vn, float An,
+                                                float dt) {
+    const float4 p = v.in_par[i];
+    const float dn = fmax32(ff_val(Vn), 0.0f) / fmax32(An, 1.0e-12f);
+    const float dh = p.x + h_cell - dn;
+    const float capc = p.y * dt;
+    const float surc = p.z * dt;
+    float cap, sur;
+    if (v.rule == FL_CAPTURE_CAPACITY) {
+        cap = capc;
+        sur = 0.0f;
+    } else if (v.rule == FL_CAPTURE_HEAD_LIMITED) {
+        cap = dh > 0.0f ? capc : 0.0f;
+        sur = dh < 0.0f ? surc : 0.0f;
+    } else {
+        const float sgn = (float)((dh > 0.0f) - (dh < 0.0f));
+        const float q = v.coef_area * sqrtf(v.g2 * fabsf(dh)) * sgn;
+        float qc = fmax32(q, 0.0f);
+        if (v.rule == FL_CAPTURE_WEIR_ORIFICE) {
+            const float dep = fmax32(h_cell, 0.0f);
+            const float wq = v.weir_coef_perim * dep * sqrtf(v.g2 * dep);
+            qc = fmin32(qc, wq);
+        }
+        cap = fmin32(qc * dt, capc);
+        sur = fmin32(fmax32(-q, 0.0f) * dt, surc);
+    }
+    return make_float2(fmax32(cap, 0.0f), fmax32(sur, 0.0f));
+}
+
 // --------------------------------------------------------------- planning
 __device__ __forceinline__ double hyeto_rate(const HyetoView &hy, double t) {
     int lo = 0, hi = hy.n;

@@ -11,12 +11,12 @@
 // code, so both sides of every exchange see bit-identical values: volume is
 // conserved exactly as in the reference and runs are reproducible.
 //
-// Two launches per step:
-//   k_inlets  one thread per inlet cell (depth after the exchange), one per
-//             node (volume after the exchange)               [reference :52-177]
-//             and one per link: the semi-implicit link update from the two
-//             end volumes after the exchange (recomputed with the node
-//             threads' own code, so bit-identical)         [pipe network :39-139]
+// The inlet requests (reference :52-131) are evaluated by k_surface, which
+// holds each inlet cell's post-surface depth; then three launches per step:
+//   k_inlets  one thread per inlet cell (depth after the exchange) and one per
+//             node (volume after the exchange)              [reference :133-177]
+//   k_links   one thread per link: the semi-implicit link update from the two
+//             end volumes after the exchange              [pipe network :39-139]
 //   k_network one thread per drainage group = a surface cell together with
 //             the nodes that overflow into it (or an orphan node): donor
 //             limiting of the link transfers, node continuity, outfall,
@@ -32,83 +32,20 @@
 
 namespace fl {
 
-struct Req {
-    float cap, sur;
-};
-
-// Requested capture / surcharge of one inlet (reference request kernel :52-131).
-__device__ __forceinline__ Req inlet_request(const D1Args &a, int i, float h_cell, float2 Vn, float An, float dt) {
-    const float4 p = a.in_par[i];
-    const float dn = fmax32(ff_val(Vn), 0.0f) / fmax32(An, 1.0e-12f);
-    const float dh = p.x + h_cell - dn;
-    const float capc = p.y * dt;
-    const float surc = p.z * dt;
-    float cap, sur;
-    if (a.rule == FL_CAPTURE_CAPACITY) {
-        cap = capc;
-        sur = 0.0f;
-    } else if (a.rule == FL_CAPTURE_HEAD_LIMITED) {
-        cap = dh > 0.0f ? capc : 0.0f;
-        sur = dh < 0.0f ? surc : 0.0f;
-    } else {
-        const float sgn = (float)((dh > 0.0f) - (dh < 0.0f));
-        const float q = a.coef_area * sqrtf(a.g2 * fabsf(dh)) * sgn;
-        float qc = fmax32(q, 0.0f);
-        if (a.rule == FL_CAPTURE_WEIR_ORIFICE) {
-            const float dep = fmax32(h_cell, 0.0f);
-            const float wq = a.weir_coef_perim * dep * sqrtf(a.g2 * dep);
-            qc = fmin32(qc, wq);
-        }
-        cap = fmin32(qc * dt, capc);
-        sur = fmin32(fmax32(-q, 0.0f) * dt, surc);
-    }
-    Req r;
-    r.cap = fmax32(cap, 0.0f);
-    r.sur = fmax32(sur, 0.0f);
-    return r;
-}
-
-// Capture limit factor of inlet cell k (surface volume over summed requests).
-__device__ __forceinline__ float cell_capture_factor(const D1Args &a, const float4 *hs, int k, float dt) {
+// Capture limit factor of inlet cell k: surface volume over the summed
+// requests of its inlets (reference inlet_exchange_apply_kernel :133-177).
+__device__ __forceinline__ float cell_capture_factor(const D1Args &a, const float4 *hs, int k) {
     const int c = a.kcell_cell[k];
-    const float h = hs[c].x;
     float sum = 0.0f;
-    for (int i = a.kcell_start[k]; i < a.kcell_start[k + 1]; ++i) {
-        const int n = a.in_node[i];
-        sum += inlet_request(a, i, h, ff_clamp0(a.Va[n]), a.node_area[n], dt).cap;
-    }
-    return fmin32(1.0f, (fmax32(h, 0.0f) * a.g1[c].w) / fmax32(sum, 1.0e-12f));
+    for (int i = a.kcell_start[k]; i < a.kcell_start[k + 1]; ++i) sum += a.req[i].x;
+    return fmin32(1.0f, (fmax32(hs[c].x, 0.0f) * a.g1[c].w) / fmax32(sum, 1.0e-12f));
 }
 
-// Surcharge limit factor of node n (stored volume over summed requests).
-__device__ __forceinline__ float node_surcharge_factor(const D1Args &a, const float4 *hs, int n, float dt) {
-    const float2 V = ff_clamp0(a.Va[n]);
-    const float An = a.node_area[n];
+// Surcharge limit factor of node n: stored volume over the summed requests.
+__device__ __forceinline__ float node_surcharge_factor(const D1Args &a, int n) {
     float sum = 0.0f;
-    for (int j = a.node_in_start[n]; j < a.node_in_start[n + 1]; ++j) {
-        const int i = a.node_in_list[j];
-        sum += inlet_request(a, i, hs[a.in_cell[i]].x, V, An, dt).sur;
-    }
-    return fmin32(1.0f, fmax32(ff_val(V), 0.0f) / fmax32(sum, 1.0e-12f));
-}
-
-// Node volume after the inlet exchange (float-float), reference apply kernel
-// :133-177 plus the node-side sum.
-__device__ __forceinline__ float2 node_after_inlets(const D1Args &a, const float4 *hs, int n, float dt) {
-    const float2 V = ff_clamp0(a.Va[n]);
-    const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
-    if (j0 == j1) return V;
-    const float An = a.node_area[n];
-    const float surf = node_surcharge_factor(a, hs, n, dt);
-    float dv = 0.0f;
-    for (int j = j0; j < j1; ++j) {
-        const int i = a.node_in_list[j];
-        const Req r = inlet_request(a, i, hs[a.in_cell[i]].x, V, An, dt);
-        const float cap = r.cap * cell_capture_factor(a, hs, a.in_kcell[i], dt);
-        const float sur = r.sur * surf;
-        dv += cap - sur;
-    }
-    return ff_add(V, dv);
+    for (int j = a.node_in_start[n]; j < a.node_in_start[n + 1]; ++j) sum += a.req[a.node_in_list[j]].y;
+    return fmin32(1.0f, fmax32(ff_val(ff_clamp0(a.Va[n])), 0.0f) / fmax32(sum, 1.0e-12f));
 }
 
 // Semi-implicit Saint-Venant link update with circular/Preissmann or
@@ -162,13 +99,16 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
     return fmax32(ff_val(ff_clamp0(V)), 0.0f) / fmax32(A, 1.0e-12f);
 }
 
+// One thread per inlet cell (its depth after the exchange) and one per node
+// (its volume after the exchange).  The requests were written by k_surface;
+// each limit factor is a fixed-order sum over the same values in both the
+// cell's and the node's thread, so capture and surcharge balance exactly.
 __global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a, int slot) {
     wait_for_previous_grid();
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
     allow_next_grid();
     const float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
-    const float dt = s.dt_f;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     float led[D1_TERMS] = {0.0f, 0.0f};
     if (t < a.K) {
@@ -176,13 +116,12 @@ __global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a
         const int c = a.kcell_cell[k];
         const float h = hs[c].x;
         const float area = a.g1[c].w;
-        const float capf = cell_capture_factor(a, hs, k, dt);
+        const float capf = cell_capture_factor(a, hs, k);
         float dh = 0.0f;
         for (int i = a.kcell_start[k]; i < a.kcell_start[k + 1]; ++i) {
-            const int n = a.in_node[i];
-            const Req r = inlet_request(a, i, h, ff_clamp0(a.Va[n]), a.node_area[n], dt);
-            const float cap = r.cap * capf;
-            const float sur = r.sur * node_surcharge_factor(a, hs, n, dt);
+            const float2 r = a.req[i];
+            const float cap = r.x * capf;
+            const float sur = r.y * node_surcharge_factor(a, a.in_node[i]);
             dh += (sur - cap) / area;
             led[0] += cap;
             led[1] += sur;
@@ -190,16 +129,38 @@ __global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a
         a.hc_out[k] = h + dh;
     } else if (t < a.K + a.N) {
         const int n = t - a.K;
-        a.Vb[n] = node_after_inlets(a, hs, n, dt);
-    } else if (t < a.K + a.N + a.L) {
-        const int l = t - a.K - a.N;
-        const int f = a.link_from[l], to = a.link_to[l];
-        const float df = node_depth(node_after_inlets(a, hs, f, dt), a.node_area[f]);
-        const float dtn = node_depth(node_after_inlets(a, hs, to, dt), a.node_area[to]);
-        const float *Qin = s.parity ? a.Q1 : a.Q0;
-        a.T[l] = link_transfer(a.lk0[l], a.lk1[l], a.lk2[l], df, dtn, Qin[l], a.g, a.wave_speed, dt);
+        const float2 V = ff_clamp0(a.Va[n]);
+        const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
+        if (j0 == j1) {
+            a.Vb[n] = V;
+        } else {
+            const float surf = node_surcharge_factor(a, n);
+            float dv = 0.0f;
+            for (int j = j0; j < j1; ++j) {
+                const int i = a.node_in_list[j];
+                const float2 r = a.req[i];
+                dv += r.x * cell_capture_factor(a, hs, a.in_kcell[i]) - r.y * surf;
+            }
+            a.Vb[n] = ff_add(V, dv);
+        }
     }
     warp_add_ledger<D1_TERMS>(led, a.ledger);
+}
+
+// One thread per link: the transfer volume from the end volumes after the
+// inlet exchange.
+__global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a, int slot) {
+    wait_for_previous_grid();
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
+    allow_next_grid();
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= a.L) return;
+    const int f = a.link_from[l], to = a.link_to[l];
+    const float df = node_depth(a.Vb[f], a.node_area[f]);
+    const float dtn = node_depth(a.Vb[to], a.node_area[to]);
+    const float *Qin = s.parity ? a.Q1 : a.Q0;
+    a.T[l] = link_transfer(a.lk0[l], a.lk1[l], a.lk2[l], df, dtn, Qin[l], a.g, a.wave_speed, s.dt_f);
 }
 
 // Sum of |transfer| over the links whose donor is node d.
@@ -308,12 +269,18 @@ static cudaError_t launch_pdl2(const void *func, dim3 grid, dim3 block, void **a
     return cudaLaunchKernelExC(&cfg, func, args);
 }
 
-int inlet_blocks(int32_t K, int32_t N, int32_t L) { return (K + N + L + 127) / 128 > 0 ? (K + N + L + 127) / 128 : 1; }
+int inlet_blocks(int32_t K, int32_t N) { return (K + N + 127) / 128 > 0 ? (K + N + 127) / 128 : 1; }
+int link_blocks(int32_t L) { return (L + 127) / 128 > 0 ? (L + 127) / 128 : 1; }
 int network_blocks(int32_t G) { return (G + 127) / 128 > 0 ? (G + 127) / 128 : 1; }
 
 cudaError_t launch_inlets(const D1Args &a, int slot, cudaStream_t stream) {
     void *args[] = {(void *)&a, (void *)&slot};
-    return launch_pdl2((const void *)k_inlets, dim3(inlet_blocks(a.K, a.N, a.L)), dim3(128), args, stream);
+    return launch_pdl2((const void *)k_inlets, dim3(inlet_blocks(a.K, a.N)), dim3(128), args, stream);
+}
+
+cudaError_t launch_links(const LinkArgs &a, int slot, cudaStream_t stream) {
+    void *args[] = {(void *)&a, (void *)&slot};
+    return launch_pdl2((const void *)k_links, dim3(link_blocks(a.L)), dim3(128), args, stream);
 }
 
 cudaError_t launch_network(const D2Args &a, int slot, cudaStream_t stream) {

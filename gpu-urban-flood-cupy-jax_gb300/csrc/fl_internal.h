@@ -27,10 +27,11 @@ constexpr int CODE_SHIFT = 28;
 constexpr uint32_t RIGHT_BIT = 1u << 31;
 constexpr int64_t MAX_CELLS = 0x07FFFFFE;
 
-// topo[c].w bits
+// topo[c].w bits; bits 3..31 hold (inlet-cell index + 1), 0 for a cell without inlets
 constexpr uint32_t CELL_ACTIVE = 1u;
 constexpr uint32_t CELL_COUPLED = 2u;       // drainage writes this cell's final depth
 constexpr uint32_t CELL_STAGE_LEDGER = 4u;  // inactive cell left of an exterior stage edge
+constexpr int CELL_KCELL_SHIFT = 3;
 
 // Per-step control, double-buffered by launch slot.  Written by the planner
 // (one thread) of the previous launch, read by every kernel of the step.
@@ -81,6 +82,20 @@ constexpr int SURF_TERMS = 4;   // rain, infil, boundary in, boundary out
 constexpr int D1_TERMS = 2;     // capture, surcharge
 constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer|
 
+// What k_surface needs to evaluate the inlet requests of its cell.
+struct InletReqView {
+    const int32_t *kcell_start;   // [K + 1] inlet range of each inlet cell
+    const int32_t *in_node;       // [I]
+    const float4 *in_par;         // [I] {bed - invert, capture capacity, surcharge capacity, 0}
+    const float2 *Va;             // node volume (float-float) at the start of the drainage step
+    const float *node_area;       // [N]
+    float2 *req;                  // [I] requested capture / surcharge volume this step
+    int32_t rule;
+    float coef_area;              // float32(Cd * A_orifice)
+    float weir_coef_perim;        // float32(Cw * perimeter) for weir_orifice
+    float g2;                     // 2 g (float32)
+};
+
 struct SurfArgs {
     const uint4 *topo;
     const float4 *g0, *g1, *g2;   // {nx, ny, len, manning}, {.., area}, {.., 0}
@@ -98,6 +113,8 @@ struct SurfArgs {
     float infil_scalar;
     float g, half_g, md, vmax, stage;
     int32_t has_stage;
+    int32_t has_inlets;
+    InletReqView inl;
 };
 
 struct DtArgs {
@@ -116,29 +133,30 @@ struct DtArgs {
 
 struct D1Args {
     // inlets sorted by (renumbered) cell
-    const int32_t *in_cell, *in_node, *in_kcell;
-    const float4 *in_par;         // {bed - invert offset, capture cap * 1, surcharge cap, unused}
+    const int32_t *in_node, *in_kcell;
     const int32_t *kcell_cell, *kcell_start;   // inlet cells and their inlet ranges
     const int32_t *node_in_start, *node_in_list;
-    const float *node_area;
+    const float2 *req;            // requested capture / surcharge (k_surface)
     const float4 *g1;             // cell area in .w
     const float4 *state0, *state1;
     float *hc_out;                // depth of each inlet cell after the exchange
     const float2 *Va;             // node volume (float-float) before
     float2 *Vb;                   // after the exchange
-    // links: the transfer volume of each link this step
-    const int32_t *link_from, *link_to;
-    const float4 *lk0, *lk1, *lk2;
-    const float *Q0, *Q1;         // link flow, ping-pong with the state parity
-    float *T;
     StepCtrl *ctrl;
     double *ledger;               // [warps * D1_TERMS]
-    int32_t K, N, L;
-    int32_t rule;
+    int32_t K, N;
+};
+
+struct LinkArgs {
+    const int32_t *link_from, *link_to;
+    const float4 *lk0, *lk1, *lk2;
+    const float *node_area;
+    const float2 *Vb;             // node volume after the inlet exchange
+    const float *Q0, *Q1;         // link flow, ping-pong with the state parity
+    float *T;                     // transfer volume of each link this step
+    StepCtrl *ctrl;
+    int32_t L;
     float g, wave_speed;
-    float coef_area;              // float32(Cd * A_orifice)
-    float weir_coef_perim;        // float32(Cw * perimeter) for weir_orifice
-    float g2;                     // 2 g (float32)
 };
 
 struct D2Args {

@@ -234,6 +234,9 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     }
     L.kcell_start.push_back(I);
     L.K = (int32_t)L.kcell_cell.size();
+    if ((int64_t)L.K >= (int64_t(1) << (32 - CELL_KCELL_SHIFT)) - 1)
+        return set_error(FL_E_INVALID, "too many inlet cells (%d)", L.K);
+    for (int32_t k = 0; k < L.K; ++k) L.topo[L.kcell_cell[k]].w |= (uint32_t)(k + 1) << CELL_KCELL_SHIFT;
     for (int32_t k = 0; k < L.K; ++k)
         L.max_inlets_per_cell = std::max(L.max_inlets_per_cell, L.kcell_start[k + 1] - L.kcell_start[k]);
 

@@ -55,7 +55,8 @@ cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *g1,
                            int32_t C, int32_t N, double *out2, cudaStream_t stream);
 cudaError_t launch_inlets(const D1Args &a, int slot, cudaStream_t stream);
 cudaError_t launch_network(const D2Args &a, int slot, cudaStream_t stream);
-int inlet_blocks(int32_t K, int32_t N, int32_t L);
+int inlet_blocks(int32_t K, int32_t N);
+cudaError_t launch_links(const LinkArgs &a, int slot, cudaStream_t stream);
 int network_blocks(int32_t G);
 
 }  // namespace fl
@@ -95,6 +96,7 @@ struct FlSolver {
     SurfArgs sa{};
     DtArgs da{};
     D1Args d1{};
+    LinkArgs la{};
     D2Args d2{};
     HyetoView hy{};
     // host
@@ -105,7 +107,7 @@ struct FlSolver {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     bool has_drain() const { return N > 0; }
-    int launches_per_step() const { return 1 + (has_drain() ? 2 : 0); }
+    int launches_per_step() const { return 1 + (has_drain() ? 3 : 0); }
 
     template <class T>
     int alloc(T **p, size_t count) {
@@ -148,8 +150,9 @@ static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStr
     g_launches++;
     if (s->has_drain()) {
         FL_CUDA(launch_inlets(s->d1, slot, st));
+        FL_CUDA(launch_links(s->la, slot, st));
         FL_CUDA(launch_network(s->d2, slot, st));
-        g_launches += 2;
+        g_launches += 3;
     }
     return FL_OK;
 }
@@ -378,24 +381,40 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         FL_CUDA(cudaMemset(s->Vb, 0, sizeof(float2) * s->N));
         FL_CUDA(cudaMemset(s->Q[0], 0, sizeof(float) * std::max(s->NL, 1)));
         FL_CUDA(cudaMemset(s->Q[1], 0, sizeof(float) * std::max(s->NL, 1)));
-        s->d1_blocks = inlet_blocks(s->K, s->N, s->NL);
+        s->d1_blocks = inlet_blocks(s->K, s->N);
         s->d2_blocks = network_blocks(s->G);
         float *T;
         if ((rc = s->alloc(&s->led_1, (size_t)s->d1_blocks * 4 * D1_TERMS)) ||
             (rc = s->alloc(&s->led_2, (size_t)s->d2_blocks * 4 * D2_TERMS)) || (rc = s->alloc(&T, s->NL)))
             return rc;
-        s->d1.T = T;
+        s->la.T = T;
         s->d2.T = T;
+        float2 *req;
+        if ((rc = s->alloc(&req, s->I))) return rc;
+        FL_CUDA(cudaMemset(req, 0, sizeof(float2) * std::max(s->I, 1)));
+        InletReqView &v = s->sa.inl;
+        v.kcell_start = kcell_start;
+        v.in_node = in_node;
+        v.in_par = in_par;
+        v.Va = s->Va;
+        v.node_area = node_area;
+        v.req = req;
+        v.rule = drain->inlet_capture_rule;
+        v.coef_area = drain->inlet_orifice_coefficient * drain->inlet_orifice_area_m2;
+        const float eq = sqrtf(4.0f * 3.14159265358979323846f * std::max(drain->inlet_orifice_area_m2, 0.0f));
+        const float perim = drain->inlet_weir_perimeter_m > 0.0f ? drain->inlet_weir_perimeter_m : eq;
+        v.weir_coef_perim = drain->inlet_weir_coefficient * std::max(perim, 0.0f);
+        v.g2 = (float)(2.0 * (double)(float)p.gravity_mps2);
+        s->sa.has_inlets = s->I > 0;
+        (void)in_cell;
         D1Args &a = s->d1;
-        a.in_cell = in_cell;
         a.in_node = in_node;
         a.in_kcell = in_kcell;
-        a.in_par = in_par;
+        a.req = req;
         a.kcell_cell = kcell_cell;
         a.kcell_start = kcell_start;
         a.node_in_start = node_in_start;
         a.node_in_list = node_in_list;
-        a.node_area = node_area;
         a.g1 = g1;
         a.state0 = s->state[0];
         a.state1 = s->state[1];
@@ -406,22 +425,20 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         a.ledger = s->led_1;
         a.K = s->K;
         a.N = s->N;
-        a.link_from = lf;
-        a.link_to = lt;
-        a.lk0 = lk0;
-        a.lk1 = lk1;
-        a.lk2 = lk2;
-        a.Q0 = s->Q[0];
-        a.Q1 = s->Q[1];
-        a.L = s->NL;
-        a.g = (float)p.gravity_mps2;
-        a.wave_speed = drain->pressurized_wave_speed_mps;
-        a.rule = drain->inlet_capture_rule;
-        a.coef_area = drain->inlet_orifice_coefficient * drain->inlet_orifice_area_m2;
-        const float eq = sqrtf(4.0f * 3.14159265358979323846f * std::max(drain->inlet_orifice_area_m2, 0.0f));
-        const float perim = drain->inlet_weir_perimeter_m > 0.0f ? drain->inlet_weir_perimeter_m : eq;
-        a.weir_coef_perim = drain->inlet_weir_coefficient * std::max(perim, 0.0f);
-        a.g2 = (float)(2.0 * (double)(float)p.gravity_mps2);
+        LinkArgs &la = s->la;
+        la.link_from = lf;
+        la.link_to = lt;
+        la.lk0 = lk0;
+        la.lk1 = lk1;
+        la.lk2 = lk2;
+        la.node_area = node_area;
+        la.Vb = s->Vb;
+        la.Q0 = s->Q[0];
+        la.Q1 = s->Q[1];
+        la.ctrl = s->ctrl;
+        la.L = s->NL;
+        la.g = (float)p.gravity_mps2;
+        la.wave_speed = drain->pressurized_wave_speed_mps;
         D2Args &b = s->d2;
         b.grp_cell = grp_cell;
         b.grp_kcell = grp_kcell;
@@ -741,8 +758,9 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
     g_launches++;
     if (s->has_drain() && (phases & FL_PHASE_DRAINAGE)) {
         FL_CUDA(launch_inlets(s->d1, s->slot, st));
+        FL_CUDA(launch_links(s->la, s->slot, st));
         FL_CUDA(launch_network(s->d2, s->slot, st));
-        g_launches += 2;
+        g_launches += 3;
     } else if (s->has_drain()) {
         // no drainage this step: carry link flow to the other parity buffer
         FL_CUDA(cudaMemcpyAsync(s->Q[r.parity], s->Q[c.parity], sizeof(float) * std::max(s->NL, 1),
@@ -756,8 +774,9 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
 
 FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *stream, double *ms_per_launch) {
     if (!s || !ms_per_launch || reps < 1) return set_error(FL_E_INVALID, "bad fl_time_kernel arguments");
-    if ((kernel == 1 || kernel == 2) && !s->has_drain()) return set_error(FL_E_INVALID, "solver has no drainage");
-    if (kernel < 0 || kernel > 3) return set_error(FL_E_INVALID, "kernel must be 0..3");
+    if ((kernel == 1 || kernel == 2 || kernel == 4) && !s->has_drain())
+        return set_error(FL_E_INVALID, "solver has no drainage");
+    if (kernel < 0 || kernel > 4) return set_error(FL_E_INVALID, "kernel must be 0..4");
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
     int rc = sync_run(s, st);
@@ -781,6 +800,7 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
             case 0: FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, st)); break;
             case 1: FL_CUDA(launch_inlets(s->d1, 0, st)); break;
             case 2: FL_CUDA(launch_network(s->d2, 0, st)); break;
+            case 4: FL_CUDA(launch_links(s->la, 0, st)); break;
             default: {
                 DtArgs a = s->da;
                 a.dt_out = s->dt_out;

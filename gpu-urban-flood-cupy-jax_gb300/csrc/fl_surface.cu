@@ -25,7 +25,7 @@
 namespace fl {
 
 template <int KIND>
-__global__ void __launch_bounds__(256) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
+__global__ void __launch_bounds__(256, 4) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
     wait_for_previous_grid();
     const StepCtrl s = a.ctrl[slot];
     if (plan_next && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -59,12 +59,19 @@ __global__ void __launch_bounds__(256) k_surface(const __grid_constant__ SurfArg
             float L0 = 0.0f, L1 = 0.0f, L2 = 0.0f, R0 = 0.0f, R1 = 0.0f, R2 = 0.0f;
             float bin = 0.0f, bout = 0.0f;
             const float4 g0 = a.g0[c], g1 = a.g1[c], g2 = a.g2[c];
+            // the three neighbour states, gathered together up front
+            const auto nb = [&](uint32_t w) {
+                const uint32_t o = w & IDX_MASK;
+                return (w != SLOT_NONE && o != NO_CELL && (w & OTHER_ACTIVE_BIT)) ? in[o] : own;
+            };
+            const float4 n0 = nb(tp.x), n1 = nb(tp.y), n2 = nb(tp.z);
             // one flux code path for all three edges (not unrolled): both cells
             // of an edge run the identical instruction sequence
 #pragma unroll 1
             for (int k = 0; k < 3; ++k) {
                 const uint32_t w = k == 0 ? tp.x : (k == 1 ? tp.y : tp.z);
                 const float4 gk = k == 0 ? g0 : (k == 1 ? g1 : g2);
+                const float4 nbk = k == 0 ? n0 : (k == 1 ? n1 : n2);
                 if (w == SLOT_NONE) continue;
                 const uint32_t other = w & IDX_MASK;
                 const bool interior = other != NO_CELL;
@@ -77,7 +84,7 @@ __global__ void __launch_bounds__(256) k_surface(const __grid_constant__ SurfArg
                 const int code = (interior && !oact) ? 0 : raw;
                 const float nx = gk.x, ny = gk.y, len = gk.z;
                 // the edge's left and right states in the reference's orientation
-                const float4 o = ai ? in[other] : ghost_state(own.x, own.y, own.z, own.w, nx, ny, code, a.stage);
+                const float4 o = ai ? nbk : ghost_state(own.x, own.y, own.z, own.w, nx, ny, code, a.stage);
                 const float4 L = is_right ? o : own;
                 const float4 R = is_right ? own : o;
                 EdgeFlux f = hr_flux(L.x, L.y, L.z, L.w, R.x, R.y, R.z, R.w, nx, ny, a.g, a.half_g, md);
@@ -151,6 +158,16 @@ __global__ void __launch_bounds__(256) k_surface(const __grid_constant__ SurfArg
             hvn = xmul(hvn, scale);
         }
         out[c] = make_float4(hn, hun, hvn, st.w);
+        // requested inlet capture / surcharge of this cell's inlets, from the
+        // depth the drainage step starts with
+        const uint32_t kc = tp.w >> CELL_KCELL_SHIFT;
+        if (kc && drain_finishes && a.has_inlets) {
+            const InletReqView &v = a.inl;
+            for (int i = v.kcell_start[kc - 1]; i < v.kcell_start[kc]; ++i) {
+                const int n = v.in_node[i];
+                v.req[i] = inlet_request(v, i, hn, ff_clamp0(v.Va[n]), v.node_area[n], dt);
+            }
+        }
         const bool final_here = !(drain_finishes && (tp.w & CELL_COUPLED));
         if (KIND == 1 && do_surface && final_here) a.wet[c] = a.wet[c] + dt * (float)(hn > md);
         if (s.snap_slot >= 0) {

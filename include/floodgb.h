@@ -210,7 +210,7 @@ FL_API int fl_get_snapshots(FlSolver *solver, int32_t first, int32_t count, doub
 FL_API int fl_plan_check(const FlMeshDesc *mesh, const FlDrainDesc *drain, int64_t *stats, int32_t *perm_out);
 
 /* Time `reps` back-to-back launches of one kernel of a step (0 surface,
- * 1 inlet exchange, 2 pipe network, 3 CFL reduction) between CUDA events on
+ * 1 inlet exchange, 2 pipe network, 3 CFL reduction, 4 link update) between CUDA events on
  * `stream`, at the solver's current state and last dt; the clock is not
  * advanced but the state buffers are overwritten (reset before the next run).
  * No reference counterpart: it is the measurement hook for the roofline. */
