@@ -133,6 +133,8 @@ _SIGNATURES = {
     "fl_plan_check": (C.c_int, [C.POINTER(FlMeshDesc), C.POINTER(FlDrainDesc), C.POINTER(C.c_int64), i32p]),
     "fl_time_kernel": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, f64p]),
     "fl_launch_count": (C.c_int64, []),
+    "fl_stable_timestep_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
+                                             C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
 }
 
 
