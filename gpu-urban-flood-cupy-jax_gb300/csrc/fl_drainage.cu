@@ -38,7 +38,7 @@ __device__ __forceinline__ float cell_capture_factor(const D1Args &a, const floa
     const int c = a.kcell_cell[k];
     float sum = 0.0f;
     for (int i = a.kcell_start[k]; i < a.kcell_start[k + 1]; ++i) sum += a.req[i].x;
-    return fmin32(1.0f, (fmax32(hs[c].x, 0.0f) * a.g1[c].w) / fmax32(sum, 1.0e-12f));
+    return fmin32(1.0f, (fmax32(hs[c].x, 0.0f) * a.cinfo[c].x) / fmax32(sum, 1.0e-12f));
 }
 
 // Surcharge limit factor of node n: stored volume over the summed requests.
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a
         const int k = t;
         const int c = a.kcell_cell[k];
         const float h = hs[c].x;
-        const float area = a.g1[c].w;
+        const float area = a.cinfo[c].x;
         const float capf = cell_capture_factor(a, hs, k);
         float dh = 0.0f;
         for (int i = a.kcell_start[k]; i < a.kcell_start[k + 1]; ++i) {
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args 
         float h = 0.0f, area = 1.0f;
         if (c >= 0) {
             h = (k >= 0) ? a.hc_out[k] : hs[c].x;
-            area = a.g1[c].w;
+            area = a.cinfo[c].x;
         }
         float hd = 0.0f;
         for (int gi = a.grp_start[g]; gi < a.grp_start[g + 1]; ++gi) {

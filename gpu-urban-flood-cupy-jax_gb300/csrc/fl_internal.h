@@ -10,28 +10,31 @@
 namespace fl {
 
 // ---------------------------------------------------------------------------
-// Per-cell "slot" words.  A triangle has up to three edges; slot k of cell c
-// describes the k-th edge in the reference's cell_edge_indices order (edges
-// the cell is left of, ascending, then edges it is right of, ascending).
-//   bits  0..26  other cell (renumbered index), NO_CELL for an exterior edge
-//   bit   27     other cell is active
-//   bits 28..30  the edge's boundary_code + 1 (0 = interior code -1)
-//   bit   31     this cell is the edge's right cell
-// SLOT_NONE marks an unused slot.
+// Surface layout.  Cells are renumbered along a Hilbert curve and processed
+// in tiles of TILE consecutive cells, one CTA per tile.  A cell's (up to
+// three) edges are its "slots", in the reference's cell_edge_indices order:
+// edges it is the left cell of (ascending), then edges it is the right cell of
+// (ascending).  Each tile has a list of edge entries: every edge with an
+// endpoint in the tile that contributes to it, once per tile (an edge inside
+// the tile is one entry serving both cells; an edge crossing two tiles has an
+// entry in each).  An entry is {left, right} (int2, right = -1 if exterior)
+// plus {nx, ny, len, flags} (float4, flags as bits):
 // ---------------------------------------------------------------------------
-constexpr uint32_t SLOT_NONE = 0xFFFFFFFFu;
-constexpr uint32_t IDX_MASK = 0x07FFFFFFu;
-constexpr uint32_t NO_CELL = 0x07FFFFFFu;
-constexpr uint32_t OTHER_ACTIVE_BIT = 1u << 27;
-constexpr int CODE_SHIFT = 28;
-constexpr uint32_t RIGHT_BIT = 1u << 31;
-constexpr int64_t MAX_CELLS = 0x07FFFFFE;
+constexpr int TILE = 256;
+constexpr uint32_t EF_LPRESENT = 1u;     // left cell is in this tile and takes -F_L
+constexpr int EF_LSLOT_SHIFT = 1;        // bits 1-2: the edge's slot in the left cell
+constexpr uint32_t EF_RPRESENT = 8u;     // right cell is in this tile and takes +F_R
+constexpr int EF_RSLOT_SHIFT = 4;        // bits 4-5: the edge's slot in the right cell
+constexpr uint32_t EF_LACTIVE = 64u;     // left cell active
+constexpr uint32_t EF_AI = 128u;         // active interior edge
+constexpr uint32_t EF_INTERIOR = 256u;   // the edge has a right cell
+constexpr int EF_CODE_SHIFT = 9;         // bits 9-11: effective boundary code + 1
+constexpr int64_t MAX_CELLS = 0x7FFFFFFE;
 
-// topo[c].w bits; bits 3..31 hold (inlet-cell index + 1), 0 for a cell without inlets
+// cinfo[c] = {area, manning, flags (bits), inlet-cell index + 1 (bits, 0 = none)}
 constexpr uint32_t CELL_ACTIVE = 1u;
 constexpr uint32_t CELL_COUPLED = 2u;       // drainage writes this cell's final depth
-constexpr uint32_t CELL_STAGE_LEDGER = 4u;  // inactive cell left of an exterior stage edge
-constexpr int CELL_KCELL_SHIFT = 3;
+constexpr int CELL_RIGHT_SHIFT = 3;         // bits 3-5: slot k is a right-side slot
 
 // Per-step control, double-buffered by launch slot.  Written by the planner
 // (one thread) of the previous launch, read by every kernel of the step.
@@ -97,8 +100,10 @@ struct InletReqView {
 };
 
 struct SurfArgs {
-    const uint4 *topo;
-    const float4 *g0, *g1, *g2;   // {nx, ny, len, manning}, {.., area}, {.., 0}
+    const float4 *cinfo;          // {area, manning, flags, inlet cell + 1}
+    const int32_t *tile_start;    // [tiles + 1] entry range of each tile
+    const int2 *ent_lr;           // entry {left, right}
+    const float4 *ent_g;          // entry {nx, ny, len, flags}
     const float4 *horton;         // {f0, fc, k, rain multiplier} (kind 1)
     float *wet;                   // wet time (kind 1)
     float4 *state0, *state1;      // {h, hu, hv, bed}
@@ -137,7 +142,7 @@ struct D1Args {
     const int32_t *kcell_cell, *kcell_start;   // inlet cells and their inlet ranges
     const int32_t *node_in_start, *node_in_list;
     const float2 *req;            // requested capture / surcharge (k_surface)
-    const float4 *g1;             // cell area in .w
+    const float4 *cinfo;          // cell area in .x
     const float4 *state0, *state1;
     float *hc_out;                // depth of each inlet cell after the exchange
     const float2 *Va;             // node volume (float-float) before
@@ -168,7 +173,7 @@ struct D2Args {
     const float4 *lk2;            // {flow capacity (inf: none), rect width, rect height, geometry code}
     const float4 *nd0;            // {storage area, outfall head offset, Cd*A outfall, outfall capacity}
     const float *nd_capv;         // storage area * max(max depth, 0)
-    const float4 *g1;
+    const float4 *cinfo;
     float4 *state0, *state1;
     const float *hc_out;
     const float2 *Vb;             // after the inlet exchange
@@ -189,8 +194,10 @@ struct HostLayout {
     int32_t C = 0, E = 0, N = 0, L = 0, I = 0, K = 0, G = 0;
     std::vector<int32_t> perm;        // perm[new] = reference cell
     std::vector<int32_t> inv;         // inv[reference] = new
-    std::vector<uint4> topo;
-    std::vector<float4> g0, g1, g2;
+    std::vector<float4> cinfo;
+    std::vector<int32_t> tile_start;
+    std::vector<int2> ent_lr;
+    std::vector<float4> ent_g;
     std::vector<float> char_len;
     std::vector<float> bed;
     int64_t slots_used = 0;

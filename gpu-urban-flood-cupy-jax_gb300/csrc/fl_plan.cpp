@@ -1,12 +1,13 @@
 // Host-side layout builder: validates the reference-layout inputs, renumbers
-// cells along a Hilbert curve of their centroids, packs each cell's three
-// edges into slot words + float4 geometry, and builds the CSR tables the
-// drainage kernels gather over.  Pure C++ (no CUDA calls), so it also runs
+// cells along a Hilbert curve of their centroids, builds each tile's edge
+// entry list and the per-cell info words, and the CSR tables the drainage
+// kernels gather over.  Pure C++ (no CUDA calls), so it also runs
 // through fl_plan_check on machines without a GPU.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 #include <limits>
 #include <numeric>
 #include <string>
@@ -126,51 +127,88 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
         }
     }
 
-    L.topo.resize(C);
-    L.g0.resize(C);
-    L.g1.resize(C);
-    L.g2.resize(C);
+    L.cinfo.resize(C);
     L.char_len.resize(C);
     L.bed.resize(C);
     L.slots_used = 0;
-    for (int64_t i = 0; i < C; ++i) {
-        const int32_t c = L.perm[i];
-        uint32_t w[3] = {SLOT_NONE, SLOT_NONE, SLOT_NONE};
-        float4 g[3] = {f4(0, 0, 0, 0), f4(0, 0, 0, 0), f4(0, 0, 0, 0)};
-        bool stage_ledger = false;
+    // slot of each edge in its left / right cell
+    std::vector<int8_t> lslot(E, -1), rslot(E, -1);
+    for (int64_t c = 0; c < C; ++c) {
         for (int k = 0; k < count[c]; ++k) {
             const int32_t e = inc[c * 3 + k];
-            const bool is_right = inc_right[c * 3 + k] != 0;
-            const int32_t other_ref = is_right ? m.edge_left_cell[e] : m.edge_right_cell[e];
-            uint32_t word = 0;
-            if (other_ref < 0) {
-                word = NO_CELL;
-            } else {
-                word = (uint32_t)L.inv[other_ref];
-                if (active[other_ref]) word |= OTHER_ACTIVE_BIT;
-            }
-            word |= (uint32_t)(m.boundary_code[e] + 1) << CODE_SHIFT;
-            if (is_right) word |= RIGHT_BIT;
-            w[k] = word;
-            g[k] = f4(m.edge_normal_x[e], m.edge_normal_y[e], m.edge_length_m[e], 0.0f);
-            if (!active[c] && !is_right && other_ref < 0 && m.boundary_code[e] == 3 && m.has_stage_boundary)
-                stage_ledger = true;
+            if (inc_right[c * 3 + k]) rslot[e] = (int8_t)k; else lslot[e] = (int8_t)k;
             L.slots_used++;
         }
+    }
+    for (int64_t i = 0; i < C; ++i) {
+        const int32_t c = L.perm[i];
         uint32_t info = 0;
         if (active[c]) info |= CELL_ACTIVE;
         if (coupled[c]) info |= CELL_COUPLED;
-        if (stage_ledger) info |= CELL_STAGE_LEDGER;
-        L.topo[i] = make_uint4(w[0], w[1], w[2], info);
-        g[0].w = m.manning_n[c];
-        g[1].w = m.cell_area_m2[c];
-        g[2].w = 0.0f;
-        L.g0[i] = g[0];
-        L.g1[i] = g[1];
-        L.g2[i] = g[2];
+        for (int k = 0; k < count[c]; ++k)
+            if (inc_right[c * 3 + k]) info |= 1u << (CELL_RIGHT_SHIFT + k);
+        uint32_t none = 0;
+        float fi, fk;
+        memcpy(&fi, &info, 4);
+        memcpy(&fk, &none, 4);
+        L.cinfo[i] = f4(m.cell_area_m2[c], m.manning_n[c], fi, fk);
         L.char_len[i] = m.characteristic_length_m[c];
         L.bed[i] = m.bed_elevation_m[c];
     }
+
+    // tile edge lists
+    const int64_t tiles = (C + TILE - 1) / TILE;
+    L.tile_start.assign(tiles + 1, 0);
+    L.ent_lr.clear();
+    L.ent_g.clear();
+    L.ent_lr.reserve((size_t)(C * 17 / 10));
+    L.ent_g.reserve((size_t)(C * 17 / 10));
+    std::vector<int32_t> entry_of(E, -1);  // entry of edge e in the current tile
+    std::vector<int64_t> entry_tile(E, -1);
+    for (int64_t t = 0; t < tiles; ++t) {
+        L.tile_start[t] = (int32_t)L.ent_lr.size();
+        const int64_t c0 = t * TILE, c1 = std::min<int64_t>(C, c0 + TILE);
+        for (int64_t i = c0; i < c1; ++i) {
+            const int32_t c = L.perm[i];
+            for (int k = 0; k < count[c]; ++k) {
+                const int32_t e = inc[c * 3 + k];
+                const bool is_right = inc_right[c * 3 + k] != 0;
+                const int32_t lref = m.edge_left_cell[e], rref = m.edge_right_cell[e];
+                const bool interior = rref >= 0;
+                const bool la = active[lref] != 0;
+                const bool ra = interior ? active[rref] != 0 : la;
+                const bool ai = interior && la && ra;
+                const int32_t raw = m.boundary_code[e];
+                const int32_t code = (interior && la && !ra) ? 0 : raw;
+                // does this side take a contribution?
+                bool contributes;
+                if (is_right) contributes = ai;
+                else contributes = la || (!interior && code == 3 && m.has_stage_boundary);
+                if (!contributes) continue;
+                int32_t idx = entry_tile[e] == t ? entry_of[e] : -1;
+                if (idx < 0) {
+                    idx = (int32_t)L.ent_lr.size();
+                    entry_of[e] = idx;
+                    entry_tile[e] = t;
+                    uint32_t flags = 0;
+                    if (la) flags |= EF_LACTIVE;
+                    if (ai) flags |= EF_AI;
+                    if (interior) flags |= EF_INTERIOR;
+                    flags |= (uint32_t)(code + 1) << EF_CODE_SHIFT;
+                    float ff;
+                    memcpy(&ff, &flags, 4);
+                    L.ent_lr.push_back(make_int2(L.inv[lref], interior ? L.inv[rref] : -1));
+                    L.ent_g.push_back(f4(m.edge_normal_x[e], m.edge_normal_y[e], m.edge_length_m[e], ff));
+                }
+                uint32_t flags;
+                memcpy(&flags, &L.ent_g[idx].w, 4);
+                if (is_right) flags |= EF_RPRESENT | ((uint32_t)rslot[e] << EF_RSLOT_SHIFT);
+                else flags |= EF_LPRESENT | ((uint32_t)lslot[e] << EF_LSLOT_SHIFT);
+                memcpy(&L.ent_g[idx].w, &flags, 4);
+            }
+        }
+    }
+    L.tile_start[tiles] = (int32_t)L.ent_lr.size();
     return FL_OK;
 }
 
@@ -234,9 +272,10 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     }
     L.kcell_start.push_back(I);
     L.K = (int32_t)L.kcell_cell.size();
-    if ((int64_t)L.K >= (int64_t(1) << (32 - CELL_KCELL_SHIFT)) - 1)
-        return set_error(FL_E_INVALID, "too many inlet cells (%d)", L.K);
-    for (int32_t k = 0; k < L.K; ++k) L.topo[L.kcell_cell[k]].w |= (uint32_t)(k + 1) << CELL_KCELL_SHIFT;
+    for (int32_t k = 0; k < L.K; ++k) {
+        const uint32_t v = (uint32_t)(k + 1);
+        memcpy(&L.cinfo[L.kcell_cell[k]].w, &v, 4);
+    }
     for (int32_t k = 0; k < L.K; ++k)
         L.max_inlets_per_cell = std::max(L.max_inlets_per_cell, L.kcell_start[k + 1] - L.kcell_start[k]);
 

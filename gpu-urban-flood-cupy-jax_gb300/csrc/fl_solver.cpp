@@ -278,7 +278,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     if (rc) return rc;
     const bool with_drain = drain && drain->node_count > 0;
     if (with_drain) {
-        rc = build_drain_layout(*mesh, *drain, L);
+        rc = build_drain_layout(*mesh, *drain, L);  // also sets the inlet-cell words of cinfo
         if (rc) return rc;
     }
     s->C = L.C;
@@ -291,11 +291,13 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     const int32_t C = s->C;
 
     // static surface layout
-    uint4 *topo;
-    float4 *g0, *g1, *g2;
+    float4 *cinfo, *ent_g;
+    int2 *ent_lr;
+    int32_t *tile_start;
     float *char_len;
-    if ((rc = s->upload(&topo, L.topo)) || (rc = s->upload(&g0, L.g0)) || (rc = s->upload(&g1, L.g1)) ||
-        (rc = s->upload(&g2, L.g2)) || (rc = s->upload(&char_len, L.char_len)) || (rc = s->upload(&s->bed, L.bed)) ||
+    if ((rc = s->upload(&cinfo, L.cinfo)) || (rc = s->upload(&tile_start, L.tile_start)) ||
+        (rc = s->upload(&ent_lr, L.ent_lr)) || (rc = s->upload(&ent_g, L.ent_g)) ||
+        (rc = s->upload(&char_len, L.char_len)) || (rc = s->upload(&s->bed, L.bed)) ||
         (rc = s->upload(&s->perm, L.perm)))
         return rc;
     float4 *horton = nullptr;
@@ -415,7 +417,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         a.kcell_start = kcell_start;
         a.node_in_start = node_in_start;
         a.node_in_list = node_in_list;
-        a.g1 = g1;
+        a.cinfo = cinfo;
         a.state0 = s->state[0];
         a.state1 = s->state[1];
         a.hc_out = hc_out;
@@ -453,7 +455,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         b.lk2 = lk2;
         b.nd0 = nd0;
         b.nd_capv = nd_capv;
-        b.g1 = g1;
+        b.cinfo = cinfo;
         b.state0 = s->state[0];
         b.state1 = s->state[1];
         b.hc_out = hc_out;
@@ -475,10 +477,10 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         b.wave_speed = drain->pressurized_wave_speed_mps;
     }
     SurfArgs &a = s->sa;
-    a.topo = topo;
-    a.g0 = g0;
-    a.g1 = g1;
-    a.g2 = g2;
+    a.cinfo = cinfo;
+    a.tile_start = tile_start;
+    a.ent_lr = ent_lr;
+    a.ent_g = ent_g;
     a.horton = horton;
     a.wet = s->wet;
     a.state0 = s->state[0];
@@ -914,7 +916,7 @@ FL_API int fl_read_ledger(FlSolver *s, double *out, int32_t n, void *stream) {
         sum_blocks(v2, D2_TERMS, all + FL_LEDGER_OUTFALL);
     }
     FL_CUDA(cudaMemsetAsync(s->vol_out, 0, 2 * sizeof(double), st));
-    FL_CUDA(launch_volumes(s->state[0], s->state[1], s->sa.g1, s->Va, s->run, s->C, s->N, s->vol_out, st));
+    FL_CUDA(launch_volumes(s->state[0], s->state[1], s->sa.cinfo, s->Va, s->run, s->C, s->N, s->vol_out, st));
     g_launches++;
     FL_CUDA(cudaMemcpyAsync(all + FL_LEDGER_SURFACE_VOLUME, s->vol_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     FL_CUDA(cudaStreamSynchronize(st));

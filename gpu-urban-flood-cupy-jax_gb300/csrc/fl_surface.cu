@@ -1,22 +1,27 @@
 // Surface kernels for sm_103a.
 //
-// k_surface: one thread per (renumbered) cell.  The thread gathers the
-// fluxes of the cell's three edges itself -- the cell-centric replacement of
-// the reference's per-edge flux kernel with float atomicAdd scatters
-// (gurugram_flood/kernels/triangular_swe_cuda_kernels.py:22-203) -- then does
-// the cell update with Manning damping (:206-252), rainfall and infiltration
-// (triangular_backend.py:1330-1379), and the velocity clamp
-// (solver/stabilizers.py:8-27), all in one pass over the state.  Both cells of
-// an interior edge evaluate the same flux with the edge's own left/right
-// orientation, so the mass flux they apply is bit-identical and the scheme
-// stays exactly conservative without atomics; summation order per cell is
-// fixed, so runs are bitwise reproducible.
+// k_surface: one CTA per tile of 256 consecutive (Hilbert-ordered) cells.
+//   phase 1  the tile's states go to shared memory;
+//   phase 2  the tile's edge entries are evaluated once each -- ghost state,
+//            hydrostatic reconstruction, HLL (reference
+//            triangular_swe_cuda_kernels.py:22-203, equations.py:20-152,
+//            triangular_backend.py:1067-1178,1294-1327) -- and each cell's
+//            share is written to its (cell, slot) place in shared memory (one
+//            writer per place: no atomics);
+//   phase 3  each thread sums its cell's slots in the reference's order and
+//            does the cell update with Manning damping (:206-252), rainfall
+//            and infiltration (triangular_backend.py:1330-1379), the velocity
+//            clamp (solver/stabilizers.py:8-27), wet time, snapshot writes,
+//            the inlet requests of its cell and the ledger.
+// An interior edge inside a tile is evaluated once; an edge between two tiles
+// once in each (same code), so the two cells always apply the same mass flux:
+// the scheme is exactly conservative and bitwise reproducible.
 //
-// The flux arithmetic uses reciprocal-based division and fast exp/log (the
-// kernel is instruction-bound); values stay within a few ulp of the
-// reference's correctly rounded float32 operations.  The velocity clamp and
-// the CFL dt use correctly rounded, uncontracted operations and match the
-// reference bit-for-bit.
+// The flux arithmetic uses reciprocal-based division and fast exp/log (it is
+// instruction-bound); values stay within a few ulp of the reference's
+// correctly rounded float32 operations.  The velocity clamp and the CFL dt use
+// correctly rounded, uncontracted operations and match the reference
+// bit-for-bit.
 //
 // k_dt: the global CFL minimum (equations.py:155-178) as a warp-shuffle and
 // single-pass grid reduction; the last block to finish plans the step.
@@ -25,7 +30,9 @@
 namespace fl {
 
 template <int KIND>
-__global__ void __launch_bounds__(256, 4) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
+__global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
+    __shared__ float4 s_state[TILE];       // the tile's cell states
+    __shared__ float s_flux[TILE * 3 * 3];  // per (cell, slot): the edge's contribution x len
     wait_for_previous_grid();
     const StepCtrl s = a.ctrl[slot];
     if (plan_next && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -35,120 +42,137 @@ __global__ void __launch_bounds__(256, 4) k_surface(const __grid_constant__ Surf
     allow_next_grid();
     const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
     float4 *__restrict__ out = s.parity ? a.state0 : a.state1;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    float led[SURF_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const int c0 = blockIdx.x * TILE;
+    const int tid = threadIdx.x;
+    const int c = c0 + tid;
+    const bool valid = c < a.C;
+    const float dt = s.dt_f;
+    const float md = a.md;
     const bool do_surface = (s.phases & FL_PHASE_SURFACE) != 0;
     const bool drain_finishes = (s.phases & FL_PHASE_DRAINAGE) != 0;
-    if (c < a.C) {
-        const float4 st = in[c];
-        const uint4 tp = a.topo[c];
+    float led[SURF_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
+
+    // phase 1: the tile's states into shared memory, contributions zeroed
+    float4 st = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 ci = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+    float4 hz = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    float wt = 0.0f;
+    if (valid) {
+        st = in[c];
+        ci = a.cinfo[c];
+        if (KIND == 1) {
+            hz = a.horton[c];
+            wt = a.wet[c];
+        }
         if (s.check_finite && !isfinite(st.x)) {
             if (atomicCAS(&a.run->error, 0, FL_E_NONFINITE) == 0) a.run->error_step = s.step;
         }
-        const float dt = s.dt_f;
-        const float md = a.md;
+    }
+    s_state[tid] = st;
+#pragma unroll
+    for (int j = 0; j < 9; ++j) s_flux[tid * 9 + j] = 0.0f;
+    __syncthreads();
+
+    // phase 2: each edge entry of the tile once; both cells of an edge get the
+    // flux of one evaluation in the edge's own (left, right) orientation, and
+    // an edge shared with another tile is evaluated there by the same code
+    // (single call site), so the mass flux always matches bit-for-bit.
+    if (do_surface) {
+        const int e1 = a.tile_start[blockIdx.x + 1];
+#pragma unroll 1
+        for (int e = a.tile_start[blockIdx.x] + tid; e < e1; e += TILE) {
+            const int2 lr = a.ent_lr[e];
+            const float4 gg = a.ent_g[e];
+            const uint32_t f = __float_as_uint(gg.w);
+            const bool lp = (f & EF_LPRESENT) != 0, rp = (f & EF_RPRESENT) != 0;
+            const bool ai = (f & EF_AI) != 0, interior = (f & EF_INTERIOR) != 0;
+            const int code = (int)((f >> EF_CODE_SHIFT) & 7u) - 1;
+            float4 Ls = lp ? s_state[lr.x - c0] : in[lr.x];
+            if (!(f & EF_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
+            const float4 Rs = ai ? (rp ? s_state[lr.y - c0] : in[lr.y])
+                                 : ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, gg.x, gg.y, code, a.stage);
+            EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, gg.x, gg.y, a.g, a.half_g, md);
+            const float len = gg.z;
+            if (lp) {
+                if (!interior && code == 4 && fl.h < 0.0f) {
+                    fl.h = 0.0f; fl.huL = 0.0f; fl.hvL = 0.0f;
+                }
+                const int o = ((lr.x - c0) * 3 + (int)((f >> EF_LSLOT_SHIFT) & 3u)) * 3;
+                s_flux[o] = (-fl.h) * len;
+                s_flux[o + 1] = (-fl.huL) * len;
+                s_flux[o + 2] = (-fl.hvL) * len;
+                if (!ai) {
+                    const float b = fl.h * len * dt;
+                    led[2] += fmax32(-b, 0.0f);
+                    led[3] += fmax32(b, 0.0f);
+                }
+            }
+            if (rp) {
+                const int o = ((lr.y - c0) * 3 + (int)((f >> EF_RSLOT_SHIFT) & 3u)) * 3;
+                s_flux[o] = fl.h * len;
+                s_flux[o + 1] = fl.huR * len;
+                s_flux[o + 2] = fl.hvR * len;
+            }
+        }
+    }
+    __syncthreads();
+
+    // phase 3: the cell update
+    if (valid) {
+        const uint32_t info = __float_as_uint(ci.z);
         float hn = 0.0f, hun = 0.0f, hvn = 0.0f;
-        const bool act = (tp.w & CELL_ACTIVE) != 0;
         if (!do_surface) {
             hn = st.x; hun = st.y; hvn = st.z;
-        } else if (act || (tp.w & CELL_STAGE_LEDGER)) {
-            // An inactive cell only evaluates its exterior stage edges: the
-            // reference counts their flux in the boundary ledger and then
-            // zeroes the cell.
-            const float4 own = act ? st : make_float4(0.0f, 0.0f, 0.0f, st.w);
+        } else if (info & CELL_ACTIVE) {
+            // the reference's scatter order: left-side contributions, then right-side ones
             float L0 = 0.0f, L1 = 0.0f, L2 = 0.0f, R0 = 0.0f, R1 = 0.0f, R2 = 0.0f;
-            float bin = 0.0f, bout = 0.0f;
-            const float4 g0 = a.g0[c], g1 = a.g1[c], g2 = a.g2[c];
-            // the three neighbour states, gathered together up front
-            const auto nb = [&](uint32_t w) {
-                const uint32_t o = w & IDX_MASK;
-                return (w != SLOT_NONE && o != NO_CELL && (w & OTHER_ACTIVE_BIT)) ? in[o] : own;
-            };
-            const float4 n0 = nb(tp.x), n1 = nb(tp.y), n2 = nb(tp.z);
-            // one flux code path for all three edges (not unrolled): both cells
-            // of an edge run the identical instruction sequence
-#pragma unroll 1
+#pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const uint32_t w = k == 0 ? tp.x : (k == 1 ? tp.y : tp.z);
-                const float4 gk = k == 0 ? g0 : (k == 1 ? g1 : g2);
-                const float4 nbk = k == 0 ? n0 : (k == 1 ? n1 : n2);
-                if (w == SLOT_NONE) continue;
-                const uint32_t other = w & IDX_MASK;
-                const bool interior = other != NO_CELL;
-                const bool oact = (w & OTHER_ACTIVE_BIT) != 0;
-                const bool is_right = (w & RIGHT_BIT) != 0;
-                const int raw = (int)((w >> CODE_SHIFT) & 7u) - 1;
-                const bool ai = interior && oact;
-                if (is_right && !ai) continue;  // the reference adds nothing here
-                if (!act && (is_right || interior || raw != 3)) continue;
-                const int code = (interior && !oact) ? 0 : raw;
-                const float nx = gk.x, ny = gk.y, len = gk.z;
-                // the edge's left and right states in the reference's orientation
-                const float4 o = ai ? nbk : ghost_state(own.x, own.y, own.z, own.w, nx, ny, code, a.stage);
-                const float4 L = is_right ? o : own;
-                const float4 R = is_right ? own : o;
-                EdgeFlux f = hr_flux(L.x, L.y, L.z, L.w, R.x, R.y, R.z, R.w, nx, ny, a.g, a.half_g, md);
-                if (!is_right) {
-                    if (!interior && code == 4 && f.h < 0.0f) {
-                        f.h = 0.0f; f.huL = 0.0f; f.hvL = 0.0f;
-                    }
-                    L0 = L0 + (-f.h) * len;
-                    L1 = L1 + (-f.huL) * len;
-                    L2 = L2 + (-f.hvL) * len;
-                    if (!ai) {
-                        const float b = f.h * len * dt;
-                        bin += fmax32(-b, 0.0f);
-                        bout += fmax32(b, 0.0f);
-                    }
+                const float x = s_flux[tid * 9 + k * 3], y = s_flux[tid * 9 + k * 3 + 1], z = s_flux[tid * 9 + k * 3 + 2];
+                if (info & (1u << (CELL_RIGHT_SHIFT + k))) {
+                    R0 = R0 + x; R1 = R1 + y; R2 = R2 + z;
                 } else {
-                    R0 = R0 + f.h * len;
-                    R1 = R1 + f.huR * len;
-                    R2 = R2 + f.hvR * len;
+                    L0 = L0 + x; L1 = L1 + y; L2 = L2 + z;
                 }
             }
-            led[2] = bin;
-            led[3] = bout;
-            if (act) {
-                const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
-                const float area = g1.w;
-                const float ia = rcp(area);
-                hn = fmax32(st.x + dt * d0 * ia, 0.0f);
-                hun = st.y + dt * d1 * ia;
-                hvn = st.z + dt * d2 * ia;
-                // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
-                const bool wet = hn > md;
-                const float hs = fmax32(hn, md);
-                const float ih = rcp(hs);
-                const float uu = hun * ih, vv = hvn * ih;
-                const float speed = fsqrt(uu * uu + vv * vv);
-                const float n = g0.w;
-                const float h43 = __expf(1.3333334f * __logf(hs));
-                const float damping = 1.0f + s.dtg_f * (n * n) * speed * rcp(h43);
-                const float idamp = rcp(damping);
-                hun = wet ? hun * idamp : 0.0f;
-                hvn = wet ? hvn * idamp : 0.0f;
-                // rainfall, infiltration, momentum rescale, dry zeroing
-                float rain, infil;
-                if (KIND == 1) {
-                    const float4 hz = a.horton[c];
-                    rain = s.rain_f * hz.w;
-                    infil = hz.y + (hz.x - hz.y) * __expf(-hz.z * a.wet[c]);
-                } else {
-                    rain = s.rain_f;
-                    infil = a.infil_scalar;
-                }
-                const float rd = fmax32(rain, 0.0f) * dt;
-                const float h1 = hn + rd;
-                const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
-                const float h2 = h1 - id;
-                const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
-                const bool wet2 = h2 > md;
-                hn = h2;
-                hun = wet2 ? hun * scale : 0.0f;
-                hvn = wet2 ? hvn * scale : 0.0f;
-                led[0] = rd * area;
-                led[1] = id * area;
+            const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
+            const float area = ci.x;
+            const float ia = rcp(area);
+            hn = fmax32(st.x + dt * d0 * ia, 0.0f);
+            hun = st.y + dt * d1 * ia;
+            hvn = st.z + dt * d2 * ia;
+            // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
+            const bool wet = hn > md;
+            const float hs = fmax32(hn, md);
+            const float ih = rcp(hs);
+            const float uu = hun * ih, vv = hvn * ih;
+            const float speed = fsqrt(uu * uu + vv * vv);
+            const float n = ci.y;
+            const float h43 = __expf(1.3333334f * __logf(hs));
+            const float damping = 1.0f + s.dtg_f * (n * n) * speed * rcp(h43);
+            const float idamp = rcp(damping);
+            hun = wet ? hun * idamp : 0.0f;
+            hvn = wet ? hvn * idamp : 0.0f;
+            // rainfall, infiltration, momentum rescale, dry zeroing
+            float rain, infil;
+            if (KIND == 1) {
+                rain = s.rain_f * hz.w;
+                infil = hz.y + (hz.x - hz.y) * __expf(-hz.z * wt);
+            } else {
+                rain = s.rain_f;
+                infil = a.infil_scalar;
             }
+            const float rd = fmax32(rain, 0.0f) * dt;
+            const float h1 = hn + rd;
+            const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
+            const float h2 = h1 - id;
+            const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
+            const bool wet2 = h2 > md;
+            hn = h2;
+            hun = wet2 ? hun * scale : 0.0f;
+            hvn = wet2 ? hvn * scale : 0.0f;
+            led[0] = rd * area;
+            led[1] = id * area;
         }
         if (s.phases & FL_PHASE_CLAMP) {
             // velocity clamp, rounded exactly as the reference computes it
@@ -160,16 +184,16 @@ __global__ void __launch_bounds__(256, 4) k_surface(const __grid_constant__ Surf
         out[c] = make_float4(hn, hun, hvn, st.w);
         // requested inlet capture / surcharge of this cell's inlets, from the
         // depth the drainage step starts with
-        const uint32_t kc = tp.w >> CELL_KCELL_SHIFT;
+        const uint32_t kc = __float_as_uint(ci.w);
         if (kc && drain_finishes && a.has_inlets) {
             const InletReqView &v = a.inl;
             for (int i = v.kcell_start[kc - 1]; i < v.kcell_start[kc]; ++i) {
-                const int n = v.in_node[i];
-                v.req[i] = inlet_request(v, i, hn, ff_clamp0(v.Va[n]), v.node_area[n], dt);
+                const int nn = v.in_node[i];
+                v.req[i] = inlet_request(v, i, hn, ff_clamp0(v.Va[nn]), v.node_area[nn], dt);
             }
         }
-        const bool final_here = !(drain_finishes && (tp.w & CELL_COUPLED));
-        if (KIND == 1 && do_surface && final_here) a.wet[c] = a.wet[c] + dt * (float)(hn > md);
+        const bool final_here = !(drain_finishes && (info & CELL_COUPLED));
+        if (KIND == 1 && do_surface && final_here) a.wet[c] = wt + dt * (float)(hn > md);
         if (s.snap_slot >= 0) {
             const size_t o = (size_t)s.snap_slot * (size_t)a.C + (size_t)c;
             if (final_here) a.snap_h[o] = hn;
@@ -303,12 +327,12 @@ __global__ void k_f32_to_f64(const float *src, double *dst, int32_t n) {
 }
 
 // Current surface volume sum(h * area) and node volume (float64 partials).
-__global__ void k_volumes(const float4 *state0, const float4 *state1, const float4 *g1, const float2 *V,
+__global__ void k_volumes(const float4 *state0, const float4 *state1, const float4 *cinfo, const float2 *V,
                           RunCtrl *run, int32_t C, int32_t N, double *out2) {
     const float4 *st = run->parity ? state1 : state0;
     double vs = 0.0, vn = 0.0;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x)
-        vs += (double)(st[c].x * g1[c].w);
+        vs += (double)(st[c].x * cinfo[c].x);
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x)
         vn += (double)V[n].x + (double)V[n].y;
 #pragma unroll
@@ -342,13 +366,13 @@ static cudaError_t launch_pdl(const void *func, dim3 grid, dim3 block, void **ar
 }
 
 cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, cudaStream_t stream) {
-    const int nb = (a.C + 255) / 256;
+    const int nb = (a.C + TILE - 1) / TILE;
     void *args[] = {(void *)&a, (void *)&slot, (void *)&plan_next};
     const void *fn = kind ? (const void *)k_surface<1> : (const void *)k_surface<0>;
-    return launch_pdl(fn, dim3(nb > 0 ? nb : 1), dim3(256), args, stream);
+    return launch_pdl(fn, dim3(nb > 0 ? nb : 1), dim3(TILE), args, stream);
 }
 
-int surface_blocks(int32_t C) { return (C + 255) / 256 > 0 ? (C + 255) / 256 : 1; }
+int surface_blocks(int32_t C) { return (C + TILE - 1) / TILE > 0 ? (C + TILE - 1) / TILE : 1; }
 
 cudaError_t launch_dt(const DtArgs &a, int blocks, int slot, int plan, cudaStream_t stream) {
     void *args[] = {(void *)&a, (void *)&slot, (void *)&plan};
@@ -403,9 +427,9 @@ cudaError_t launch_f32_to_f64(const float *src, double *dst, int32_t n, cudaStre
     return cudaGetLastError();
 }
 
-cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *g1, const float2 *V, RunCtrl *run,
+cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *cinfo, const float2 *V, RunCtrl *run,
                            int32_t C, int32_t N, double *out2, cudaStream_t stream) {
-    k_volumes<<<608, 256, 0, stream>>>(s0, s1, g1, V, run, C, N, out2);
+    k_volumes<<<608, 256, 0, stream>>>(s0, s1, cinfo, V, run, C, N, out2);
     return cudaGetLastError();
 }
 
