@@ -233,19 +233,92 @@ static __device__ __noinline__ void plan_step(RunCtrl *run, double *snap_t, cons
 }
 
 // --------------------------------------------------------------- reductions
+// Float-float running sum: (hi, lo) += x with TwoSum (Knuth), so per-slot
+// totals over thousands of steps keep about 48 bits without FP64 (whose
+// pipe is a small fraction of the FP32 rate on this part).
+__device__ __forceinline__ void ff_accumulate(float2 *slot, float x) {
+    const float2 v = *slot;
+    const float s = __fadd_rn(v.x, x);
+    const float bp = __fsub_rn(s, v.x);
+    const float e = __fadd_rn(__fsub_rn(v.x, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    const float lo = __fadd_rn(v.y, e);
+    const float hi = __fadd_rn(s, lo);
+    *slot = make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+
 // Per-warp running ledger: lane 0 adds the warp's float32 sums into the
-// warp's own float64 slots (no block barrier; slot = global warp index).
+// warp's own float-float slots (no block barrier; slot = global warp index).
 template <int NT>
-__device__ __forceinline__ void warp_add_ledger(const float (&v)[NT], double *ledger) {
+__device__ __forceinline__ void warp_add_ledger(const float (&v)[NT], float2 *ledger) {
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 #pragma unroll
     for (int j = 0; j < NT; ++j) {
         float x = v[j];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if ((threadIdx.x & 31) == 0) ledger[(size_t)warp * NT + j] += (double)x;
+        if ((threadIdx.x & 31) == 0) ff_accumulate(&ledger[(size_t)warp * NT + j], x);
     }
 }
+
+// --------------------------------------------------------------- async copies
+// Bulk (TMA engine) copies global -> shared completing on an mbarrier, and
+// 16-byte cp.async gathers.  Every wait on an mbarrier is bounded in time.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase with the given parity to complete; false after limit_ns.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+// dst (shared) and src (global) 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Programmatic dependent launch: wait for the previous kernel's writes.
 __device__ __forceinline__ void wait_for_previous_grid() {

@@ -10,25 +10,34 @@
 namespace fl {
 
 // ---------------------------------------------------------------------------
-// Surface layout.  Cells are renumbered along a Hilbert curve and processed
-// in tiles of TILE consecutive cells, one CTA per tile.  A cell's (up to
-// three) edges are its "slots", in the reference's cell_edge_indices order:
-// edges it is the left cell of (ascending), then edges it is the right cell of
-// (ascending).  Each tile has a list of edge entries: every edge with an
-// endpoint in the tile that contributes to it, once per tile (an edge inside
-// the tile is one entry serving both cells; an edge crossing two tiles has an
-// entry in each).  An entry is {left, right} (int2, right = -1 if exterior)
-// plus {nx, ny, len, flags} (float4, flags as bits):
+// Surface layout.  Cells are renumbered along a Hilbert curve and grouped in
+// tiles of TILE consecutive cells; per-cell arrays are padded to a whole
+// number of tiles so every tile is one contiguous, 16-byte aligned block.  A
+// cell's (up to three) edges are its "slots", in the reference's
+// cell_edge_indices order: edges it is the left cell of (ascending), then
+// edges it is the right cell of (ascending).
+//
+// Each tile has a list of edge entries (every edge with an endpoint in the
+// tile that contributes to it, once per tile: an edge inside the tile is one
+// entry serving both cells, an edge between two tiles has an entry in each)
+// and a halo: the cells outside the tile whose state its entries read,
+// ascending.  Entries address cells by tile-local index: 0..TILE-1 for the
+// tile's own cells, TILE + j for halo cell j.  An entry is one float4
+// {nx, ny, len, bits}:
 // ---------------------------------------------------------------------------
 constexpr int TILE = 256;
-constexpr uint32_t EF_LPRESENT = 1u;     // left cell is in this tile and takes -F_L
-constexpr int EF_LSLOT_SHIFT = 1;        // bits 1-2: the edge's slot in the left cell
-constexpr uint32_t EF_RPRESENT = 8u;     // right cell is in this tile and takes +F_R
-constexpr int EF_RSLOT_SHIFT = 4;        // bits 4-5: the edge's slot in the right cell
-constexpr uint32_t EF_LACTIVE = 64u;     // left cell active
-constexpr uint32_t EF_AI = 128u;         // active interior edge
-constexpr uint32_t EF_INTERIOR = 256u;   // the edge has a right cell
-constexpr int EF_CODE_SHIFT = 9;         // bits 9-11: effective boundary code + 1
+constexpr uint32_t EB_IDX_MASK = 1023u;    // bits 0-9: left local index
+constexpr int EB_RIGHT_SHIFT = 10;         // bits 10-19: right local index
+constexpr int EB_LSLOT_SHIFT = 20;         // bits 20-21: the edge's slot in the left cell
+constexpr uint32_t EB_LPRESENT = 1u << 22; // the left cell is in this tile and takes -F_L
+constexpr int EB_RSLOT_SHIFT = 23;         // bits 23-24: the edge's slot in the right cell
+constexpr uint32_t EB_RPRESENT = 1u << 25; // the right cell is in this tile and takes +F_R
+constexpr uint32_t EB_LACTIVE = 1u << 26;  // left cell active
+constexpr uint32_t EB_AI = 1u << 27;       // active interior edge
+constexpr uint32_t EB_INTERIOR = 1u << 28; // the edge has a right cell
+constexpr int EB_CODE_SHIFT = 29;          // bits 29-31: effective boundary code + 1
+constexpr int MAX_HALO = 3 * TILE;         // local indices stay below 1024
+// tile_info[t] = {first entry, entry count, first halo index (multiple of 4), halo count}
 constexpr int64_t MAX_CELLS = 0x7FFFFFFE;
 
 // cinfo[c] = {area, manning, flags (bits), inlet-cell index + 1 (bits, 0 = none)}
@@ -80,7 +89,7 @@ struct HyetoView {
     int32_t n;
 };
 
-// Ledger slots of the per-warp running sums.
+// Ledger slots of the per-warp running sums (float-float pairs).
 constexpr int SURF_TERMS = 4;   // rain, infil, boundary in, boundary out
 constexpr int D1_TERMS = 2;     // capture, surcharge
 constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer|
@@ -100,17 +109,22 @@ struct InletReqView {
 };
 
 struct SurfArgs {
-    const float4 *cinfo;          // {area, manning, flags, inlet cell + 1}
-    const int32_t *tile_start;    // [tiles + 1] entry range of each tile
-    const int2 *ent_lr;           // entry {left, right}
-    const float4 *ent_g;          // entry {nx, ny, len, flags}
-    const float4 *horton;         // {f0, fc, k, rain multiplier} (kind 1)
-    float *wet;                   // wet time (kind 1)
-    float4 *state0, *state1;      // {h, hu, hv, bed}
+    const float4 *cinfo;          // [Cp] {area, manning, flags, inlet cell + 1}
+    const int4 *tile_info;        // [tiles]
+    const float4 *ent;            // entries {nx, ny, len, bits}
+    const int32_t *halo_src;      // halo cells of each tile (padded to 4 per tile)
+    const float4 *horton;         // [Cp] {f0, fc, k, rain multiplier} (kind 1)
+    float *wet;                   // [Cp] wet time (kind 1)
+    float4 *state0, *state1;      // [Cp] {h, hu, hv, bed}
     StepCtrl *ctrl;
     RunCtrl *run;
     HyetoView hy;
-    double *ledger;               // [warps * SURF_TERMS]
+    float2 *ledger;               // [grid * 8 * SURF_TERMS] float-float running sums
+    int32_t n_tiles;
+    int32_t e_cap, h_cap;         // largest entry / padded halo count of a tile
+    // dynamic shared memory layout (bytes): flux slots, barriers, two stages
+    int32_t off_bar, off_stage, stage_bytes;
+    int32_t so_ci, so_hz, so_wt, so_en, so_hs;  // offsets inside a stage (states at 0)
     float *snap_h, *snap_hu, *snap_hv;
     double *snap_t;
     int32_t C;
@@ -148,7 +162,7 @@ struct D1Args {
     const float2 *Va;             // node volume (float-float) before
     float2 *Vb;                   // after the exchange
     StepCtrl *ctrl;
-    double *ledger;               // [warps * D1_TERMS]
+    float2 *ledger;               // [warps * D1_TERMS] float-float running sums
     int32_t K, N;
 };
 
@@ -183,7 +197,7 @@ struct D2Args {
     float *wet;
     float *snap_h, *snap_v;
     StepCtrl *ctrl;
-    double *ledger;               // [warps * D2_TERMS]
+    float2 *ledger;               // [warps * D2_TERMS] float-float running sums
     int32_t G, C, N;
     int32_t forcing_kind;
     float g, md, wave_speed;
@@ -194,10 +208,12 @@ struct HostLayout {
     int32_t C = 0, E = 0, N = 0, L = 0, I = 0, K = 0, G = 0;
     std::vector<int32_t> perm;        // perm[new] = reference cell
     std::vector<int32_t> inv;         // inv[reference] = new
-    std::vector<float4> cinfo;
-    std::vector<int32_t> tile_start;
-    std::vector<int2> ent_lr;
-    std::vector<float4> ent_g;
+    int32_t Cp = 0;                   // C rounded up to whole tiles
+    std::vector<float4> cinfo;        // [Cp]
+    std::vector<int4> tile_info;
+    std::vector<float4> ent;
+    std::vector<int32_t> halo_src;
+    int32_t e_cap = 0, h_cap = 0;
     std::vector<float> char_len;
     std::vector<float> bed;
     int64_t slots_used = 0;

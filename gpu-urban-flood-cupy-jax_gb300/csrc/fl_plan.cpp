@@ -44,6 +44,39 @@ float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); 
 
 }  // namespace
 
+// Bounds check of the tile tables against the buffers the surface kernel
+// copies and indexes: every entry's local indices inside its tile's own cells
+// plus halo, every halo cell a real cell, every copy 16-byte sized.
+static int validate_tiles(const HostLayout &L) {
+    const int64_t tiles = (int64_t)L.tile_info.size();
+    for (int64_t t = 0; t < tiles; ++t) {
+        const int4 ti = L.tile_info[t];
+        const int64_t own = std::min<int64_t>(TILE, (int64_t)L.C - t * TILE);
+        if (ti.x < 0 || ti.y < 0 || (int64_t)ti.x + ti.y > (int64_t)L.ent.size() || ti.y > L.e_cap ||
+            ti.z < 0 || ti.z % 4 != 0 || ti.w < 0 || ti.w > MAX_HALO || (int64_t)ti.z + ((ti.w + 3) & ~3) > (int64_t)L.halo_src.size() ||
+            ((ti.w + 3) & ~3) > L.h_cap)
+            return set_error(FL_E_INVALID, "internal: tile %lld table out of range", (long long)t);
+        for (int32_t j = 0; j < ti.w; ++j) {
+            const int32_t g = L.halo_src[ti.z + j];
+            if (g < 0 || g >= L.C || (g >= t * TILE && g < t * TILE + own))
+                return set_error(FL_E_INVALID, "internal: tile %lld halo cell %d out of range", (long long)t, g);
+        }
+        for (int32_t j = 0; j < ti.y; ++j) {
+            uint32_t bits;
+            memcpy(&bits, &L.ent[ti.x + j].w, 4);
+            const uint32_t li = bits & EB_IDX_MASK, ri = (bits >> EB_RIGHT_SHIFT) & EB_IDX_MASK;
+            const bool lin = li < (uint32_t)own, rin = ri < (uint32_t)own;
+            const bool lok = lin || (li >= (uint32_t)TILE && li < (uint32_t)(TILE + ti.w));
+            const bool rok = !(bits & EB_AI) || rin || (ri >= (uint32_t)TILE && ri < (uint32_t)(TILE + ti.w));
+            const uint32_t ls = (bits >> EB_LSLOT_SHIFT) & 3u, rs = (bits >> EB_RSLOT_SHIFT) & 3u;
+            if (!lok || !rok || ((bits & EB_LPRESENT) && (!lin || ls > 2u)) ||
+                ((bits & EB_RPRESENT) && (!(bits & EB_AI) || !rin || rs > 2u)))
+                return set_error(FL_E_INVALID, "internal: tile %lld entry %d has an out-of-range cell index", (long long)t, j);
+        }
+    }
+    return FL_OK;
+}
+
 int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) {
     const int64_t C = m.cell_count, E = m.edge_count;
     if (C <= 0 || E <= 0) return set_error(FL_E_INVALID, "mesh needs cell_count > 0 and edge_count > 0");
@@ -156,18 +189,32 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
         L.bed[i] = m.bed_elevation_m[c];
     }
 
-    // tile edge lists
+    // tile entry lists and halos
     const int64_t tiles = (C + TILE - 1) / TILE;
-    L.tile_start.assign(tiles + 1, 0);
-    L.ent_lr.clear();
-    L.ent_g.clear();
-    L.ent_lr.reserve((size_t)(C * 17 / 10));
-    L.ent_g.reserve((size_t)(C * 17 / 10));
+    L.Cp = (int32_t)(tiles * TILE);
+    {
+        uint32_t none = 0;
+        float fz;
+        memcpy(&fz, &none, 4);
+        L.cinfo.resize((size_t)L.Cp, f4(1.0f, 0.0f, fz, fz));  // padding cells: inactive, never referenced
+    }
+    L.tile_info.assign((size_t)tiles, make_int4(0, 0, 0, 0));
+    L.ent.clear();
+    L.halo_src.clear();
+    L.ent.reserve((size_t)(C * 17 / 10));
+    L.e_cap = 0;
+    L.h_cap = 0;
     std::vector<int32_t> entry_of(E, -1);  // entry of edge e in the current tile
     std::vector<int64_t> entry_tile(E, -1);
+    std::vector<int32_t> ent_left, ent_right;  // global (renumbered) cells of the tile's entries
+    std::vector<uint32_t> ent_bits;
+    std::vector<int32_t> halo;
     for (int64_t t = 0; t < tiles; ++t) {
-        L.tile_start[t] = (int32_t)L.ent_lr.size();
         const int64_t c0 = t * TILE, c1 = std::min<int64_t>(C, c0 + TILE);
+        const size_t first = L.ent.size();
+        ent_left.clear();
+        ent_right.clear();
+        ent_bits.clear();
         for (int64_t i = c0; i < c1; ++i) {
             const int32_t c = L.perm[i];
             for (int k = 0; k < count[c]; ++k) {
@@ -187,29 +234,76 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
                 if (!contributes) continue;
                 int32_t idx = entry_tile[e] == t ? entry_of[e] : -1;
                 if (idx < 0) {
-                    idx = (int32_t)L.ent_lr.size();
+                    idx = (int32_t)ent_bits.size();
                     entry_of[e] = idx;
                     entry_tile[e] = t;
-                    uint32_t flags = 0;
-                    if (la) flags |= EF_LACTIVE;
-                    if (ai) flags |= EF_AI;
-                    if (interior) flags |= EF_INTERIOR;
-                    flags |= (uint32_t)(code + 1) << EF_CODE_SHIFT;
-                    float ff;
-                    memcpy(&ff, &flags, 4);
-                    L.ent_lr.push_back(make_int2(L.inv[lref], interior ? L.inv[rref] : -1));
-                    L.ent_g.push_back(f4(m.edge_normal_x[e], m.edge_normal_y[e], m.edge_length_m[e], ff));
+                    uint32_t bits = 0;
+                    if (la) bits |= EB_LACTIVE;
+                    if (ai) bits |= EB_AI;
+                    if (interior) bits |= EB_INTERIOR;
+                    bits |= (uint32_t)(code + 1) << EB_CODE_SHIFT;
+                    ent_bits.push_back(bits);
+                    ent_left.push_back(L.inv[lref]);
+                    ent_right.push_back(ai ? L.inv[rref] : -1);  // the right state is read only on active interior edges
+                    L.ent.push_back(f4(m.edge_normal_x[e], m.edge_normal_y[e], m.edge_length_m[e], 0.0f));
                 }
-                uint32_t flags;
-                memcpy(&flags, &L.ent_g[idx].w, 4);
-                if (is_right) flags |= EF_RPRESENT | ((uint32_t)rslot[e] << EF_RSLOT_SHIFT);
-                else flags |= EF_LPRESENT | ((uint32_t)lslot[e] << EF_LSLOT_SHIFT);
-                memcpy(&L.ent_g[idx].w, &flags, 4);
+                if (is_right) ent_bits[idx] |= EB_RPRESENT | ((uint32_t)rslot[e] << EB_RSLOT_SHIFT);
+                else ent_bits[idx] |= EB_LPRESENT | ((uint32_t)lslot[e] << EB_LSLOT_SHIFT);
             }
         }
+        // halo: cells outside the tile that an entry reads, ascending
+        halo.clear();
+        for (size_t j = 0; j < ent_bits.size(); ++j) {
+            if (ent_left[j] < c0 || ent_left[j] >= c1) halo.push_back(ent_left[j]);
+            if (ent_right[j] >= 0 && (ent_right[j] < c0 || ent_right[j] >= c1)) halo.push_back(ent_right[j]);
+        }
+        std::sort(halo.begin(), halo.end());
+        halo.erase(std::unique(halo.begin(), halo.end()), halo.end());
+        if ((int64_t)halo.size() > MAX_HALO)
+            return set_error(FL_E_INVALID, "tile %lld reads %zu outside cells (limit %d)", (long long)t, halo.size(), MAX_HALO);
+        auto local = [&](int32_t g) -> uint32_t {
+            if (g >= c0 && g < c1) return (uint32_t)(g - c0);
+            return (uint32_t)(TILE + (std::lower_bound(halo.begin(), halo.end(), g) - halo.begin()));
+        };
+        for (size_t j = 0; j < ent_bits.size(); ++j) {
+            uint32_t bits = ent_bits[j] | local(ent_left[j]);
+            if (ent_right[j] >= 0) bits |= local(ent_right[j]) << EB_RIGHT_SHIFT;
+            memcpy(&L.ent[first + j].w, &bits, 4);
+        }
+        const int32_t hstart = (int32_t)L.halo_src.size();
+        L.halo_src.insert(L.halo_src.end(), halo.begin(), halo.end());
+        while (L.halo_src.size() % 4) L.halo_src.push_back(halo.empty() ? 0 : halo.back());
+        const int32_t hpad = (int32_t)L.halo_src.size() - hstart;
+        L.tile_info[t] = make_int4((int32_t)first, (int32_t)ent_bits.size(), hstart, (int32_t)halo.size());
+        L.e_cap = std::max(L.e_cap, (int32_t)ent_bits.size());
+        L.h_cap = std::max(L.h_cap, hpad);
+        if (L.ent.size() > (size_t)INT32_MAX) return set_error(FL_E_INVALID, "mesh has too many edge entries");
     }
-    L.tile_start[tiles] = (int32_t)L.ent_lr.size();
-    return FL_OK;
+    return validate_tiles(L);
+}
+
+// Dynamic shared memory of k_surface for the layout's largest tile: the
+// per-(cell, slot) flux places, two mbarriers + two tile records, and two
+// stages of {own + halo states, cell info, [Horton, wet time], entries, halo
+// list}.  Returns the total bytes and fills the offsets in `a`.
+int surface_smem_layout(SurfArgs &a, int kind) {
+    auto up = [](int x, int m) { return (x + m - 1) / m * m; };
+    const int flux = TILE * 3 * 16;
+    a.off_bar = flux;
+    a.off_stage = up(flux + 64, 128);
+    int o = (TILE + a.h_cap) * 16;
+    a.so_ci = o;
+    o += TILE * 16;
+    a.so_hz = o;
+    if (kind) o += TILE * 16;
+    a.so_wt = o;
+    if (kind) o += TILE * 4;
+    a.so_en = o;
+    o += a.e_cap * 16;
+    a.so_hs = o;
+    o += a.h_cap * 4;
+    a.stage_bytes = up(o, 128);
+    return a.off_stage + 2 * a.stage_bytes;
 }
 
 int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L) {

@@ -34,10 +34,13 @@ int set_error(int code, const char *fmt, ...) {
 
 int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L);
 int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L);
+int surface_smem_layout(SurfArgs &a, int kind);
 
 // kernel launchers (fl_surface.cu / fl_drainage.cu)
-cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, cudaStream_t stream);
-int surface_blocks(int32_t C);
+cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, int grid, int smem_bytes,
+                           cudaStream_t stream);
+cudaError_t plan_surface_launch(SurfArgs &a, int kind, int device, int *grid, int *smem_bytes);
+int surface_warps(int grid);
 cudaError_t launch_dt(const DtArgs &a, int blocks, int slot, int plan, cudaStream_t stream);
 cudaError_t launch_replan(RunCtrl *run, double *snap_t, HyetoView hy, StepCtrl *ctrl, int slot, cudaStream_t stream);
 cudaError_t launch_finite(const float4 *s0, const float4 *s1, RunCtrl *run, int32_t C, cudaStream_t stream);
@@ -74,7 +77,8 @@ struct FlSolver {
     int32_t C = 0, N = 0, NL = 0, I = 0, K = 0, G = 0;
     int kind = 0;
     FlParams params{};
-    int dt_blocks = 0, surf_blocks = 0, d1_blocks = 0, d2_blocks = 0;
+    int32_t Cp = 0;  // cells padded to whole tiles
+    int dt_blocks = 0, surf_grid = 0, surf_smem = 0, d1_blocks = 0, d2_blocks = 0;
     int chunk = 32;
     std::vector<void *> allocs;
     // device
@@ -89,7 +93,8 @@ struct FlSolver {
     RunCtrl *run = nullptr;
     double *snap_t = nullptr;
     float *snap_h = nullptr, *snap_hu = nullptr, *snap_hv = nullptr, *snap_v = nullptr;
-    double *led_s = nullptr, *led_1 = nullptr, *led_2 = nullptr;
+    float2 *led_s = nullptr, *led_1 = nullptr, *led_2 = nullptr;  // float-float running sums
+    size_t n_led_s = 0, n_led_1 = 0, n_led_2 = 0;
     double *dt_out = nullptr, *vol_out = nullptr;
     float *stage_f[3] = {nullptr, nullptr, nullptr};
     double *stage_d = nullptr;
@@ -146,7 +151,7 @@ static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStr
         FL_CUDA(launch_dt(s->da, s->dt_blocks, slot, 1, st));
         g_launches++;
     }
-    FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, st));
+    FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, s->surf_grid, s->surf_smem, st));
     g_launches++;
     if (s->has_drain()) {
         FL_CUDA(launch_inlets(s->d1, slot, st));
@@ -191,6 +196,9 @@ static int error_code_message(FlSolver *s) {
                          (long long)r.error_step, r.t / 60.0);
     if (r.error == FL_E_SNAPSHOTS) return set_error(FL_E_SNAPSHOTS, "more than %d snapshots requested", r.max_snaps);
     if (r.error == FL_E_INVALID) return set_error(FL_E_INVALID, "No finite cells are available for timestep calculation.");
+    if (r.error == FL_E_TIMEOUT)
+        return set_error(FL_E_TIMEOUT, "a tile copy of the surface kernel did not complete within its time limit at step %lld",
+                         (long long)r.error_step);
     if (r.error) return set_error(r.error, "device error %d at step %lld", r.error, (long long)r.error_step);
     return FL_OK;
 }
@@ -231,6 +239,25 @@ FL_API int fl_plan_check(const FlMeshDesc *mesh, const FlDrainDesc *drain, int64
         stats[7] = L.max_inlets_per_cell;
     }
     if (perm_out) memcpy(perm_out, L.perm.data(), sizeof(int32_t) * L.perm.size());
+    return FL_OK;
+}
+
+FL_API int fl_plan_tiles(const FlMeshDesc *mesh, int64_t *tiles) {
+    if (!mesh || !tiles) return set_error(FL_E_INVALID, "mesh descriptor or output is NULL");
+    HostLayout L;
+    int rc = build_mesh_layout(*mesh, nullptr, L);
+    if (rc) return rc;
+    int64_t halo = 0;
+    for (const int4 &t : L.tile_info) halo += t.w;
+    SurfArgs a{};
+    a.e_cap = L.e_cap;
+    a.h_cap = L.h_cap;
+    tiles[0] = (int64_t)L.tile_info.size();
+    tiles[1] = (int64_t)L.ent.size();
+    tiles[2] = halo;
+    tiles[3] = L.e_cap;
+    tiles[4] = L.h_cap;
+    tiles[5] = surface_smem_layout(a, 1);
     return FL_OK;
 }
 
@@ -288,21 +315,22 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     s->I = L.I;
     s->K = L.K;
     s->G = L.G;
-    const int32_t C = s->C;
+    s->Cp = L.Cp;
+    const int32_t C = s->C, Cp = s->Cp;
 
-    // static surface layout
-    float4 *cinfo, *ent_g;
-    int2 *ent_lr;
-    int32_t *tile_start;
+    // static surface layout (per-cell arrays padded to whole tiles)
+    float4 *cinfo, *ent;
+    int4 *tile_info;
+    int32_t *halo_src;
     float *char_len;
-    if ((rc = s->upload(&cinfo, L.cinfo)) || (rc = s->upload(&tile_start, L.tile_start)) ||
-        (rc = s->upload(&ent_lr, L.ent_lr)) || (rc = s->upload(&ent_g, L.ent_g)) ||
+    if ((rc = s->upload(&cinfo, L.cinfo)) || (rc = s->upload(&tile_info, L.tile_info)) ||
+        (rc = s->upload(&ent, L.ent)) || (rc = s->upload(&halo_src, L.halo_src)) ||
         (rc = s->upload(&char_len, L.char_len)) || (rc = s->upload(&s->bed, L.bed)) ||
         (rc = s->upload(&s->perm, L.perm)))
         return rc;
     float4 *horton = nullptr;
     if (s->kind == 1) {
-        std::vector<float4> hz(C);
+        std::vector<float4> hz(Cp, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         for (int32_t i = 0; i < C; ++i) {
             const int32_t r = L.perm[i];
             hz[i] = make_float4(forcing->horton_f0_mps[r], forcing->horton_fc_mps[r], forcing->horton_k_per_s[r],
@@ -310,16 +338,16 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         }
         if ((rc = s->upload(&horton, hz))) return rc;
     }
-    if ((rc = s->alloc(&s->wet, C))) return rc;
-    FL_CUDA(cudaMemset(s->wet, 0, sizeof(float) * C));
+    if ((rc = s->alloc(&s->wet, Cp))) return rc;
+    FL_CUDA(cudaMemset(s->wet, 0, sizeof(float) * Cp));
     for (int b = 0; b < 2; ++b) {
-        if ((rc = s->alloc(&s->state[b], C))) return rc;
+        if ((rc = s->alloc(&s->state[b], Cp))) return rc;
     }
     {
-        std::vector<float4> st0(C);
+        std::vector<float4> st0(Cp, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         for (int32_t i = 0; i < C; ++i) st0[i] = make_float4(0.0f, 0.0f, 0.0f, L.bed[i]);
-        FL_CUDA(cudaMemcpy(s->state[0], st0.data(), sizeof(float4) * C, cudaMemcpyHostToDevice));
-        FL_CUDA(cudaMemcpy(s->state[1], st0.data(), sizeof(float4) * C, cudaMemcpyHostToDevice));
+        FL_CUDA(cudaMemcpy(s->state[0], st0.data(), sizeof(float4) * Cp, cudaMemcpyHostToDevice));
+        FL_CUDA(cudaMemcpy(s->state[1], st0.data(), sizeof(float4) * Cp, cudaMemcpyHostToDevice));
     }
     if ((rc = s->alloc(&s->ctrl, 2)) || (rc = s->alloc(&s->run, 1)) || (rc = s->alloc(&s->snap_t, p.max_snapshots)))
         return rc;
@@ -342,14 +370,18 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     s->hy.rate = hy + 2 * nh;
     s->hy.n = nh;
     // scratch
-    s->surf_blocks = surface_blocks(C);
+    s->sa.n_tiles = (int32_t)L.tile_info.size();
+    s->sa.e_cap = L.e_cap;
+    s->sa.h_cap = L.h_cap;
+    FL_CUDA(plan_surface_launch(s->sa, s->kind, device, &s->surf_grid, &s->surf_smem));
+    s->n_led_s = (size_t)surface_warps(s->surf_grid) * SURF_TERMS;
     int sms = 0;
     FL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     s->dt_blocks = std::max(1, std::min(sms * 4, (C + 255) / 256));
     float *dt_partial;
     unsigned int *counter;
     if ((rc = s->alloc(&dt_partial, s->dt_blocks)) || (rc = s->alloc(&counter, 1)) || (rc = s->alloc(&s->dt_out, 1)) ||
-        (rc = s->alloc(&s->vol_out, 2)) || (rc = s->alloc(&s->led_s, (size_t)s->surf_blocks * 8 * SURF_TERMS)))
+        (rc = s->alloc(&s->vol_out, 2)) || (rc = s->alloc(&s->led_s, s->n_led_s)))
         return rc;
     FL_CUDA(cudaMemset(counter, 0, sizeof(unsigned int)));
     for (int b = 0; b < 3; ++b)
@@ -386,8 +418,10 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         s->d1_blocks = inlet_blocks(s->K, s->N);
         s->d2_blocks = network_blocks(s->G);
         float *T;
-        if ((rc = s->alloc(&s->led_1, (size_t)s->d1_blocks * 4 * D1_TERMS)) ||
-            (rc = s->alloc(&s->led_2, (size_t)s->d2_blocks * 4 * D2_TERMS)) || (rc = s->alloc(&T, s->NL)))
+        s->n_led_1 = (size_t)s->d1_blocks * 4 * D1_TERMS;
+        s->n_led_2 = (size_t)s->d2_blocks * 4 * D2_TERMS;
+        if ((rc = s->alloc(&s->led_1, s->n_led_1)) || (rc = s->alloc(&s->led_2, s->n_led_2)) ||
+            (rc = s->alloc(&T, s->NL)))
             return rc;
         s->la.T = T;
         s->d2.T = T;
@@ -478,9 +512,9 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     }
     SurfArgs &a = s->sa;
     a.cinfo = cinfo;
-    a.tile_start = tile_start;
-    a.ent_lr = ent_lr;
-    a.ent_g = ent_g;
+    a.tile_info = tile_info;
+    a.ent = ent;
+    a.halo_src = halo_src;
     a.horton = horton;
     a.wet = s->wet;
     a.state0 = s->state[0];
@@ -579,10 +613,10 @@ FL_API int fl_reset_clock(FlSolver *s, void *stream) {
     FL_CUDA(cudaMemcpyAsync(s->run, s->run_h, sizeof(RunCtrl), cudaMemcpyHostToDevice, st));
     FL_CUDA(cudaMemsetAsync(s->ctrl, 0, sizeof(StepCtrl) * 2, st));
     FL_CUDA(cudaMemsetAsync(s->wet, 0, sizeof(float) * (size_t)s->C, st));
-    FL_CUDA(cudaMemsetAsync(s->led_s, 0, sizeof(double) * (size_t)s->surf_blocks * 8 * SURF_TERMS, st));
+    FL_CUDA(cudaMemsetAsync(s->led_s, 0, sizeof(float2) * s->n_led_s, st));
     if (s->has_drain()) {
-        FL_CUDA(cudaMemsetAsync(s->led_1, 0, sizeof(double) * (size_t)s->d1_blocks * 4 * D1_TERMS, st));
-        FL_CUDA(cudaMemsetAsync(s->led_2, 0, sizeof(double) * (size_t)s->d2_blocks * 4 * D2_TERMS, st));
+        FL_CUDA(cudaMemsetAsync(s->led_1, 0, sizeof(float2) * s->n_led_1, st));
+        FL_CUDA(cudaMemsetAsync(s->led_2, 0, sizeof(float2) * s->n_led_2, st));
     }
     FL_CUDA(cudaStreamSynchronize(st));
     s->slot = 0;
@@ -756,7 +790,7 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
     r.last_dt = dt_s;
     FL_CUDA(cudaMemcpyAsync(&s->ctrl[s->slot], &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, st));
     FL_CUDA(cudaMemcpyAsync(s->run, s->run_h, sizeof(RunCtrl), cudaMemcpyHostToDevice, st));
-    FL_CUDA(launch_surface(s->sa, s->kind, s->slot, 0, st));
+    FL_CUDA(launch_surface(s->sa, s->kind, s->slot, 0, s->surf_grid, s->surf_smem, st));
     g_launches++;
     if (s->has_drain() && (phases & FL_PHASE_DRAINAGE)) {
         FL_CUDA(launch_inlets(s->d1, s->slot, st));
@@ -799,7 +833,7 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
     FL_CUDA(cudaMemcpyAsync(&s->ctrl[0], &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, st));
     auto launch = [&]() -> int {
         switch (kernel) {
-            case 0: FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, st)); break;
+            case 0: FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, s->surf_grid, s->surf_smem, st)); break;
             case 1: FL_CUDA(launch_inlets(s->d1, 0, st)); break;
             case 2: FL_CUDA(launch_network(s->d2, 0, st)); break;
             case 4: FL_CUDA(launch_links(s->la, 0, st)); break;
@@ -891,11 +925,11 @@ FL_API int fl_get_progress(FlSolver *s, FlProgress *out, void *stream) {
     return FL_OK;
 }
 
-static void sum_blocks(const std::vector<double> &v, int terms, double *out) {
+static void sum_blocks(const std::vector<float2> &v, int terms, double *out) {
     for (int j = 0; j < terms; ++j) out[j] = 0.0;
     const size_t blocks = v.size() / terms;
     for (size_t b = 0; b < blocks; ++b)
-        for (int j = 0; j < terms; ++j) out[j] += v[b * terms + j];
+        for (int j = 0; j < terms; ++j) out[j] += (double)v[b * terms + j].x + (double)v[b * terms + j].y;
 }
 
 FL_API int fl_read_ledger(FlSolver *s, double *out, int32_t n, void *stream) {
@@ -903,14 +937,14 @@ FL_API int fl_read_ledger(FlSolver *s, double *out, int32_t n, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
     double all[FL_LEDGER_COUNT] = {0};
-    std::vector<double> v((size_t)s->surf_blocks * 8 * SURF_TERMS);
-    FL_CUDA(cudaMemcpyAsync(v.data(), s->led_s, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, st));
+    std::vector<float2> v(s->n_led_s);
+    FL_CUDA(cudaMemcpyAsync(v.data(), s->led_s, sizeof(float2) * v.size(), cudaMemcpyDeviceToHost, st));
     FL_CUDA(cudaStreamSynchronize(st));
     sum_blocks(v, SURF_TERMS, all + FL_LEDGER_RAINFALL);
     if (s->has_drain()) {
-        std::vector<double> v1((size_t)s->d1_blocks * 4 * D1_TERMS), v2((size_t)s->d2_blocks * 4 * D2_TERMS);
-        FL_CUDA(cudaMemcpyAsync(v1.data(), s->led_1, sizeof(double) * v1.size(), cudaMemcpyDeviceToHost, st));
-        FL_CUDA(cudaMemcpyAsync(v2.data(), s->led_2, sizeof(double) * v2.size(), cudaMemcpyDeviceToHost, st));
+        std::vector<float2> v1(s->n_led_1), v2(s->n_led_2);
+        FL_CUDA(cudaMemcpyAsync(v1.data(), s->led_1, sizeof(float2) * v1.size(), cudaMemcpyDeviceToHost, st));
+        FL_CUDA(cudaMemcpyAsync(v2.data(), s->led_2, sizeof(float2) * v2.size(), cudaMemcpyDeviceToHost, st));
         FL_CUDA(cudaStreamSynchronize(st));
         sum_blocks(v1, D1_TERMS, all + FL_LEDGER_CAPTURE);
         sum_blocks(v2, D2_TERMS, all + FL_LEDGER_OUTFALL);

@@ -1,21 +1,26 @@
 // Surface kernels for sm_103a.
 //
-// k_surface: one CTA per tile of 256 consecutive (Hilbert-ordered) cells.
-//   phase 1  the tile's states go to shared memory;
-//   phase 2  the tile's edge entries are evaluated once each -- ghost state,
-//            hydrostatic reconstruction, HLL (reference
-//            triangular_swe_cuda_kernels.py:22-203, equations.py:20-152,
-//            triangular_backend.py:1067-1178,1294-1327) -- and each cell's
-//            share is written to its (cell, slot) place in shared memory (one
-//            writer per place: no atomics);
+// k_surface: a persistent kernel.  Each CTA walks its tiles (256 consecutive
+// Hilbert-ordered cells each) through a two-stage shared-memory pipeline:
+// while it computes tile i, the bulk-copy (TMA) engine brings tile i+1's
+// contiguous blocks -- states, cell info, Horton fields, wet time, the edge
+// entries and the halo cell list -- into the other stage, and cp.async
+// gathers the halo states, so DRAM latency overlaps the arithmetic.  Per tile:
+//   phase 2  every edge entry of the tile once -- ghost state, hydrostatic
+//            reconstruction, HLL (reference triangular_swe_cuda_kernels.py
+//            :22-203, equations.py:20-152, triangular_backend.py:1067-1178,
+//            1294-1327) -- each cell's share written to its (cell, slot)
+//            place in shared memory (one writer per place: no atomics);
 //   phase 3  each thread sums its cell's slots in the reference's order and
 //            does the cell update with Manning damping (:206-252), rainfall
 //            and infiltration (triangular_backend.py:1330-1379), the velocity
 //            clamp (solver/stabilizers.py:8-27), wet time, snapshot writes,
 //            the inlet requests of its cell and the ledger.
-// An interior edge inside a tile is evaluated once; an edge between two tiles
-// once in each (same code), so the two cells always apply the same mass flux:
-// the scheme is exactly conservative and bitwise reproducible.
+// An edge between two tiles is evaluated in each (same code, same inputs),
+// so its two cells always apply the same mass flux: the scheme is exactly
+// conservative and bitwise reproducible.  The last CTA of the grid only plans
+// the next step (a single thread of float64 control arithmetic that would
+// otherwise delay one CTA's tiles).
 //
 // The flux arithmetic uses reciprocal-based division and fast exp/log (it is
 // instruction-bound); values stay within a few ulp of the reference's
@@ -25,183 +30,290 @@
 //
 // k_dt: the global CFL minimum (equations.py:155-178) as a warp-shuffle and
 // single-pass grid reduction; the last block to finish plans the step.
+#include <algorithm>
+
 #include "fl_device.cuh"
 
 namespace fl {
 
+int surface_smem_layout(SurfArgs &a, int kind);
+
+constexpr uint64_t COPY_WAIT_NS = 1000000000ull;  // 1 s per wait on a tile copy
+
+struct TileStage {
+    float4 *st;         // [TILE + h_cap] own states then halo states
+    float4 *ci;         // [TILE]
+    float4 *hz;         // [TILE] (kind 1)
+    float *wt;          // [TILE] (kind 1)
+    float4 *en;         // [e_cap]
+    int32_t *hs;        // [h_cap]
+};
+
+__device__ __forceinline__ TileStage stage_at(const SurfArgs &a, unsigned char *smem, int s) {
+    unsigned char *b = smem + a.off_stage + s * a.stage_bytes;
+    TileStage t;
+    t.st = (float4 *)b;
+    t.ci = (float4 *)(b + a.so_ci);
+    t.hz = (float4 *)(b + a.so_hz);
+    t.wt = (float *)(b + a.so_wt);
+    t.en = (float4 *)(b + a.so_en);
+    t.hs = (int32_t *)(b + a.so_hs);
+    return t;
+}
+
+// Issue the bulk copies of tile t into a stage (one thread).  The byte count
+// the barrier expects is the sum of exactly the copies issued here.
 template <int KIND>
-__global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
-    __shared__ float4 s_state[TILE];       // the tile's cell states
-    __shared__ float s_flux[TILE * 3 * 3];  // per (cell, slot): the edge's contribution x len
-    wait_for_previous_grid();
-    const StepCtrl s = a.ctrl[slot];
-    if (plan_next && blockIdx.x == 0 && threadIdx.x == 0) {
-        plan_step(a.run, a.snap_t, a.hy, &a.ctrl[slot ^ 1], false, 0.0f, FL_PHASE_ALL);
+__device__ __forceinline__ void issue_tile(const SurfArgs &a, const float4 *in, const TileStage &S, int4 *info_slot,
+                                           uint32_t bar, int t) {
+    const int4 ti = a.tile_info[t];
+    *info_slot = ti;
+    const uint32_t ent_bytes = (uint32_t)ti.y * 16u;
+    const uint32_t halo_bytes = (uint32_t)((ti.w + 3) & ~3) * 4u;
+    uint32_t bytes = TILE * 16u * 2u + ent_bytes + halo_bytes;
+    if (KIND == 1) bytes += TILE * 16u + TILE * 4u;
+    mbar_arrive_expect_tx(bar, bytes);
+    const size_t c0 = (size_t)t * TILE;
+    bulk_copy_g2s(smem_addr(S.st), in + c0, TILE * 16u, bar);
+    bulk_copy_g2s(smem_addr(S.ci), a.cinfo + c0, TILE * 16u, bar);
+    if (KIND == 1) {
+        bulk_copy_g2s(smem_addr(S.hz), a.horton + c0, TILE * 16u, bar);
+        bulk_copy_g2s(smem_addr(S.wt), a.wet + c0, TILE * 4u, bar);
     }
-    if (!s.active) return;
+    if (ent_bytes) bulk_copy_g2s(smem_addr(S.en), a.ent + ti.x, ent_bytes, bar);
+    if (halo_bytes) bulk_copy_g2s(smem_addr(S.hs), a.halo_src + ti.z, halo_bytes, bar);
+}
+
+// Gather the halo states of a staged tile (all threads; after its copy landed).
+__device__ __forceinline__ void gather_halo(const float4 *in, const TileStage &S, int halo_count) {
+    for (int j = threadIdx.x; j < halo_count; j += TILE) cp_async16(smem_addr(&S.st[TILE + j]), in + S.hs[j]);
+    cp_async_commit();
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(TILE, 3) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    float4 *s_flux = (float4 *)smem;  // [TILE * 3] per (cell, slot): {mass, x-mom, y-mom} x len
+    uint64_t *s_bar = (uint64_t *)(smem + a.off_bar);
+    int4 *s_info = (int4 *)(smem + a.off_bar + 16);
+    const int tid = threadIdx.x;
+    const int ncta = (int)gridDim.x - 1;  // the last CTA plans
+    wait_for_previous_grid();
+    if ((int)blockIdx.x == ncta) {
+        if (plan_next && tid == 0) plan_step(a.run, a.snap_t, a.hy, &a.ctrl[slot ^ 1], false, 0.0f, FL_PHASE_ALL);
+        allow_next_grid();
+        return;
+    }
+    const StepCtrl s = a.ctrl[slot];
     allow_next_grid();
+    if (!s.active) return;
     const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
     float4 *__restrict__ out = s.parity ? a.state0 : a.state1;
-    const int c0 = blockIdx.x * TILE;
-    const int tid = threadIdx.x;
-    const int c = c0 + tid;
-    const bool valid = c < a.C;
     const float dt = s.dt_f;
     const float md = a.md;
     const bool do_surface = (s.phases & FL_PHASE_SURFACE) != 0;
     const bool drain_finishes = (s.phases & FL_PHASE_DRAINAGE) != 0;
     float led[SURF_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
 
-    // phase 1: the tile's states into shared memory, contributions zeroed
-    float4 st = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float4 ci = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
-    float4 hz = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-    float wt = 0.0f;
-    if (valid) {
-        st = in[c];
-        ci = a.cinfo[c];
-        if (KIND == 1) {
-            hz = a.horton[c];
-            wt = a.wet[c];
-        }
-        if (s.check_finite && !isfinite(st.x)) {
-            if (atomicCAS(&a.run->error, 0, FL_E_NONFINITE) == 0) a.run->error_step = s.step;
-        }
-    }
-    s_state[tid] = st;
+    const uint32_t bar0 = smem_addr(&s_bar[0]), bar1 = smem_addr(&s_bar[1]);
+    const TileStage S0 = stage_at(a, smem, 0), S1 = stage_at(a, smem, 1);
 #pragma unroll
-    for (int j = 0; j < 9; ++j) s_flux[tid * 9 + j] = 0.0f;
+    for (int k = 0; k < 3; ++k) s_flux[tid * 3 + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t wpar = 0u;     // bit k: parity of the next wait on stage k's barrier
+    uint32_t pending = 0u;  // bit k: stage k has copies issued and not yet waited for (thread 0)
+    if (tid == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar1, 1);
+        mbar_fence_init();
+    }
     __syncthreads();
+    int t = blockIdx.x;
+    if (tid == 0) {
+        issue_tile<KIND>(a, in, S0, &s_info[0], bar0, t);
+        pending = 1u;
+    }
+    bool timed_out = !mbar_wait_bounded(bar0, 0, COPY_WAIT_NS);
+    wpar ^= 1u;
+    if (__syncthreads_or(timed_out)) goto abort;
+    pending = 0u;
+    gather_halo(in, S0, s_info[0].w);
 
-    // phase 2: each edge entry of the tile once; both cells of an edge get the
-    // flux of one evaluation in the edge's own (left, right) orientation, and
-    // an edge shared with another tile is evaluated there by the same code
-    // (single call site), so the mass flux always matches bit-for-bit.
-    if (do_surface) {
-        const int e1 = a.tile_start[blockIdx.x + 1];
+    for (int i = 0; t < a.n_tiles; ++i, t += ncta) {
+        const int st_i = i & 1;
+        const TileStage &S = st_i ? S1 : S0;
+        const TileStage &SN = st_i ? S0 : S1;
+        const uint32_t barN = st_i ? bar0 : bar1;
+        const int tn = t + ncta;
+        if (tid == 0 && tn < a.n_tiles) {
+            issue_tile<KIND>(a, in, SN, &s_info[st_i ^ 1], barN, tn);
+            pending |= 1u << (st_i ^ 1);
+        }
+        cp_async_wait_all();
+        __syncthreads();  // this tile's halo states are in place
+
+        // phase 2: each edge entry of the tile once
+        const int c0 = t * TILE;
+        if (do_surface) {
+            const int n_e = s_info[st_i].y;
 #pragma unroll 1
-        for (int e = a.tile_start[blockIdx.x] + tid; e < e1; e += TILE) {
-            const int2 lr = a.ent_lr[e];
-            const float4 gg = a.ent_g[e];
-            const uint32_t f = __float_as_uint(gg.w);
-            const bool lp = (f & EF_LPRESENT) != 0, rp = (f & EF_RPRESENT) != 0;
-            const bool ai = (f & EF_AI) != 0, interior = (f & EF_INTERIOR) != 0;
-            const int code = (int)((f >> EF_CODE_SHIFT) & 7u) - 1;
-            float4 Ls = lp ? s_state[lr.x - c0] : in[lr.x];
-            if (!(f & EF_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
-            const float4 Rs = ai ? (rp ? s_state[lr.y - c0] : in[lr.y])
-                                 : ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, gg.x, gg.y, code, a.stage);
-            EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, gg.x, gg.y, a.g, a.half_g, md);
-            const float len = gg.z;
-            if (lp) {
-                if (!interior && code == 4 && fl.h < 0.0f) {
-                    fl.h = 0.0f; fl.huL = 0.0f; fl.hvL = 0.0f;
+            for (int e = tid; e < n_e; e += TILE) {
+                const float4 en = S.en[e];
+                const uint32_t f = __float_as_uint(en.w);
+                const uint32_t li = f & EB_IDX_MASK, ri = (f >> EB_RIGHT_SHIFT) & EB_IDX_MASK;
+                const bool ai = (f & EB_AI) != 0;
+                const int code = (int)(f >> EB_CODE_SHIFT) - 1;
+                float4 Ls = S.st[li];
+                if (!(f & EB_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
+                const float4 Rs = ai ? S.st[ri] : ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, en.x, en.y, code, a.stage);
+                EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, en.x, en.y, a.g, a.half_g, md);
+                const float len = en.z;
+                if (f & EB_LPRESENT) {
+                    if (!(f & EB_INTERIOR) && code == 4 && fl.h < 0.0f) {
+                        fl.h = 0.0f; fl.huL = 0.0f; fl.hvL = 0.0f;
+                    }
+                    s_flux[li * 3 + ((f >> EB_LSLOT_SHIFT) & 3u)] = make_float4((-fl.h) * len, (-fl.huL) * len,
+                                                                                (-fl.hvL) * len, 0.0f);
+                    if (!ai) {
+                        const float b = fl.h * len * dt;
+                        led[2] += fmax32(-b, 0.0f);
+                        led[3] += fmax32(b, 0.0f);
+                    }
                 }
-                const int o = ((lr.x - c0) * 3 + (int)((f >> EF_LSLOT_SHIFT) & 3u)) * 3;
-                s_flux[o] = (-fl.h) * len;
-                s_flux[o + 1] = (-fl.huL) * len;
-                s_flux[o + 2] = (-fl.hvL) * len;
-                if (!ai) {
-                    const float b = fl.h * len * dt;
-                    led[2] += fmax32(-b, 0.0f);
-                    led[3] += fmax32(b, 0.0f);
-                }
-            }
-            if (rp) {
-                const int o = ((lr.y - c0) * 3 + (int)((f >> EF_RSLOT_SHIFT) & 3u)) * 3;
-                s_flux[o] = fl.h * len;
-                s_flux[o + 1] = fl.huR * len;
-                s_flux[o + 2] = fl.hvR * len;
+                if (f & EB_RPRESENT)
+                    s_flux[ri * 3 + ((f >> EB_RSLOT_SHIFT) & 3u)] = make_float4(fl.h * len, fl.huR * len, fl.hvR * len, 0.0f);
             }
         }
-    }
-    __syncthreads();
+        // the next tile's copies: wait for them here (they had all of phase 2)
+        // and start its halo gathers, which then overlap phase 3
+        bool bad = false;
+        if (tn < a.n_tiles) {
+            bad = !mbar_wait_bounded(barN, (wpar >> (st_i ^ 1)) & 1u, COPY_WAIT_NS);
+            wpar ^= 1u << (st_i ^ 1);
+        }
+        if (__syncthreads_or(bad)) goto abort;  // also: phase 2's slots are complete
+        pending = 0u;
+        if (tn < a.n_tiles) gather_halo(in, SN, s_info[st_i ^ 1].w);
 
-    // phase 3: the cell update
-    if (valid) {
-        const uint32_t info = __float_as_uint(ci.z);
-        float hn = 0.0f, hun = 0.0f, hvn = 0.0f;
-        if (!do_surface) {
-            hn = st.x; hun = st.y; hvn = st.z;
-        } else if (info & CELL_ACTIVE) {
-            // the reference's scatter order: left-side contributions, then right-side ones
-            float L0 = 0.0f, L1 = 0.0f, L2 = 0.0f, R0 = 0.0f, R1 = 0.0f, R2 = 0.0f;
+        // phase 3: the cell update
+        const int c = c0 + tid;
+        if (c < a.C) {
+            const float4 st = S.st[tid];
+            const float4 ci = S.ci[tid];
+            const uint32_t info = __float_as_uint(ci.z);
+            if (s.check_finite && !isfinite(st.x)) {
+                if (atomicCAS(&a.run->error, 0, FL_E_NONFINITE) == 0) a.run->error_step = s.step;
+            }
+            float wt = 0.0f;
+            float4 hz = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+            if (KIND == 1) {
+                wt = S.wt[tid];
+                hz = S.hz[tid];
+            }
+            float hn = 0.0f, hun = 0.0f, hvn = 0.0f;
+            if (!do_surface) {
+                hn = st.x; hun = st.y; hvn = st.z;
+            } else if (info & CELL_ACTIVE) {
+                // the reference's scatter order: left-side contributions, then right-side ones
+                float L0 = 0.0f, L1 = 0.0f, L2 = 0.0f, R0 = 0.0f, R1 = 0.0f, R2 = 0.0f;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float x = s_flux[tid * 9 + k * 3], y = s_flux[tid * 9 + k * 3 + 1], z = s_flux[tid * 9 + k * 3 + 2];
-                if (info & (1u << (CELL_RIGHT_SHIFT + k))) {
-                    R0 = R0 + x; R1 = R1 + y; R2 = R2 + z;
+                for (int k = 0; k < 3; ++k) {
+                    const float4 v = s_flux[tid * 3 + k];
+                    if (info & (1u << (CELL_RIGHT_SHIFT + k))) {
+                        R0 = R0 + v.x; R1 = R1 + v.y; R2 = R2 + v.z;
+                    } else {
+                        L0 = L0 + v.x; L1 = L1 + v.y; L2 = L2 + v.z;
+                    }
+                }
+                const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
+                const float area = ci.x;
+                const float ia = rcp(area);
+                hn = fmax32(st.x + dt * d0 * ia, 0.0f);
+                hun = st.y + dt * d1 * ia;
+                hvn = st.z + dt * d2 * ia;
+                // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
+                const bool wet = hn > md;
+                const float hs = fmax32(hn, md);
+                const float ih = rcp(hs);
+                const float uu = hun * ih, vv = hvn * ih;
+                const float speed = fsqrt(uu * uu + vv * vv);
+                const float n = ci.y;
+                const float h43 = __expf(1.3333334f * __logf(hs));
+                const float damping = 1.0f + s.dtg_f * (n * n) * speed * rcp(h43);
+                const float idamp = rcp(damping);
+                hun = wet ? hun * idamp : 0.0f;
+                hvn = wet ? hvn * idamp : 0.0f;
+                // rainfall, infiltration, momentum rescale, dry zeroing
+                float rain, infil;
+                if (KIND == 1) {
+                    rain = s.rain_f * hz.w;
+                    infil = hz.y + (hz.x - hz.y) * __expf(-hz.z * wt);
                 } else {
-                    L0 = L0 + x; L1 = L1 + y; L2 = L2 + z;
+                    rain = s.rain_f;
+                    infil = a.infil_scalar;
+                }
+                const float rd = fmax32(rain, 0.0f) * dt;
+                const float h1 = hn + rd;
+                const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
+                const float h2 = h1 - id;
+                const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
+                const bool wet2 = h2 > md;
+                hn = h2;
+                hun = wet2 ? hun * scale : 0.0f;
+                hvn = wet2 ? hvn * scale : 0.0f;
+                led[0] += rd * area;
+                led[1] += id * area;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s_flux[tid * 3 + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (s.phases & FL_PHASE_CLAMP) {
+                // velocity clamp, rounded exactly as the reference computes it.  When
+                // |q|^2 < 0.9999 (vmax max(h, 1e-8))^2 the exact speed is below vmax,
+                // the exact scale is 1 and the momenta are unchanged: skip it.
+                const float hm = fmax32(hn, 1.0e-8f);
+                const float lim = a.vmax * hm;
+                if (!(hun * hun + hvn * hvn < 0.9999f * (lim * lim))) {
+                    const float speed = xdiv(xsqrt(xadd(xmul(hun, hun), xmul(hvn, hvn))), hm);
+                    const float scale = fmin32(1.0f, xdiv(a.vmax, fmax32(speed, 1.0e-12f)));
+                    hun = xmul(hun, scale);
+                    hvn = xmul(hvn, scale);
                 }
             }
-            const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
-            const float area = ci.x;
-            const float ia = rcp(area);
-            hn = fmax32(st.x + dt * d0 * ia, 0.0f);
-            hun = st.y + dt * d1 * ia;
-            hvn = st.z + dt * d2 * ia;
-            // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
-            const bool wet = hn > md;
-            const float hs = fmax32(hn, md);
-            const float ih = rcp(hs);
-            const float uu = hun * ih, vv = hvn * ih;
-            const float speed = fsqrt(uu * uu + vv * vv);
-            const float n = ci.y;
-            const float h43 = __expf(1.3333334f * __logf(hs));
-            const float damping = 1.0f + s.dtg_f * (n * n) * speed * rcp(h43);
-            const float idamp = rcp(damping);
-            hun = wet ? hun * idamp : 0.0f;
-            hvn = wet ? hvn * idamp : 0.0f;
-            // rainfall, infiltration, momentum rescale, dry zeroing
-            float rain, infil;
-            if (KIND == 1) {
-                rain = s.rain_f * hz.w;
-                infil = hz.y + (hz.x - hz.y) * __expf(-hz.z * wt);
-            } else {
-                rain = s.rain_f;
-                infil = a.infil_scalar;
+            out[c] = make_float4(hn, hun, hvn, st.w);
+            // requested inlet capture / surcharge of this cell's inlets, from the
+            // depth the drainage step starts with
+            const uint32_t kc = __float_as_uint(ci.w);
+            if (kc && drain_finishes && a.has_inlets) {
+                const InletReqView &v = a.inl;
+                for (int q = v.kcell_start[kc - 1]; q < v.kcell_start[kc]; ++q) {
+                    const int nn = v.in_node[q];
+                    v.req[q] = inlet_request(v, q, hn, ff_clamp0(v.Va[nn]), v.node_area[nn], dt);
+                }
             }
-            const float rd = fmax32(rain, 0.0f) * dt;
-            const float h1 = hn + rd;
-            const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
-            const float h2 = h1 - id;
-            const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
-            const bool wet2 = h2 > md;
-            hn = h2;
-            hun = wet2 ? hun * scale : 0.0f;
-            hvn = wet2 ? hvn * scale : 0.0f;
-            led[0] = rd * area;
-            led[1] = id * area;
-        }
-        if (s.phases & FL_PHASE_CLAMP) {
-            // velocity clamp, rounded exactly as the reference computes it
-            const float speed = xdiv(xsqrt(xadd(xmul(hun, hun), xmul(hvn, hvn))), fmax32(hn, 1.0e-8f));
-            const float scale = fmin32(1.0f, xdiv(a.vmax, fmax32(speed, 1.0e-12f)));
-            hun = xmul(hun, scale);
-            hvn = xmul(hvn, scale);
-        }
-        out[c] = make_float4(hn, hun, hvn, st.w);
-        // requested inlet capture / surcharge of this cell's inlets, from the
-        // depth the drainage step starts with
-        const uint32_t kc = __float_as_uint(ci.w);
-        if (kc && drain_finishes && a.has_inlets) {
-            const InletReqView &v = a.inl;
-            for (int i = v.kcell_start[kc - 1]; i < v.kcell_start[kc]; ++i) {
-                const int nn = v.in_node[i];
-                v.req[i] = inlet_request(v, i, hn, ff_clamp0(v.Va[nn]), v.node_area[nn], dt);
+            const bool final_here = !(drain_finishes && (info & CELL_COUPLED));
+            if (KIND == 1 && do_surface && final_here) a.wet[c] = wt + dt * (float)(hn > md);
+            if (s.snap_slot >= 0) {
+                const size_t o = (size_t)s.snap_slot * (size_t)a.C + (size_t)c;
+                if (final_here) a.snap_h[o] = hn;
+                a.snap_hu[o] = hun;
+                a.snap_hv[o] = hvn;
             }
         }
-        const bool final_here = !(drain_finishes && (info & CELL_COUPLED));
-        if (KIND == 1 && do_surface && final_here) a.wet[c] = wt + dt * (float)(hn > md);
-        if (s.snap_slot >= 0) {
-            const size_t o = (size_t)s.snap_slot * (size_t)a.C + (size_t)c;
-            if (final_here) a.snap_h[o] = hn;
-            a.snap_hu[o] = hun;
-            a.snap_hv[o] = hvn;
-        }
+        __syncthreads();  // this stage and the flux slots are free again
     }
     warp_add_ledger<SURF_TERMS>(led, a.ledger);
+    return;
+
+abort:
+    // a tile copy did not land in time: record it, give the copies in flight a
+    // second bounded wait so none lands after the CTA has left, and stop
+    if (tid == 0) {
+        if (atomicCAS(&a.run->error, 0, FL_E_TIMEOUT) == 0) a.run->error_step = s.step;
+        // a pending stage's wait gave up; wpar was already advanced past it
+        if (pending & 1u) (void)mbar_wait_bounded(bar0, (wpar & 1u) ^ 1u, COPY_WAIT_NS);
+        if (pending & 2u) (void)mbar_wait_bounded(bar1, ((wpar >> 1) & 1u) ^ 1u, COPY_WAIT_NS);
+    }
+    cp_async_wait_all();
+    __syncthreads();
 }
 
 template __global__ void k_surface<0>(const __grid_constant__ SurfArgs, int, int);
@@ -365,14 +477,45 @@ static cudaError_t launch_pdl(const void *func, dim3 grid, dim3 block, void **ar
     return cudaLaunchKernelExC(&cfg, func, args);
 }
 
-cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, cudaStream_t stream) {
-    const int nb = (a.C + TILE - 1) / TILE;
+cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, int grid, int smem_bytes,
+                           cudaStream_t stream) {
     void *args[] = {(void *)&a, (void *)&slot, (void *)&plan_next};
     const void *fn = kind ? (const void *)k_surface<1> : (const void *)k_surface<0>;
-    return launch_pdl(fn, dim3(nb > 0 ? nb : 1), dim3(TILE), args, stream);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(TILE);
+    cfg.dynamicSmemBytes = (size_t)smem_bytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
-int surface_blocks(int32_t C) { return (C + TILE - 1) / TILE > 0 ? (C + TILE - 1) / TILE : 1; }
+// The persistent grid of k_surface: as many compute CTAs as fit (never more
+// than the tiles), spread so that every CTA gets the same number of tiles,
+// plus the planner CTA.
+cudaError_t plan_surface_launch(SurfArgs &a, int kind, int device, int *grid, int *smem_bytes) {
+    *smem_bytes = surface_smem_layout(a, kind);
+    const void *fn = kind ? (const void *)k_surface<1> : (const void *)k_surface<0>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, *smem_bytes);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TILE, (size_t)*smem_bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int slots = std::max(1, per_sm * sms - 1);
+    const int rounds = (a.n_tiles + slots - 1) / slots;
+    const int ctas = std::max(1, (a.n_tiles + rounds - 1) / rounds);
+    *grid = ctas + 1;
+    return cudaSuccess;
+}
+
+int surface_warps(int grid) { return grid * (TILE / 32); }
 
 cudaError_t launch_dt(const DtArgs &a, int blocks, int slot, int plan, cudaStream_t stream) {
     void *args[] = {(void *)&a, (void *)&slot, (void *)&plan};

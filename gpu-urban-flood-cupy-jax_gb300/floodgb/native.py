@@ -26,6 +26,7 @@ FL_E_STEP_CAP = -5
 FL_E_NOMEM = -6
 FL_E_UNSUPPORTED = -7
 FL_E_SNAPSHOTS = -8
+FL_E_TIMEOUT = -9
 
 FL_PHASE_SURFACE = 1
 FL_PHASE_CLAMP = 2
@@ -131,6 +132,7 @@ _SIGNATURES = {
     "fl_get_snapshots": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_int32, C.c_void_p]),
     "fl_plan_check": (C.c_int, [C.POINTER(FlMeshDesc), C.POINTER(FlDrainDesc), C.POINTER(C.c_int64), i32p]),
+    "fl_plan_tiles": (C.c_int, [C.POINTER(FlMeshDesc), C.POINTER(C.c_int64)]),
     "fl_time_kernel": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, f64p]),
     "fl_launch_count": (C.c_int64, []),
     "fl_stable_timestep_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
@@ -180,7 +182,7 @@ def check(rc: int, what: str = "") -> None:
         raise ValueError(msg)
     if rc == FL_E_NO_DEVICE:
         raise BackendUnavailableError(text)
-    if rc in (FL_E_NONFINITE, FL_E_STEP_CAP, FL_E_SNAPSHOTS):
+    if rc in (FL_E_NONFINITE, FL_E_STEP_CAP, FL_E_SNAPSHOTS, FL_E_TIMEOUT):
         raise SimulationError(msg)
     if rc == FL_E_UNSUPPORTED:
         raise NotImplementedError(msg)
@@ -292,3 +294,15 @@ def plan_check(topo, coupling=None, pipe=None, centroids=None):
     check(rc, "fl_plan_check")
     names = ["cells", "edges", "slots", "inlet_cells", "nodes", "links", "groups", "max_inlets_per_cell"]
     return dict(zip(names, [int(v) for v in stats])), perm
+
+
+def plan_tiles(topo, centroids=None):
+    """Host-only surface tiling report (no GPU): tiles, entries, halo cells,
+    largest tile entry count and halo, shared memory per CTA (bytes)."""
+
+    keep = Keep()
+    m = mesh_desc(topo, keep, centroids)
+    out = (C.c_int64 * 6)()
+    check(load().fl_plan_tiles(C.byref(m), out), "fl_plan_tiles")
+    names = ["tiles", "entries", "halo_cells", "max_entries", "max_halo", "smem_bytes"]
+    return dict(zip(names, [int(v) for v in out]))

@@ -36,7 +36,8 @@ enum {
     FL_E_STEP_CAP = -5,    /* the step cap ended fl_run before the target time */
     FL_E_NOMEM = -6,       /* host or device allocation failed */
     FL_E_UNSUPPORTED = -7, /* input uses a reference feature this library does not implement */
-    FL_E_SNAPSHOTS = -8    /* more snapshots than FlParams.max_snapshots */
+    FL_E_SNAPSHOTS = -8,   /* more snapshots than FlParams.max_snapshots */
+    FL_E_TIMEOUT = -9      /* a device-side wait gave up after its time limit (the run stops) */
 };
 
 /* Step phases for fl_step (a bit set). */
@@ -208,6 +209,12 @@ FL_API int fl_get_snapshots(FlSolver *solver, int32_t first, int32_t count, doub
  * reports its sizes.  stats[0..7] = cells, edges, slots used, inlet cells,
  * nodes, links, drainage groups, max inlets per cell. */
 FL_API int fl_plan_check(const FlMeshDesc *mesh, const FlDrainDesc *drain, int64_t *stats, int32_t *perm_out);
+
+/* Host-only surface tiling report (no GPU needed; no reference counterpart).
+ * tiles[0..5] = tiles, edge entries, halo cells (sum over tiles), largest
+ * entry count of a tile, largest padded halo of a tile, and the shared memory
+ * the surface kernel needs per CTA with per-cell forcing (bytes). */
+FL_API int fl_plan_tiles(const FlMeshDesc *mesh, int64_t *tiles);
 
 /* Time `reps` back-to-back launches of one kernel of a step (0 surface,
  * 1 inlet exchange, 2 pipe network, 3 CFL reduction, 4 link update) between CUDA events on
