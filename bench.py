@@ -302,6 +302,7 @@ def our_arm(args):
     net_ms = solver.time_kernel(2, reps=200, stream=stream)
     dt_ms = solver.time_kernel(3, reps=200, stream=stream)
     link_ms = solver.time_kernel(4, reps=200, stream=stream)
+    donor_ms = solver.time_kernel(5, reps=200, stream=stream)
     alg_surface = C * (24 + 20 + 16 + 8) + E * 24
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_surface / (surf_ms * 1e-3) / 1e9
@@ -324,7 +325,7 @@ def our_arm(args):
             "parallelism": f"replicas x{world}",
             "vs_baseline_ref": "7.447e8 cell-steps/s: reference CuPy on RTX PRO 4000, real 981,880-tri city",
             "algorithmic_bytes_per_solver_step": alg_step,
-            "kernel_ms": {"k_surface": surf_ms, "k_inlets": inlet_ms, "k_links": link_ms, "k_network": net_ms,
+            "kernel_ms": {"k_surface": surf_ms, "k_nodes": inlet_ms, "k_links": link_ms, "k_donor": donor_ms, "k_network": net_ms,
                           "k_dt": dt_ms},
             "solver_step_us": total_ms / len(ms) / steps[-1] * 1000.0,
             "wall_s_timed_region": wall,
@@ -368,7 +369,7 @@ def profile_arm(args):
         except SimulationError:
             pass  # the step cap ends the slice
     else:
-        for k in range(5):
+        for k in range(6):
             solver.time_kernel(k, reps=1)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()

@@ -121,10 +121,9 @@ __device__ __forceinline__ float2 ff_clamp0(float2 a) {
 // inlet_exchange_request_kernel, triangular_inlet_exchange_cuda_kernels.py:52-131).
 // The head difference is (bed - invert) + h - V/A: a static datum offset plus
 // two small depths, exact in float32 at any elevation.
-__device__ __forceinline__ float2 inlet_request(const InletReqView &v, int i, float h_cell, float2 Vn, float An,
-                                                float dt) {
+__device__ __forceinline__ float2 inlet_request(const InletReqView &v, int i, float h_cell, float2 Vn, float dt) {
     const float4 p = v.in_par[i];
-    const float dn = fmax32(ff_val(Vn), 0.0f) / fmax32(An, 1.0e-12f);
+    const float dn = fmax32(ff_val(Vn), 0.0f) / fmax32(p.w, 1.0e-12f);
     const float dh = p.x + h_cell - dn;
     const float capc = p.y * dt;
     const float surc = p.z * dt;
@@ -319,18 +318,5 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-// Programmatic dependent launch: wait for the previous kernel's writes.
-__device__ __forceinline__ void wait_for_previous_grid() {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-#endif
-}
-
-__device__ __forceinline__ void allow_next_grid() {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-#endif
-}
 
 }  // namespace fl

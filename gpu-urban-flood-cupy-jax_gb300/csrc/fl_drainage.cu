@@ -4,24 +4,23 @@
 //
 // The reference does each many-to-one sum (requests per cell, per node, per
 // donor node; volume deltas per node; depth deltas per cell) with float64
-// atomicAdd.  Here every sum is a gather over a precomputed CSR list in a
-// fixed order, and where a quantity of a neighbour is needed (the capture
-// limit of an inlet's cell, the surcharge limit of its node, the donor limit
-// of a link's other end) it is recomputed from the same inputs with the same
-// code, so both sides of every exchange see bit-identical values: volume is
-// conserved exactly as in the reference and runs are reproducible.
-//
-// The inlet requests (reference :52-131) are evaluated by k_surface, which
-// holds each inlet cell's post-surface depth; then three launches per step:
-//   k_inlets  one thread per inlet cell (depth after the exchange) and one per
-//             node (volume after the exchange)              [reference :133-177]
+// atomicAdd.  Here every sum is a gather over a precomputed list in a fixed
+// order, so runs are reproducible, and every exchanged quantity is computed
+// once and read by both sides, so volume is conserved exactly as in the
+// reference.  Per step, after k_surface (which evaluates the inlet requests of
+// its inlet cells and their capture limit factor, reference :52-177):
+//   k_nodes   one thread per node: captures limited by their cells, the
+//             surcharge limit by the node's volume, the node volume after
+//             the exchange                                [reference :133-177]
 //   k_links   one thread per link: the semi-implicit link update from the two
-//             end volumes after the exchange              [pipe network :39-139]
-//   k_network one thread per drainage group = a surface cell together with
-//             the nodes that overflow into it (or an orphan node): donor
-//             limiting of the link transfers, node continuity, outfall,
-//             overflow return and the cell's final depth      [reference
-//             pipe network :141-211, overflow :179-207]
+//             end volumes                              [pipe network :39-139]
+//   k_donor   one thread per node: its donor limit factor, its volume over
+//             the transfers it gives                   [pipe network :141-175]
+//   k_network one thread per group = a surface cell with the nodes that
+//             overflow into it (nodes are numbered so a group's nodes are
+//             consecutive), or a node without a cell: limited transfers, node
+//             continuity, outfall, overflow return, and the cell's final
+//             depth                    [pipe network :141-211, overflow :179-207]
 //
 // Heads are carried as depth relative to a static per-link / per-inlet datum
 // offset (bed - invert, invert_from - invert_to, ...), so float32 keeps
@@ -31,22 +30,6 @@
 #include "fl_device.cuh"
 
 namespace fl {
-
-// Capture limit factor of inlet cell k: surface volume over the summed
-// requests of its inlets (reference inlet_exchange_apply_kernel :133-177).
-__device__ __forceinline__ float cell_capture_factor(const D1Args &a, const float4 *hs, int k) {
-    const int c = a.kcell_cell[k];
-    float sum = 0.0f;
-    for (int i = a.kcell_start[k]; i < a.kcell_start[k + 1]; ++i) sum += a.req[i].x;
-    return fmin32(1.0f, (fmax32(hs[c].x, 0.0f) * a.cinfo[c].x) / fmax32(sum, 1.0e-12f));
-}
-
-// Surcharge limit factor of node n: stored volume over the summed requests.
-__device__ __forceinline__ float node_surcharge_factor(const D1Args &a, int n) {
-    float sum = 0.0f;
-    for (int j = a.node_in_start[n]; j < a.node_in_start[n + 1]; ++j) sum += a.req[a.node_in_list[j]].y;
-    return fmin32(1.0f, fmax32(ff_val(ff_clamp0(a.Va[n])), 0.0f) / fmax32(sum, 1.0e-12f));
-}
 
 // Semi-implicit Saint-Venant link update with circular/Preissmann or
 // rectangular geometry (reference pipe_link_flow_kernel :39-139); returns the
@@ -99,47 +82,31 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
     return fmax32(ff_val(ff_clamp0(V)), 0.0f) / fmax32(A, 1.0e-12f);
 }
 
-// One thread per inlet cell (its depth after the exchange) and one per node
-// (its volume after the exchange).  The requests were written by k_surface;
-// each limit factor is a fixed-order sum over the same values in both the
-// cell's and the node's thread, so capture and surcharge balance exactly.
-__global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a, int slot) {
-    wait_for_previous_grid();
+// One thread per node: the inlet exchange of its volume.
+__global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs a, int slot) {
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    allow_next_grid();
-    const float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
     float led[D1_TERMS] = {0.0f, 0.0f};
-    if (t < a.K) {
-        const int k = t;
-        const int c = a.kcell_cell[k];
-        const float h = hs[c].x;
-        const float area = a.cinfo[c].x;
-        const float capf = cell_capture_factor(a, hs, k);
-        float dh = 0.0f;
-        for (int i = a.kcell_start[k]; i < a.kcell_start[k + 1]; ++i) {
-            const float2 r = a.req[i];
-            const float cap = r.x * capf;
-            const float sur = r.y * node_surcharge_factor(a, a.in_node[i]);
-            dh += (sur - cap) / area;
-            led[0] += cap;
-            led[1] += sur;
-        }
-        a.hc_out[k] = h + dh;
-    } else if (t < a.K + a.N) {
-        const int n = t - a.K;
+    if (n < a.N) {
         const float2 V = ff_clamp0(a.Va[n]);
         const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
         if (j0 == j1) {
             a.Vb[n] = V;
         } else {
-            const float surf = node_surcharge_factor(a, n);
+            float sum = 0.0f;
+            for (int j = j0; j < j1; ++j) sum += a.req[a.in_qk[j].x].y;
+            const float sf = fmin32(1.0f, fmax32(ff_val(V), 0.0f) / fmax32(sum, 1.0e-12f));
             float dv = 0.0f;
             for (int j = j0; j < j1; ++j) {
-                const int i = a.node_in_list[j];
-                const float2 r = a.req[i];
-                dv += r.x * cell_capture_factor(a, hs, a.in_kcell[i]) - r.y * surf;
+                const int2 qk = a.in_qk[j];
+                const float2 r = a.req[qk.x];
+                const float cap = r.x * a.capf[qk.y];
+                const float sur = r.y * sf;
+                a.capsur[qk.x] = make_float2(cap, sur);
+                dv += cap - sur;
+                led[0] += cap;
+                led[1] += sur;
             }
             a.Vb[n] = ff_add(V, dv);
         }
@@ -150,10 +117,8 @@ __global__ void __launch_bounds__(128) k_inlets(const __grid_constant__ D1Args a
 // One thread per link: the transfer volume from the end volumes after the
 // inlet exchange.
 __global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a, int slot) {
-    wait_for_previous_grid();
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    allow_next_grid();
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= a.L) return;
     const int f = a.link_from[l], to = a.link_to[l];
@@ -163,20 +128,33 @@ __global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs 
     a.T[l] = link_transfer(a.lk0[l], a.lk1[l], a.lk2[l], df, dtn, Qin[l], a.g, a.wave_speed, s.dt_f);
 }
 
-// Sum of |transfer| over the links whose donor is node d.
-__device__ __forceinline__ float donor_request(const D2Args &a, int d) {
-    float sum = 0.0f;
-    for (int j = a.node_link_start[d]; j < a.node_link_start[d + 1]; ++j) {
-        const int l = a.node_link_list[j];
-        const float t = a.T[l];
-        const int donor = t >= 0.0f ? a.link_from[l] : a.link_to[l];
-        if (donor == d) sum += fabsf(t);
+// One thread per node: its donor factor min(1, V / sum of the transfers it
+// gives), summed in ascending link order.
+__global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs a, int slot) {
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.N) return;
+    const int js = a.node_link_start[n], je = a.node_link_start[n + 1];
+    float given = 0.0f;
+    for (int j0 = js; j0 < je; j0 += 4) {
+        int2 e[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) e[u] = (j0 + u < je) ? a.nl[j0 + u] : make_int2(-1, 0);
+        float t[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[u] = e[u].x >= 0 ? a.T[e[u].x] : 0.0f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (e[u].x < 0) continue;
+            const uint32_t meta = (uint32_t)e[u].y;
+            if (t[u] >= 0.0f ? (meta & NL_FROM) : (meta & NL_TO)) given += fabsf(t[u]);
+        }
     }
-    return sum;
+    a.fac[n] = fmin32(1.0f, fmax32(ff_val(ff_clamp0(a.Vb[n])), 0.0f) / fmax32(given, 1.0e-12f));
 }
 
-__global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args a, int slot) {
-    wait_for_previous_grid();
+__global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs a, int slot) {
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
     float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
@@ -185,41 +163,56 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args 
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     float led[D2_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (g < a.G) {
-        const int c = a.grp_cell[g];
-        const int k = a.grp_kcell[g];
+        const int4 gr = a.grp[g];
+        const int c = gr.x, k = gr.y;
         float h = 0.0f, area = 1.0f;
         if (c >= 0) {
-            h = (k >= 0) ? a.hc_out[k] : hs[c].x;
+            h = hs[c].x;
             area = a.cinfo[c].x;
+            if (k >= 0) {  // the cell's inlet exchange, in its inlets' order
+                float dh = 0.0f;
+                for (int q = a.kcell_start[k]; q < a.kcell_start[k + 1]; ++q) {
+                    const float2 cs = a.capsur[q];
+                    dh += (cs.y - cs.x) / area;
+                }
+                h = h + dh;
+            }
         }
         float hd = 0.0f;
-        for (int gi = a.grp_start[g]; gi < a.grp_start[g + 1]; ++gi) {
-            const int n = a.grp_nodes[gi];
+        for (int n = gr.z; n < gr.w; ++n) {
             const float2 Vp = ff_clamp0(a.Vb[n]);
-            const float Vpf = fmax32(ff_val(Vp), 0.0f);
-            const int j0 = a.node_link_start[n], j1 = a.node_link_start[n + 1];
-            const float own = donor_request(a, n);
+            const float fn = a.fac[n];
+            const int js = a.node_link_start[n], je = a.node_link_start[n + 1];
             float dv = 0.0f;
-            for (int j = j0; j < j1; ++j) {
-                const int l = a.node_link_list[j];
-                const float t = a.T[l];
-                const int from = a.link_from[l], to = a.link_to[l];
-                const int d = t >= 0.0f ? from : to;
-                float factor;
-                if (d == n) {
-                    factor = fmin32(1.0f, Vpf / fmax32(own, 1.0e-12f));
-                } else {
-                    const float Vd = fmax32(ff_val(ff_clamp0(a.Vb[d])), 0.0f);
-                    factor = fmin32(1.0f, Vd / fmax32(donor_request(a, d), 1.0e-12f));
+            for (int j0 = js; j0 < je; j0 += 4) {
+                int2 e[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) e[u] = (j0 + u < je) ? a.nl[j0 + u] : make_int2(-1, 0);
+                float t[4], fo[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (e[u].x >= 0) {
+                        t[u] = a.T[e[u].x];
+                        fo[u] = a.fac[(uint32_t)e[u].y & NL_NODE_MASK];
+                    }
                 }
-                const float lim = fabsf(t) * factor;
-                const float sgn = (d == from) ? lim : -lim;
-                if (from == n) {
-                    dv -= sgn;
-                    Qout[l] = sgn / fmax32(dt, 1.0e-12f);
-                    led[3] += lim;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (e[u].x < 0) continue;
+                    const uint32_t meta = (uint32_t)e[u].y;
+                    const bool is_from = (meta & NL_FROM) != 0, is_to = (meta & NL_TO) != 0;
+                    // donor = the from-node for t >= 0, else the to-node
+                    const bool donor_is_from = t[u] >= 0.0f || (is_from && is_to);
+                    const bool donor_here = donor_is_from ? is_from : is_to;
+                    const float lim = fabsf(t[u]) * (donor_here ? fn : fo[u]);
+                    const float sgn = donor_is_from ? lim : -lim;
+                    if (is_from) {
+                        dv -= sgn;
+                        Qout[e[u].x] = sgn / fmax32(dt, 1.0e-12f);
+                        led[3] += lim;
+                    }
+                    if (is_to) dv += sgn;
                 }
-                if (to == n) dv += sgn;
             }
             float2 V = ff_clamp0(ff_add(Vp, dv));
             // outfall (reference pipe_outfall_kernel :176-211)
@@ -228,9 +221,9 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args 
             if (nd.z > 0.0f) {
                 const float dh = nd.y + vol / fmax32(nd.x, 1.0e-12f);
                 const float sgn = (float)((dh > 0.0f) - (dh < 0.0f));
-                float q = nd.z * sqrtf(2.0f * a.g * fabsf(dh)) * sgn;
-                q = fmin32(q, nd.w);
-                const float out = fmin32(vol, fmax32(q, 0.0f) * dt);
+                float qo = nd.z * sqrtf(2.0f * a.g * fabsf(dh)) * sgn;
+                qo = fmin32(qo, nd.w);
+                const float out = fmin32(vol, fmax32(qo, 0.0f) * dt);
                 V = ff_add(V, -out);
                 led[0] += out;
             }
@@ -256,36 +249,29 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ D2Args 
     warp_add_ledger<D2_TERMS>(led, a.ledger);
 }
 
-static cudaError_t launch_pdl2(const void *func, dim3 grid, dim3 block, void **args, cudaStream_t stream) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelExC(&cfg, func, args);
-}
-
-int inlet_blocks(int32_t K, int32_t N) { return (K + N + 127) / 128 > 0 ? (K + N + 127) / 128 : 1; }
-int link_blocks(int32_t L) { return (L + 127) / 128 > 0 ? (L + 127) / 128 : 1; }
+int node_blocks(int32_t N) { return (N + 127) / 128 > 0 ? (N + 127) / 128 : 1; }
 int network_blocks(int32_t G) { return (G + 127) / 128 > 0 ? (G + 127) / 128 : 1; }
 
-cudaError_t launch_inlets(const D1Args &a, int slot, cudaStream_t stream) {
-    void *args[] = {(void *)&a, (void *)&slot};
-    return launch_pdl2((const void *)k_inlets, dim3(inlet_blocks(a.K, a.N)), dim3(128), args, stream);
+cudaError_t launch_nodes(const NodeArgs &a, int slot, cudaStream_t stream) {
+    k_nodes<<<node_blocks(a.N), 128, 0, stream>>>(a, slot);
+    return cudaGetLastError();
 }
+
+int link_blocks(int32_t L) { return (L + 127) / 128 > 0 ? (L + 127) / 128 : 1; }
 
 cudaError_t launch_links(const LinkArgs &a, int slot, cudaStream_t stream) {
-    void *args[] = {(void *)&a, (void *)&slot};
-    return launch_pdl2((const void *)k_links, dim3(link_blocks(a.L)), dim3(128), args, stream);
+    k_links<<<link_blocks(a.L), 128, 0, stream>>>(a, slot);
+    return cudaGetLastError();
 }
 
-cudaError_t launch_network(const D2Args &a, int slot, cudaStream_t stream) {
-    void *args[] = {(void *)&a, (void *)&slot};
-    return launch_pdl2((const void *)k_network, dim3(network_blocks(a.G)), dim3(128), args, stream);
+cudaError_t launch_donor(const DonorArgs &a, int slot, cudaStream_t stream) {
+    k_donor<<<node_blocks(a.N), 128, 0, stream>>>(a, slot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_network(const NetArgs &a, int slot, cudaStream_t stream) {
+    k_network<<<network_blocks(a.G), 128, 0, stream>>>(a, slot);
+    return cudaGetLastError();
 }
 
 }  // namespace fl

@@ -94,14 +94,27 @@ constexpr int SURF_TERMS = 4;   // rain, infil, boundary in, boundary out
 constexpr int D1_TERMS = 2;     // capture, surcharge
 constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer|
 
+// ---------------------------------------------------------------------------
+// Drainage layout.  Nodes are renumbered so that the nodes overflowing into
+// one surface cell are consecutive ("groups", in cell order; nodes without a
+// surface cell last).  Inlets are in cell order (q, the order the surface
+// kernel evaluates them in); each node lists its inlets (node order j) as
+// in_qk[j] = {q, inlet cell}.  Each node lists its incident links as slots
+// {link, meta}: meta = the other end node | NL_FROM if the node is the link's
+// from-node | NL_TO if it is its to-node (a self-loop has both).
+// ---------------------------------------------------------------------------
+constexpr uint32_t NL_NODE_MASK = 0x3FFFFFFFu;
+constexpr uint32_t NL_FROM = 1u << 30;
+constexpr uint32_t NL_TO = 1u << 31;
+
 // What k_surface needs to evaluate the inlet requests of its cell.
 struct InletReqView {
-    const int32_t *kcell_start;   // [K + 1] inlet range of each inlet cell
-    const int32_t *in_node;       // [I]
-    const float4 *in_par;         // [I] {bed - invert, capture capacity, surcharge capacity, 0}
+    const int32_t *kcell_start;   // [K + 1] inlet range (cell order) of each inlet cell
+    const int32_t *in_node;       // [I] cell order
+    const float4 *in_par;         // [I] {bed - invert, capture capacity, surcharge capacity, node storage area}
     const float2 *Va;             // node volume (float-float) at the start of the drainage step
-    const float *node_area;       // [N]
-    float2 *req;                  // [I] requested capture / surcharge volume this step
+    float2 *req;                  // [I] cell order: requested {capture, surcharge}
+    float *capf;                  // [K] capture limit factor of each inlet cell
     int32_t rule;
     float coef_area;              // float32(Cd * A_orifice)
     float weir_coef_perim;        // float32(Cw * perimeter) for weir_orifice
@@ -150,57 +163,67 @@ struct DtArgs {
     double *dt_out;               // optional: fl_stable_timestep result
 };
 
-struct D1Args {
-    // inlets sorted by (renumbered) cell
-    const int32_t *in_node, *in_kcell;
-    const int32_t *kcell_cell, *kcell_start;   // inlet cells and their inlet ranges
-    const int32_t *node_in_start, *node_in_list;
-    const float2 *req;            // requested capture / surcharge (k_surface)
-    const float4 *cinfo;          // cell area in .x
-    const float4 *state0, *state1;
-    float *hc_out;                // depth of each inlet cell after the exchange
-    const float2 *Va;             // node volume (float-float) before
-    float2 *Vb;                   // after the exchange
+// k_nodes: one thread per node, the inlet exchange of its volume.
+struct NodeArgs {
+    const int32_t *node_in_start; // [N + 1] inlet range (node order)
+    const int2 *in_qk;            // [I] node order: {inlet in cell order, its inlet cell}
+    const float2 *req;            // [I] cell order requested {capture, surcharge}
+    const float *capf;            // [K]
+    float2 *capsur;               // [I] cell order: granted {capture, surcharge}
+    const float2 *Va;             // node volume before the exchange
+    float2 *Vb;                   // after
     StepCtrl *ctrl;
     float2 *ledger;               // [warps * D1_TERMS] float-float running sums
-    int32_t K, N;
+    int32_t N;
 };
 
+// k_links: one thread per link, its transfer volume from the end volumes.
 struct LinkArgs {
     const int32_t *link_from, *link_to;
     const float4 *lk0, *lk1, *lk2;
     const float *node_area;
-    const float2 *Vb;             // node volume after the inlet exchange
+    const float2 *Vb;
     const float *Q0, *Q1;         // link flow, ping-pong with the state parity
-    float *T;                     // transfer volume of each link this step
+    float *T;
     StepCtrl *ctrl;
     int32_t L;
     float g, wave_speed;
 };
 
-struct D2Args {
-    const int32_t *grp_cell, *grp_kcell, *grp_start, *grp_nodes;
-    const int32_t *node_link_start, *node_link_list;
-    const int32_t *link_from, *link_to;
-    const float4 *lk0;            // {length, from-to invert difference, depth offset, manning n}
-    const float4 *lk1;            // {diameter (0: none), area, hydraulic radius, minor loss}
-    const float4 *lk2;            // {flow capacity (inf: none), rect width, rect height, geometry code}
+// k_donor: one thread per node, its donor limit factor.
+struct DonorArgs {
+    const int32_t *node_link_start;  // [N + 1]
+    const int2 *nl;               // link slots {link, meta}
+    const float2 *Vb;
+    const float *T;
+    float *fac;
+    StepCtrl *ctrl;
+    int32_t N;
+};
+
+// k_network: one thread per group (a surface cell with the nodes that overflow
+// into it, or a node without a surface cell).
+struct NetArgs {
+    const int4 *grp;              // {cell or -1, inlet cell or -1, first node, end node}
+    const int32_t *kcell_start;
+    const float2 *capsur;         // cell order granted {capture, surcharge}
+    const int32_t *node_link_start;
+    const int2 *nl;
+    const float *T, *fac;
     const float4 *nd0;            // {storage area, outfall head offset, Cd*A outfall, outfall capacity}
     const float *nd_capv;         // storage area * max(max depth, 0)
     const float4 *cinfo;
     float4 *state0, *state1;
-    const float *hc_out;
     const float2 *Vb;             // after the inlet exchange
     float2 *Va;                   // final
-    const float *T;               // link transfer volumes (k_inlets)
-    float *Q0, *Q1;               // link flow, ping-pong with the state parity
+    float *Q0, *Q1;
     float *wet;
     float *snap_h, *snap_v;
     StepCtrl *ctrl;
     float2 *ledger;               // [warps * D2_TERMS] float-float running sums
     int32_t G, C, N;
     int32_t forcing_kind;
-    float g, md, wave_speed;
+    float g, md;
 };
 
 // Host-side renumbered layout (fl_plan.cpp).
@@ -218,15 +241,18 @@ struct HostLayout {
     std::vector<float> bed;
     int64_t slots_used = 0;
     // drainage
-    std::vector<int32_t> in_cell, in_node, in_kcell, in_order; // in_order[new inlet] = reference inlet
+    std::vector<int32_t> in_cell, in_node, in_kcell, in_order; // cell order; in_order[q] = reference inlet
+    std::vector<int2> in_qk;          // node order: {inlet in cell order, inlet cell}
     std::vector<float4> in_par;
     std::vector<int32_t> kcell_cell, kcell_start;
-    std::vector<int32_t> node_in_start, node_in_list;
+    std::vector<int32_t> node_in_start;
+    std::vector<int32_t> node_perm, node_inv;  // node_perm[new] = reference node
     std::vector<float> node_area, nd_capv;
     std::vector<float4> nd0;
-    std::vector<int32_t> grp_cell, grp_kcell, grp_start, grp_nodes;
-    std::vector<int32_t> node_link_start, node_link_list;
-    std::vector<int32_t> link_from, link_to;
+    std::vector<int4> grp;
+    std::vector<int32_t> node_link_start;
+    std::vector<int2> nl;
+    std::vector<int32_t> link_from, link_to;   // renumbered nodes
     std::vector<float4> lk0, lk1, lk2;
     int32_t max_inlets_per_cell = 0;
 };

@@ -306,6 +306,40 @@ int surface_smem_layout(SurfArgs &a, int kind) {
     return a.off_stage + 2 * a.stage_bytes;
 }
 
+// Bounds check of the drainage tables against the arrays the kernels index.
+static int validate_drain(const HostLayout &L) {
+    const int32_t N = L.N, I = L.I, K = L.K, NL = L.L, C = L.C;
+    if ((int32_t)L.node_in_start.size() != N + 1 || L.node_in_start[0] != 0 || L.node_in_start[N] != I ||
+        (int32_t)L.node_link_start.size() != N + 1 || L.node_link_start[0] != 0 ||
+        L.node_link_start[N] != (int32_t)L.nl.size() || (int32_t)L.kcell_start.size() != K + 1 ||
+        L.kcell_start[0] != 0 || L.kcell_start[K] != I)
+        return set_error(FL_E_INVALID, "internal: drainage table sizes");
+    for (int32_t n = 0; n < N; ++n)
+        if (L.node_in_start[n + 1] < L.node_in_start[n] || L.node_link_start[n + 1] < L.node_link_start[n])
+            return set_error(FL_E_INVALID, "internal: drainage CSR not monotone at node %d", n);
+    for (int32_t k = 0; k < K; ++k)
+        if (L.kcell_start[k + 1] <= L.kcell_start[k] || L.kcell_cell[k] < 0 || L.kcell_cell[k] >= C)
+            return set_error(FL_E_INVALID, "internal: inlet cell %d", k);
+    for (int32_t q = 0; q < I; ++q)
+        if (L.in_node[q] < 0 || L.in_node[q] >= N || L.in_kcell[q] < 0 || L.in_kcell[q] >= K)
+            return set_error(FL_E_INVALID, "internal: inlet %d tables", q);
+    for (int32_t n = 0; n < N; ++n)
+        for (int32_t j = L.node_in_start[n]; j < L.node_in_start[n + 1]; ++j)
+            if (L.in_qk[j].x < 0 || L.in_qk[j].x >= I || L.in_node[L.in_qk[j].x] != n || L.in_qk[j].y != L.in_kcell[L.in_qk[j].x])
+                return set_error(FL_E_INVALID, "internal: node %d inlet list", n);
+    for (const int2 &e : L.nl)
+        if (e.x < 0 || e.x >= NL || (int32_t)((uint32_t)e.y & NL_NODE_MASK) >= N || !((uint32_t)e.y & (NL_FROM | NL_TO)))
+            return set_error(FL_E_INVALID, "internal: link slot out of range");
+    int32_t prev = 0;
+    for (const int4 &g : L.grp) {
+        if (g.x < -1 || g.x >= C || g.y < -1 || g.y >= K || g.z != prev || g.w < g.z || g.w > N)
+            return set_error(FL_E_INVALID, "internal: drainage group out of range");
+        prev = g.w;
+    }
+    if (prev != N) return set_error(FL_E_INVALID, "internal: drainage groups do not cover the nodes");
+    return FL_OK;
+}
+
 int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L) {
     const int32_t N = d.node_count, NL = d.link_count, I = d.inlet_count, C = L.C;
     if (N < 0 || NL < 0 || I < 0) return set_error(FL_E_INVALID, "negative drainage counts");
@@ -329,14 +363,33 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     }
     const float INF = std::numeric_limits<float>::infinity();
 
-    // inlets sorted by renumbered cell (stable in reference order)
-    std::vector<int32_t> order(I);
-    std::iota(order.begin(), order.end(), 0);
+    if ((uint32_t)N > NL_NODE_MASK) return set_error(FL_E_INVALID, "too many drainage nodes");
+    // drainage groups: each coupled cell (a cell with inlets or with nodes that
+    // overflow into it) with its nodes, in cell order, then the nodes without a
+    // surface cell.  Nodes are renumbered in group order.
     for (int32_t i = 0; i < I; ++i) {
         const int32_t c = d.inlet_cell_index[i], n = d.inlet_node_index[i];
         if (c < 0 || c >= C) return set_error(FL_E_INVALID, "inlet_cell_index[%d] = %d is out of range", i, c);
         if (n < 0 || n >= N) return set_error(FL_E_INVALID, "inlet_node_index[%d] = %d is out of range", i, n);
     }
+    std::vector<int32_t> node_cell_new(N, -1);
+    for (int32_t n = 0; n < N; ++n) {
+        const int32_t c = d.node_surface_cell_index[n];
+        node_cell_new[n] = c >= 0 ? L.inv[c] : -1;
+    }
+    L.node_perm.resize(N);
+    std::iota(L.node_perm.begin(), L.node_perm.end(), 0);
+    std::stable_sort(L.node_perm.begin(), L.node_perm.end(), [&](int32_t a, int32_t b) {
+        const int32_t ca = node_cell_new[a] < 0 ? std::numeric_limits<int32_t>::max() : node_cell_new[a];
+        const int32_t cb = node_cell_new[b] < 0 ? std::numeric_limits<int32_t>::max() : node_cell_new[b];
+        return ca < cb;
+    });
+    L.node_inv.assign(N, 0);
+    for (int32_t k = 0; k < N; ++k) L.node_inv[L.node_perm[k]] = k;
+
+    // inlets in cell order (stable in reference order)
+    std::vector<int32_t> order(I);
+    std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
         return L.inv[d.inlet_cell_index[a]] < L.inv[d.inlet_cell_index[b]];
     });
@@ -348,21 +401,21 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     L.kcell_cell.clear();
     L.kcell_start.clear();
     L.max_inlets_per_cell = 0;
-    for (int32_t j = 0; j < I; ++j) {
-        const int32_t i = order[j];
-        const int32_t cref = d.inlet_cell_index[i], n = d.inlet_node_index[i];
+    for (int32_t q = 0; q < I; ++q) {
+        const int32_t i = order[q];
+        const int32_t cref = d.inlet_cell_index[i], nref = d.inlet_node_index[i];
         const int32_t c = L.inv[cref];
         if (L.kcell_cell.empty() || L.kcell_cell.back() != c) {
             L.kcell_cell.push_back(c);
-            L.kcell_start.push_back(j);
+            L.kcell_start.push_back(q);
         }
-        L.in_cell[j] = c;
-        L.in_node[j] = n;
-        L.in_kcell[j] = (int32_t)L.kcell_cell.size() - 1;
-        const double off = (double)m.bed_elevation_m[cref] - (double)d.node_invert_elevation_m[n];
+        L.in_cell[q] = c;
+        L.in_node[q] = L.node_inv[nref];
+        L.in_kcell[q] = (int32_t)L.kcell_cell.size() - 1;
+        const double off = (double)m.bed_elevation_m[cref] - (double)d.node_invert_elevation_m[nref];
         const float capc = d.inlet_capture_capacity_m3ps ? std::max(d.inlet_capture_capacity_m3ps[i], 0.0f) : INF;
         const float surc = d.inlet_surcharge_capacity_m3ps ? std::max(d.inlet_surcharge_capacity_m3ps[i], 0.0f) : INF;
-        L.in_par[j] = f4((float)off, capc, surc, 0.0f);
+        L.in_par[q] = f4((float)off, capc, surc, d.node_storage_area_m2[nref]);
     }
     L.kcell_start.push_back(I);
     L.K = (int32_t)L.kcell_cell.size();
@@ -373,76 +426,55 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     for (int32_t k = 0; k < L.K; ++k)
         L.max_inlets_per_cell = std::max(L.max_inlets_per_cell, L.kcell_start[k + 1] - L.kcell_start[k]);
 
-    // inlets per node (CSR over the sorted inlet order)
+    // inlets in node order (stable in cell order)
     L.node_in_start.assign(N + 1, 0);
-    for (int32_t j = 0; j < I; ++j) L.node_in_start[L.in_node[j] + 1]++;
+    for (int32_t q = 0; q < I; ++q) L.node_in_start[L.in_node[q] + 1]++;
     for (int32_t n = 0; n < N; ++n) L.node_in_start[n + 1] += L.node_in_start[n];
-    L.node_in_list.assign(I, 0);
+    L.in_qk.assign(I, make_int2(0, 0));
     {
         std::vector<int32_t> fill(L.node_in_start.begin(), L.node_in_start.end() - 1);
-        for (int32_t j = 0; j < I; ++j) L.node_in_list[fill[L.in_node[j]]++] = j;
+        for (int32_t q = 0; q < I; ++q) L.in_qk[fill[L.in_node[q]]++] = make_int2(q, L.in_kcell[q]);
     }
 
-    // node parameters
+    // node parameters (renumbered)
     const bool has_outfall = d.outfall_area_m2 && d.outfall_coefficient && d.outfall_tailwater_head_m;
     L.node_area.resize(N);
     L.nd0.resize(N);
     L.nd_capv.resize(N);
-    for (int32_t n = 0; n < N; ++n) {
+    for (int32_t k = 0; k < N; ++k) {
+        const int32_t n = L.node_perm[k];
         const float A = d.node_storage_area_m2[n];
-        L.node_area[n] = A;
+        L.node_area[k] = A;
         float off = 0.0f, ca = 0.0f, cap = INF;
         if (has_outfall) {
             off = (float)((double)d.node_invert_elevation_m[n] - (double)d.outfall_tailwater_head_m[n]);
             ca = d.outfall_coefficient[n] * d.outfall_area_m2[n];
             if (d.outfall_flow_capacity_m3ps) cap = std::max(d.outfall_flow_capacity_m3ps[n], 0.0f);
         }
-        L.nd0[n] = f4(A, off, ca, cap);
-        L.nd_capv[n] = (float)((double)A * (double)std::max(d.node_max_depth_m[n], 0.0f));
+        L.nd0[k] = f4(A, off, ca, cap);
+        L.nd_capv[k] = (float)((double)A * (double)std::max(d.node_max_depth_m[n], 0.0f));
     }
 
-    // drainage groups: each coupled cell with the nodes that overflow into it,
-    // then orphan nodes (no surface cell)
-    std::vector<int32_t> node_cell_new(N, -1);
-    for (int32_t n = 0; n < N; ++n) {
-        const int32_t c = d.node_surface_cell_index[n];
-        node_cell_new[n] = c >= 0 ? L.inv[c] : -1;
-    }
-    std::vector<int32_t> nodes_by_cell(N);
-    std::iota(nodes_by_cell.begin(), nodes_by_cell.end(), 0);
-    std::stable_sort(nodes_by_cell.begin(), nodes_by_cell.end(), [&](int32_t a, int32_t b) {
-        const int32_t ca = node_cell_new[a] < 0 ? std::numeric_limits<int32_t>::max() : node_cell_new[a];
-        const int32_t cb = node_cell_new[b] < 0 ? std::numeric_limits<int32_t>::max() : node_cell_new[b];
-        return ca < cb;
-    });
-    L.grp_cell.clear();
-    L.grp_kcell.clear();
-    L.grp_start.clear();
-    L.grp_nodes.clear();
-    size_t ni = 0;   // cursor into nodes_by_cell
+    // groups over the renumbered nodes
+    L.grp.clear();
+    int32_t ni = 0;  // next renumbered node
     size_t ki = 0;   // cursor into kcell_cell (sorted)
     while (true) {
-        int32_t next_node_cell = std::numeric_limits<int32_t>::max();
-        if (ni < nodes_by_cell.size() && node_cell_new[nodes_by_cell[ni]] >= 0) next_node_cell = node_cell_new[nodes_by_cell[ni]];
+        const int32_t next_node_cell = ni < N && node_cell_new[L.node_perm[ni]] >= 0 ? node_cell_new[L.node_perm[ni]]
+                                                                                      : std::numeric_limits<int32_t>::max();
         const int32_t next_k_cell = ki < L.kcell_cell.size() ? L.kcell_cell[ki] : std::numeric_limits<int32_t>::max();
         const int32_t c = std::min(next_node_cell, next_k_cell);
         if (c == std::numeric_limits<int32_t>::max()) break;
-        L.grp_cell.push_back(c);
-        L.grp_kcell.push_back(next_k_cell == c ? (int32_t)ki : -1);
+        const int32_t kc = next_k_cell == c ? (int32_t)ki : -1;
         if (next_k_cell == c) ++ki;
-        L.grp_start.push_back((int32_t)L.grp_nodes.size());
-        while (ni < nodes_by_cell.size() && node_cell_new[nodes_by_cell[ni]] == c) L.grp_nodes.push_back(nodes_by_cell[ni++]);
+        const int32_t first = ni;
+        while (ni < N && node_cell_new[L.node_perm[ni]] == c) ++ni;
+        L.grp.push_back(make_int4(c, kc, first, ni));
     }
-    for (; ni < nodes_by_cell.size(); ++ni) {  // orphans
-        L.grp_cell.push_back(-1);
-        L.grp_kcell.push_back(-1);
-        L.grp_start.push_back((int32_t)L.grp_nodes.size());
-        L.grp_nodes.push_back(nodes_by_cell[ni]);
-    }
-    L.grp_start.push_back((int32_t)L.grp_nodes.size());
-    L.G = (int32_t)L.grp_cell.size();
+    for (; ni < N; ++ni) L.grp.push_back(make_int4(-1, -1, ni, ni + 1));  // nodes without a surface cell
+    L.G = (int32_t)L.grp.size();
 
-    // links
+    // links (reference order, renumbered end nodes) and each node's link slots
     L.link_from.resize(NL);
     L.link_to.resize(NL);
     L.lk0.resize(NL);
@@ -454,8 +486,9 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
         const int32_t f = d.link_from_node_index[l], t = d.link_to_node_index[l];
         if (f < 0 || f >= N || t < 0 || t >= N)
             return set_error(FL_E_INVALID, "link %d has a node index out of range", l);
-        L.link_from[l] = f;
-        L.link_to[l] = t;
+        const int32_t fn = L.node_inv[f], tn = L.node_inv[t];
+        L.link_from[l] = fn;
+        L.link_to[l] = tn;
         const double invf = d.node_invert_elevation_m[f], invt = d.node_invert_elevation_m[t];
         const double inv = d.link_invert_elevation_m ? (double)d.link_invert_elevation_m[l] : std::min(invf, invt);
         L.lk0[l] = f4(d.link_length_m[l], (float)(invf - invt), (float)(0.5 * (invf + invt) - inv),
@@ -472,20 +505,24 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
         }
         const float capq = d.link_flow_capacity_m3ps ? std::max(d.link_flow_capacity_m3ps[l], 0.0f) : INF;
         L.lk2[l] = f4(capq, W, H, (float)flags);
-        L.node_link_start[f + 1]++;
-        if (t != f) L.node_link_start[t + 1]++;
+        L.node_link_start[fn + 1]++;
+        if (tn != fn) L.node_link_start[tn + 1]++;
     }
     for (int32_t n = 0; n < N; ++n) L.node_link_start[n + 1] += L.node_link_start[n];
-    L.node_link_list.assign(L.node_link_start[N], 0);
+    L.nl.assign(L.node_link_start[N], make_int2(0, 0));
     {
         std::vector<int32_t> fill(L.node_link_start.begin(), L.node_link_start.end() - 1);
-        for (int32_t l = 0; l < NL; ++l) {
+        for (int32_t l = 0; l < NL; ++l) {  // ascending link order in every node's list
             const int32_t f = L.link_from[l], t = L.link_to[l];
-            L.node_link_list[fill[f]++] = l;
-            if (t != f) L.node_link_list[fill[t]++] = l;
+            if (t == f) {
+                L.nl[fill[f]++] = make_int2(l, (int32_t)((uint32_t)f | NL_FROM | NL_TO));
+            } else {
+                L.nl[fill[f]++] = make_int2(l, (int32_t)((uint32_t)t | NL_FROM));
+                L.nl[fill[t]++] = make_int2(l, (int32_t)((uint32_t)f | NL_TO));
+            }
         }
     }
-    return FL_OK;
+    return validate_drain(L);
 }
 
 }  // namespace fl

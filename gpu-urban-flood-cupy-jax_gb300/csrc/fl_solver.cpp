@@ -56,11 +56,14 @@ cudaError_t launch_f64_to_f32(const double *src, float *dst, int32_t n, cudaStre
 cudaError_t launch_f32_to_f64(const float *src, double *dst, int32_t n, cudaStream_t stream);
 cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *g1, const float2 *V, RunCtrl *run,
                            int32_t C, int32_t N, double *out2, cudaStream_t stream);
-cudaError_t launch_inlets(const D1Args &a, int slot, cudaStream_t stream);
-cudaError_t launch_network(const D2Args &a, int slot, cudaStream_t stream);
-int inlet_blocks(int32_t K, int32_t N);
+cudaError_t launch_nodes(const NodeArgs &a, int slot, cudaStream_t stream);
 cudaError_t launch_links(const LinkArgs &a, int slot, cudaStream_t stream);
+cudaError_t launch_donor(const DonorArgs &a, int slot, cudaStream_t stream);
+cudaError_t launch_network(const NetArgs &a, int slot, cudaStream_t stream);
+int node_blocks(int32_t N);
 int network_blocks(int32_t G);
+cudaError_t launch_f64_to_ff_perm(const double *src, float2 *dst, const int32_t *perm, int32_t n, cudaStream_t stream);
+cudaError_t launch_ff_to_f64_perm(const float2 *src, double *dst, const int32_t *perm, int32_t n, cudaStream_t stream);
 
 }  // namespace fl
 
@@ -100,9 +103,12 @@ struct FlSolver {
     double *stage_d = nullptr;
     SurfArgs sa{};
     DtArgs da{};
-    D1Args d1{};
-    LinkArgs la{};
-    D2Args d2{};
+    NodeArgs nd{};
+    LinkArgs lk{};
+    DonorArgs dn{};
+    NetArgs nw{};
+    int32_t *node_perm = nullptr;  // node_perm[new] = reference node
+    float *stage_n = nullptr;      // [N] node-order staging
     HyetoView hy{};
     // host
     RunCtrl *run_h = nullptr;   // pinned mirror
@@ -112,7 +118,7 @@ struct FlSolver {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     bool has_drain() const { return N > 0; }
-    int launches_per_step() const { return 1 + (has_drain() ? 3 : 0); }
+    int launches_per_step() const { return 1 + (has_drain() ? 4 : 0); }
 
     template <class T>
     int alloc(T **p, size_t count) {
@@ -154,10 +160,11 @@ static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStr
     FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, s->surf_grid, s->surf_smem, st));
     g_launches++;
     if (s->has_drain()) {
-        FL_CUDA(launch_inlets(s->d1, slot, st));
-        FL_CUDA(launch_links(s->la, slot, st));
-        FL_CUDA(launch_network(s->d2, slot, st));
-        g_launches += 3;
+        FL_CUDA(launch_nodes(s->nd, slot, st));
+        FL_CUDA(launch_links(s->lk, slot, st));
+        FL_CUDA(launch_donor(s->dn, slot, st));
+        FL_CUDA(launch_network(s->nw, slot, st));
+        g_launches += 4;
     }
     return FL_OK;
 }
@@ -378,8 +385,8 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     int sms = 0;
     FL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     s->dt_blocks = std::max(1, std::min(sms * 4, (C + 255) / 256));
-    float *dt_partial;
-    unsigned int *counter;
+    float *dt_partial = nullptr;
+    unsigned int *counter = nullptr;
     if ((rc = s->alloc(&dt_partial, s->dt_blocks)) || (rc = s->alloc(&counter, 1)) || (rc = s->alloc(&s->dt_out, 1)) ||
         (rc = s->alloc(&s->vol_out, 2)) || (rc = s->alloc(&s->led_s, s->n_led_s)))
         return rc;
@@ -391,50 +398,47 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
 
     // drainage
     if (with_drain) {
-        int32_t *in_cell, *in_node, *in_kcell, *kcell_cell, *kcell_start, *node_in_start, *node_in_list;
+        int32_t *in_node, *kcell_start, *node_in_start, *nls, *lf, *lt;
         float4 *in_par, *nd0, *lk0, *lk1, *lk2;
         float *node_area, *nd_capv;
-        int32_t *grp_cell, *grp_kcell, *grp_start, *grp_nodes, *nls, *nll, *lf, *lt;
-        if ((rc = s->upload(&in_cell, L.in_cell)) || (rc = s->upload(&in_node, L.in_node)) ||
-            (rc = s->upload(&in_kcell, L.in_kcell)) || (rc = s->upload(&in_par, L.in_par)) ||
-            (rc = s->upload(&kcell_cell, L.kcell_cell)) || (rc = s->upload(&kcell_start, L.kcell_start)) ||
-            (rc = s->upload(&node_in_start, L.node_in_start)) || (rc = s->upload(&node_in_list, L.node_in_list)) ||
-            (rc = s->upload(&node_area, L.node_area)) || (rc = s->upload(&nd0, L.nd0)) ||
-            (rc = s->upload(&nd_capv, L.nd_capv)) || (rc = s->upload(&grp_cell, L.grp_cell)) ||
-            (rc = s->upload(&grp_kcell, L.grp_kcell)) || (rc = s->upload(&grp_start, L.grp_start)) ||
-            (rc = s->upload(&grp_nodes, L.grp_nodes)) || (rc = s->upload(&nls, L.node_link_start)) ||
-            (rc = s->upload(&nll, L.node_link_list)) || (rc = s->upload(&lf, L.link_from)) ||
-            (rc = s->upload(&lt, L.link_to)) || (rc = s->upload(&lk0, L.lk0)) || (rc = s->upload(&lk1, L.lk1)) ||
-            (rc = s->upload(&lk2, L.lk2)))
+        int4 *grp;
+        int2 *nl, *in_qk;
+        if ((rc = s->upload(&in_node, L.in_node)) || (rc = s->upload(&in_qk, L.in_qk)) ||
+            (rc = s->upload(&lf, L.link_from)) || (rc = s->upload(&lt, L.link_to)) ||
+            (rc = s->upload(&in_par, L.in_par)) || (rc = s->upload(&kcell_start, L.kcell_start)) ||
+            (rc = s->upload(&node_in_start, L.node_in_start)) || (rc = s->upload(&node_area, L.node_area)) ||
+            (rc = s->upload(&nd0, L.nd0)) || (rc = s->upload(&nd_capv, L.nd_capv)) || (rc = s->upload(&grp, L.grp)) ||
+            (rc = s->upload(&nls, L.node_link_start)) || (rc = s->upload(&nl, L.nl)) ||
+            (rc = s->upload(&lk0, L.lk0)) || (rc = s->upload(&lk1, L.lk1)) || (rc = s->upload(&lk2, L.lk2)) ||
+            (rc = s->upload(&s->node_perm, L.node_perm)))
             return rc;
-        float *hc_out;
         if ((rc = s->alloc(&s->Va, s->N)) || (rc = s->alloc(&s->Vb, s->N)) || (rc = s->alloc(&s->Q[0], s->NL)) ||
-            (rc = s->alloc(&s->Q[1], s->NL)) || (rc = s->alloc(&hc_out, s->K)))
+            (rc = s->alloc(&s->Q[1], s->NL)) || (rc = s->alloc(&s->stage_n, s->N)))
             return rc;
         FL_CUDA(cudaMemset(s->Va, 0, sizeof(float2) * s->N));
         FL_CUDA(cudaMemset(s->Vb, 0, sizeof(float2) * s->N));
         FL_CUDA(cudaMemset(s->Q[0], 0, sizeof(float) * std::max(s->NL, 1)));
         FL_CUDA(cudaMemset(s->Q[1], 0, sizeof(float) * std::max(s->NL, 1)));
-        s->d1_blocks = inlet_blocks(s->K, s->N);
+        s->d1_blocks = node_blocks(s->N);
         s->d2_blocks = network_blocks(s->G);
-        float *T;
         s->n_led_1 = (size_t)s->d1_blocks * 4 * D1_TERMS;
         s->n_led_2 = (size_t)s->d2_blocks * 4 * D2_TERMS;
+        float *T, *fac, *capf;
+        float2 *req, *capsur;
         if ((rc = s->alloc(&s->led_1, s->n_led_1)) || (rc = s->alloc(&s->led_2, s->n_led_2)) ||
-            (rc = s->alloc(&T, s->NL)))
+            (rc = s->alloc(&T, s->NL)) || (rc = s->alloc(&fac, s->N)) || (rc = s->alloc(&capsur, s->I)) ||
+            (rc = s->alloc(&req, s->I)) || (rc = s->alloc(&capf, s->K)))
             return rc;
-        s->la.T = T;
-        s->d2.T = T;
-        float2 *req;
-        if ((rc = s->alloc(&req, s->I))) return rc;
         FL_CUDA(cudaMemset(req, 0, sizeof(float2) * std::max(s->I, 1)));
+        FL_CUDA(cudaMemset(capsur, 0, sizeof(float2) * std::max(s->I, 1)));
+        FL_CUDA(cudaMemset(capf, 0, sizeof(float) * std::max(s->K, 1)));
         InletReqView &v = s->sa.inl;
         v.kcell_start = kcell_start;
         v.in_node = in_node;
         v.in_par = in_par;
         v.Va = s->Va;
-        v.node_area = node_area;
         v.req = req;
+        v.capf = capf;
         v.rule = drain->inlet_capture_rule;
         v.coef_area = drain->inlet_orifice_coefficient * drain->inlet_orifice_area_m2;
         const float eq = sqrtf(4.0f * 3.14159265358979323846f * std::max(drain->inlet_orifice_area_m2, 0.0f));
@@ -442,26 +446,18 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         v.weir_coef_perim = drain->inlet_weir_coefficient * std::max(perim, 0.0f);
         v.g2 = (float)(2.0 * (double)(float)p.gravity_mps2);
         s->sa.has_inlets = s->I > 0;
-        (void)in_cell;
-        D1Args &a = s->d1;
-        a.in_node = in_node;
-        a.in_kcell = in_kcell;
-        a.req = req;
-        a.kcell_cell = kcell_cell;
-        a.kcell_start = kcell_start;
+        NodeArgs &a = s->nd;
         a.node_in_start = node_in_start;
-        a.node_in_list = node_in_list;
-        a.cinfo = cinfo;
-        a.state0 = s->state[0];
-        a.state1 = s->state[1];
-        a.hc_out = hc_out;
+        a.in_qk = in_qk;
+        a.req = req;
+        a.capf = capf;
+        a.capsur = capsur;
         a.Va = s->Va;
         a.Vb = s->Vb;
         a.ctrl = s->ctrl;
         a.ledger = s->led_1;
-        a.K = s->K;
         a.N = s->N;
-        LinkArgs &la = s->la;
+        LinkArgs &la = s->lk;
         la.link_from = lf;
         la.link_to = lt;
         la.lk0 = lk0;
@@ -471,28 +467,32 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         la.Vb = s->Vb;
         la.Q0 = s->Q[0];
         la.Q1 = s->Q[1];
+        la.T = T;
         la.ctrl = s->ctrl;
         la.L = s->NL;
         la.g = (float)p.gravity_mps2;
         la.wave_speed = drain->pressurized_wave_speed_mps;
-        D2Args &b = s->d2;
-        b.grp_cell = grp_cell;
-        b.grp_kcell = grp_kcell;
-        b.grp_start = grp_start;
-        b.grp_nodes = grp_nodes;
+        DonorArgs &dn = s->dn;
+        dn.node_link_start = nls;
+        dn.nl = nl;
+        dn.Vb = s->Vb;
+        dn.T = T;
+        dn.fac = fac;
+        dn.ctrl = s->ctrl;
+        dn.N = s->N;
+        NetArgs &b = s->nw;
+        b.grp = grp;
+        b.kcell_start = kcell_start;
+        b.capsur = capsur;
         b.node_link_start = nls;
-        b.node_link_list = nll;
-        b.link_from = lf;
-        b.link_to = lt;
-        b.lk0 = lk0;
-        b.lk1 = lk1;
-        b.lk2 = lk2;
+        b.nl = nl;
+        b.T = T;
+        b.fac = fac;
         b.nd0 = nd0;
         b.nd_capv = nd_capv;
         b.cinfo = cinfo;
         b.state0 = s->state[0];
         b.state1 = s->state[1];
-        b.hc_out = hc_out;
         b.Vb = s->Vb;
         b.Va = s->Va;
         b.Q0 = s->Q[0];
@@ -508,7 +508,6 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         b.forcing_kind = s->kind;
         b.g = (float)p.gravity_mps2;
         b.md = (float)p.min_depth_m;
-        b.wave_speed = drain->pressurized_wave_speed_mps;
     }
     SurfArgs &a = s->sa;
     a.cinfo = cinfo;
@@ -649,7 +648,7 @@ FL_API int fl_set_state(FlSolver *s, const float *h, const float *hu, const floa
     }
     if (node_volume && s->N > 0) {
         FL_CUDA(cudaMemcpyAsync(s->stage_d, node_volume, sizeof(double) * s->N, k, st));
-        FL_CUDA(launch_f64_to_ff(s->stage_d, s->Va, s->N, st));
+        FL_CUDA(launch_f64_to_ff_perm(s->stage_d, s->Va, s->node_perm, s->N, st));
     }
     if (link_flow && s->NL > 0) {
         FL_CUDA(cudaStreamSynchronize(st));
@@ -684,7 +683,7 @@ FL_API int fl_get_state(FlSolver *s, float *h, float *hu, float *hv, double *nod
         FL_CUDA(cudaStreamSynchronize(st));
     }
     if (node_volume && s->N > 0) {
-        FL_CUDA(launch_ff_to_f64(s->Va, s->stage_d, s->N, st));
+        FL_CUDA(launch_ff_to_f64_perm(s->Va, s->stage_d, s->node_perm, s->N, st));
         FL_CUDA(cudaMemcpyAsync(node_volume, s->stage_d, sizeof(double) * s->N, k, st));
         FL_CUDA(cudaStreamSynchronize(st));
     }
@@ -793,9 +792,10 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
     FL_CUDA(launch_surface(s->sa, s->kind, s->slot, 0, s->surf_grid, s->surf_smem, st));
     g_launches++;
     if (s->has_drain() && (phases & FL_PHASE_DRAINAGE)) {
-        FL_CUDA(launch_inlets(s->d1, s->slot, st));
-        FL_CUDA(launch_links(s->la, s->slot, st));
-        FL_CUDA(launch_network(s->d2, s->slot, st));
+        FL_CUDA(launch_nodes(s->nd, s->slot, st));
+        FL_CUDA(launch_links(s->lk, s->slot, st));
+        FL_CUDA(launch_donor(s->dn, s->slot, st));
+        FL_CUDA(launch_network(s->nw, s->slot, st));
         g_launches += 3;
     } else if (s->has_drain()) {
         // no drainage this step: carry link flow to the other parity buffer
@@ -810,9 +810,9 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
 
 FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *stream, double *ms_per_launch) {
     if (!s || !ms_per_launch || reps < 1) return set_error(FL_E_INVALID, "bad fl_time_kernel arguments");
-    if ((kernel == 1 || kernel == 2 || kernel == 4) && !s->has_drain())
+    if ((kernel == 1 || kernel == 2 || kernel == 4 || kernel == 5) && !s->has_drain())
         return set_error(FL_E_INVALID, "solver has no drainage");
-    if (kernel < 0 || kernel > 4) return set_error(FL_E_INVALID, "kernel must be 0..4");
+    if (kernel < 0 || kernel > 5) return set_error(FL_E_INVALID, "kernel must be 0..5");
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
     int rc = sync_run(s, st);
@@ -834,9 +834,10 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
     auto launch = [&]() -> int {
         switch (kernel) {
             case 0: FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, s->surf_grid, s->surf_smem, st)); break;
-            case 1: FL_CUDA(launch_inlets(s->d1, 0, st)); break;
-            case 2: FL_CUDA(launch_network(s->d2, 0, st)); break;
-            case 4: FL_CUDA(launch_links(s->la, 0, st)); break;
+            case 1: FL_CUDA(launch_nodes(s->nd, 0, st)); break;
+            case 2: FL_CUDA(launch_network(s->nw, 0, st)); break;
+            case 4: FL_CUDA(launch_links(s->lk, 0, st)); break;
+            case 5: FL_CUDA(launch_donor(s->dn, 0, st)); break;
             default: {
                 DtArgs a = s->da;
                 a.dt_out = s->dt_out;
@@ -984,7 +985,11 @@ FL_API int fl_get_snapshots(FlSolver *s, int32_t first, int32_t count, double *t
         }
     }
     if (node_volume && s->N > 0 && count > 0) {
-        FL_CUDA(cudaMemcpyAsync(node_volume, s->snap_v + (size_t)first * s->N, sizeof(float) * (size_t)count * s->N, k, st));
+        for (int32_t i = 0; i < count; ++i) {
+            FL_CUDA(launch_permute_f32(s->snap_v + (size_t)(first + i) * s->N, s->stage_n, s->node_perm, s->N, 1, st));
+            FL_CUDA(cudaMemcpyAsync(node_volume + (size_t)i * s->N, s->stage_n, sizeof(float) * s->N, k, st));
+            FL_CUDA(cudaStreamSynchronize(st));
+        }
     }
     FL_CUDA(cudaStreamSynchronize(st));
     return FL_OK;

@@ -91,21 +91,18 @@ __device__ __forceinline__ void gather_halo(const float4 *in, const TileStage &S
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(TILE, 3) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
+__global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
     extern __shared__ __align__(128) unsigned char smem[];
     float4 *s_flux = (float4 *)smem;  // [TILE * 3] per (cell, slot): {mass, x-mom, y-mom} x len
     uint64_t *s_bar = (uint64_t *)(smem + a.off_bar);
     int4 *s_info = (int4 *)(smem + a.off_bar + 16);
     const int tid = threadIdx.x;
     const int ncta = (int)gridDim.x - 1;  // the last CTA plans
-    wait_for_previous_grid();
     if ((int)blockIdx.x == ncta) {
         if (plan_next && tid == 0) plan_step(a.run, a.snap_t, a.hy, &a.ctrl[slot ^ 1], false, 0.0f, FL_PHASE_ALL);
-        allow_next_grid();
         return;
     }
     const StepCtrl s = a.ctrl[slot];
-    allow_next_grid();
     if (!s.active) return;
     const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
     float4 *__restrict__ out = s.parity ? a.state0 : a.state1;
@@ -280,14 +277,19 @@ __global__ void __launch_bounds__(TILE, 3) k_surface(const __grid_constant__ Sur
             }
             out[c] = make_float4(hn, hun, hvn, st.w);
             // requested inlet capture / surcharge of this cell's inlets, from the
-            // depth the drainage step starts with
+            // depth the drainage step starts with, and the cell's capture limit
+            // factor: its volume over the summed capture requests (reference
+            // :52-177)
             const uint32_t kc = __float_as_uint(ci.w);
             if (kc && drain_finishes && a.has_inlets) {
                 const InletReqView &v = a.inl;
+                float sum = 0.0f;
                 for (int q = v.kcell_start[kc - 1]; q < v.kcell_start[kc]; ++q) {
-                    const int nn = v.in_node[q];
-                    v.req[q] = inlet_request(v, q, hn, ff_clamp0(v.Va[nn]), v.node_area[nn], dt);
+                    const float2 r = inlet_request(v, q, hn, ff_clamp0(v.Va[v.in_node[q]]), dt);
+                    v.req[q] = r;
+                    sum += r.x;
                 }
+                v.capf[kc - 1] = fmin32(1.0f, (fmax32(hn, 0.0f) * ci.x) / fmax32(sum, 1.0e-12f));
             }
             const bool final_here = !(drain_finishes && (info & CELL_COUPLED));
             if (KIND == 1 && do_surface && final_here) a.wet[c] = wt + dt * (float)(hn > md);
@@ -321,7 +323,6 @@ template __global__ void k_surface<1>(const __grid_constant__ SurfArgs, int, int
 
 // Global CFL minimum over all cells; the last block plans the step.
 __global__ void __launch_bounds__(256) k_dt(const __grid_constant__ DtArgs a, int slot, int plan) {
-    wait_for_previous_grid();
     const float4 *__restrict__ st = a.run->parity ? a.state1 : a.state0;
     float best = CUDART_INF_F;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.C; c += gridDim.x * blockDim.x) {
@@ -430,6 +431,20 @@ __global__ void k_ff_to_f64(const float2 *src, double *dst, int32_t n) {
     }
 }
 
+__global__ void k_f64_to_ff_perm(const double *src, float2 *dst, const int32_t *perm, int32_t n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double v = src[perm[i]];
+        const float hi = (float)v;
+        dst[i] = make_float2(hi, (float)(v - (double)hi));
+    }
+}
+
+__global__ void k_ff_to_f64_perm(const float2 *src, double *dst, const int32_t *perm, int32_t n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        dst[perm[i]] = (double)src[i].x + (double)src[i].y;
+    }
+}
+
 __global__ void k_f64_to_f32(const double *src, float *dst, int32_t n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = (float)src[i];
 }
@@ -463,35 +478,11 @@ __global__ void k_volumes(const float4 *state0, const float4 *state1, const floa
 // Host launch wrappers (C++ linkage, used by fl_solver.cpp).
 namespace fl {
 
-static cudaError_t launch_pdl(const void *func, dim3 grid, dim3 block, void **args, cudaStream_t stream) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelExC(&cfg, func, args);
-}
-
 cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, int grid, int smem_bytes,
                            cudaStream_t stream) {
-    void *args[] = {(void *)&a, (void *)&slot, (void *)&plan_next};
-    const void *fn = kind ? (const void *)k_surface<1> : (const void *)k_surface<0>;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(TILE);
-    cfg.dynamicSmemBytes = (size_t)smem_bytes;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelExC(&cfg, fn, args);
+    if (kind) k_surface<1><<<grid, TILE, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
+    else k_surface<0><<<grid, TILE, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
+    return cudaGetLastError();
 }
 
 // The persistent grid of k_surface: as many compute CTAs as fit (never more
@@ -518,8 +509,8 @@ cudaError_t plan_surface_launch(SurfArgs &a, int kind, int device, int *grid, in
 int surface_warps(int grid) { return grid * (TILE / 32); }
 
 cudaError_t launch_dt(const DtArgs &a, int blocks, int slot, int plan, cudaStream_t stream) {
-    void *args[] = {(void *)&a, (void *)&slot, (void *)&plan};
-    return launch_pdl((const void *)k_dt, dim3(blocks), dim3(256), args, stream);
+    k_dt<<<blocks, 256, 0, stream>>>(a, slot, plan);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_replan(RunCtrl *run, double *snap_t, HyetoView hy, StepCtrl *ctrl, int slot, cudaStream_t stream) {
@@ -557,6 +548,16 @@ cudaError_t launch_f64_to_ff(const double *src, float2 *dst, int32_t n, cudaStre
 
 cudaError_t launch_ff_to_f64(const float2 *src, double *dst, int32_t n, cudaStream_t stream) {
     k_ff_to_f64<<<304, 256, 0, stream>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_f64_to_ff_perm(const double *src, float2 *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
+    k_f64_to_ff_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ff_to_f64_perm(const float2 *src, double *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
+    k_ff_to_f64_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
     return cudaGetLastError();
 }
 
