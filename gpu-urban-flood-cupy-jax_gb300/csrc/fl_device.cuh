@@ -116,6 +116,115 @@ __device__ __forceinline__ float2 ff_clamp0(float2 a) {
     return (a.x + a.y < 0.0f) ? make_float2(0.0f, 0.0f) : a;
 }
 
+// --------------------------------------------------------------- tile steps
+// Phase 2 of a surface tile: one edge entry {nx, ny, len, bits} over the
+// staged states st[] (own cells, then halo), written into the per-(cell, slot)
+// places of s_flux; boundary in/outflow volume of exterior entries goes to
+// led_in / led_out.
+__device__ __forceinline__ void tile_entry(const float4 en, const float4 *st, float4 *s_flux, float g, float half_g,
+                                           float md, float stage, float dt, float &led_in, float &led_out) {
+    const uint32_t f = __float_as_uint(en.w);
+    const uint32_t li = f & EB_IDX_MASK, ri = (f >> EB_RIGHT_SHIFT) & EB_IDX_MASK;
+    const bool ai = (f & EB_AI) != 0;
+    const int code = (int)(f >> EB_CODE_SHIFT) - 1;
+    float4 Ls = st[li];
+    if (!(f & EB_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
+    const float4 Rs = ai ? st[ri] : ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, en.x, en.y, code, stage);
+    EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, en.x, en.y, g, half_g, md);
+    const float len = en.z;
+    if (f & EB_LPRESENT) {
+        if (!(f & EB_INTERIOR) && code == 4 && fl.h < 0.0f) {
+            fl.h = 0.0f; fl.huL = 0.0f; fl.hvL = 0.0f;
+        }
+        s_flux[li * 3 + ((f >> EB_LSLOT_SHIFT) & 3u)] = make_float4((-fl.h) * len, (-fl.huL) * len, (-fl.hvL) * len, 0.0f);
+        if (!ai) {
+            const float b = fl.h * len * dt;
+            led_in += fmax32(-b, 0.0f);
+            led_out += fmax32(b, 0.0f);
+        }
+    }
+    if (f & EB_RPRESENT)
+        s_flux[ri * 3 + ((f >> EB_RSLOT_SHIFT) & 3u)] = make_float4(fl.h * len, fl.huR * len, fl.hvR * len, 0.0f);
+}
+
+// Phase 3 of a surface tile for one active cell: the sum of its slot
+// contributions in the reference's scatter order (left-side slots, then
+// right-side ones), the update with semi-implicit Manning damping, rainfall,
+// infiltration, momentum rescale and dry zeroing.  rd / id: the cell's rain
+// and infiltration depth of the step.
+struct CellNew {
+    float h, hu, hv, rd, id;
+};
+
+__device__ __forceinline__ CellNew cell_update(const float4 st, const float4 ci, const float4 *slots, float dt, float dtg,
+                                              float md, float rain, float infil) {
+    const uint32_t info = __float_as_uint(ci.z);
+    float L0 = 0.0f, L1 = 0.0f, L2 = 0.0f, R0 = 0.0f, R1 = 0.0f, R2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float4 v = slots[k];
+        if (info & (1u << (CELL_RIGHT_SHIFT + k))) {
+            R0 = R0 + v.x; R1 = R1 + v.y; R2 = R2 + v.z;
+        } else {
+            L0 = L0 + v.x; L1 = L1 + v.y; L2 = L2 + v.z;
+        }
+    }
+    const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
+    const float ia = rcp(ci.x);
+    float hn = fmax32(st.x + dt * d0 * ia, 0.0f);
+    float hun = st.y + dt * d1 * ia;
+    float hvn = st.z + dt * d2 * ia;
+    // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
+    const bool wet = hn > md;
+    const float hs = fmax32(hn, md);
+    const float ih = rcp(hs);
+    const float uu = hun * ih, vv = hvn * ih;
+    const float speed = fsqrt(uu * uu + vv * vv);
+    const float n = ci.y;
+    const float h43 = __expf(1.3333334f * __logf(hs));
+    const float damping = 1.0f + dtg * (n * n) * speed * rcp(h43);
+    const float idamp = rcp(damping);
+    hun = wet ? hun * idamp : 0.0f;
+    hvn = wet ? hvn * idamp : 0.0f;
+    // rainfall, infiltration, momentum rescale, dry zeroing
+    const float rd = fmax32(rain, 0.0f) * dt;
+    const float h1 = hn + rd;
+    const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
+    const float h2 = h1 - id;
+    const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
+    const bool wet2 = h2 > md;
+    CellNew r;
+    r.h = h2;
+    r.hu = wet2 ? hun * scale : 0.0f;
+    r.hv = wet2 ? hvn * scale : 0.0f;
+    r.rd = rd;
+    r.id = id;
+    return r;
+}
+
+// Velocity clamp (solver/stabilizers.py:8-27), rounded exactly as the
+// reference computes it.  When |q|^2 < 0.9999 (vmax max(h, 1e-8))^2 the exact
+// speed is below vmax, the exact scale is 1 and the momenta are unchanged.
+__device__ __forceinline__ void clamp_velocity_exact(float h, float &hu, float &hv, float vmax) {
+    const float hm = fmax32(h, 1.0e-8f);
+    const float lim = vmax * hm;
+    if (!(hu * hu + hv * hv < 0.9999f * (lim * lim))) {
+        const float speed = xdiv(xsqrt(xadd(xmul(hu, hu), xmul(hv, hv))), hm);
+        const float scale = fmin32(1.0f, xdiv(vmax, fmax32(speed, 1.0e-12f)));
+        hu = xmul(hu, scale);
+        hv = xmul(hv, scale);
+    }
+}
+
+// CFL local timestep of one cell (equations.py:155-178), correctly rounded
+// and uncontracted: the reference's float32 expression bit-for-bit.
+__device__ __forceinline__ float cfl_local(float h, float hu, float hv, float char_len, float cfl, float g, float md) {
+    const float hs = fmax32(h, md);
+    const float u = xdiv(hu, hs), w = xdiv(hv, hs);
+    const float speed = xadd(xsqrt(xadd(xmul(u, u), xmul(w, w))), xsqrt(xmul(g, hs)));
+    return xdiv(xmul(cfl, char_len), fmax32(speed, 1.0e-12f));
+}
+
 // --------------------------------------------------------------- inlets
 // Requested capture and surcharge volume of inlet i for one step (reference
 // inlet_exchange_request_kernel, triangular_inlet_exchange_cuda_kernels.py:52-131).

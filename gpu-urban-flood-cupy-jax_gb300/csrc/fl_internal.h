@@ -36,7 +36,6 @@ constexpr uint32_t EB_LACTIVE = 1u << 26;  // left cell active
 constexpr uint32_t EB_AI = 1u << 27;       // active interior edge
 constexpr uint32_t EB_INTERIOR = 1u << 28; // the edge has a right cell
 constexpr int EB_CODE_SHIFT = 29;          // bits 29-31: effective boundary code + 1
-constexpr int MAX_HALO = 3 * TILE;         // local indices stay below 1024
 // tile_info[t] = {first entry, entry count, first halo index (multiple of 4), halo count}
 constexpr int64_t MAX_CELLS = 0x7FFFFFFE;
 
@@ -229,6 +228,7 @@ struct NetArgs {
 // Host-side renumbered layout (fl_plan.cpp).
 struct HostLayout {
     int32_t C = 0, E = 0, N = 0, L = 0, I = 0, K = 0, G = 0;
+    int32_t tile = TILE;              // cells per tile (multiple of 32, at most TILE)
     std::vector<int32_t> perm;        // perm[new] = reference cell
     std::vector<int32_t> inv;         // inv[reference] = new
     int32_t Cp = 0;                   // C rounded up to whole tiles

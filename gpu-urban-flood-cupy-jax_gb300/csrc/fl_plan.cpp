@@ -48,17 +48,18 @@ float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); 
 // copies and indexes: every entry's local indices inside its tile's own cells
 // plus halo, every halo cell a real cell, every copy 16-byte sized.
 static int validate_tiles(const HostLayout &L) {
+    const int64_t TL = L.tile, MAXH = 3 * L.tile;
     const int64_t tiles = (int64_t)L.tile_info.size();
     for (int64_t t = 0; t < tiles; ++t) {
         const int4 ti = L.tile_info[t];
-        const int64_t own = std::min<int64_t>(TILE, (int64_t)L.C - t * TILE);
+        const int64_t own = std::min<int64_t>(TL, (int64_t)L.C - t * TL);
         if (ti.x < 0 || ti.y < 0 || (int64_t)ti.x + ti.y > (int64_t)L.ent.size() || ti.y > L.e_cap ||
-            ti.z < 0 || ti.z % 4 != 0 || ti.w < 0 || ti.w > MAX_HALO || (int64_t)ti.z + ((ti.w + 3) & ~3) > (int64_t)L.halo_src.size() ||
+            ti.z < 0 || ti.z % 4 != 0 || ti.w < 0 || ti.w > MAXH || (int64_t)ti.z + ((ti.w + 3) & ~3) > (int64_t)L.halo_src.size() ||
             ((ti.w + 3) & ~3) > L.h_cap)
             return set_error(FL_E_INVALID, "internal: tile %lld table out of range", (long long)t);
         for (int32_t j = 0; j < ti.w; ++j) {
             const int32_t g = L.halo_src[ti.z + j];
-            if (g < 0 || g >= L.C || (g >= t * TILE && g < t * TILE + own))
+            if (g < 0 || g >= L.C || (g >= t * TL && g < t * TL + own))
                 return set_error(FL_E_INVALID, "internal: tile %lld halo cell %d out of range", (long long)t, g);
         }
         for (int32_t j = 0; j < ti.y; ++j) {
@@ -66,8 +67,8 @@ static int validate_tiles(const HostLayout &L) {
             memcpy(&bits, &L.ent[ti.x + j].w, 4);
             const uint32_t li = bits & EB_IDX_MASK, ri = (bits >> EB_RIGHT_SHIFT) & EB_IDX_MASK;
             const bool lin = li < (uint32_t)own, rin = ri < (uint32_t)own;
-            const bool lok = lin || (li >= (uint32_t)TILE && li < (uint32_t)(TILE + ti.w));
-            const bool rok = !(bits & EB_AI) || rin || (ri >= (uint32_t)TILE && ri < (uint32_t)(TILE + ti.w));
+            const bool lok = lin || (li >= (uint32_t)TL && li < (uint32_t)(TL + ti.w));
+            const bool rok = !(bits & EB_AI) || rin || (ri >= (uint32_t)TL && ri < (uint32_t)(TL + ti.w));
             const uint32_t ls = (bits >> EB_LSLOT_SHIFT) & 3u, rs = (bits >> EB_RSLOT_SHIFT) & 3u;
             if (!lok || !rok || ((bits & EB_LPRESENT) && (!lin || ls > 2u)) ||
                 ((bits & EB_RPRESENT) && (!(bits & EB_AI) || !rin || rs > 2u)))
@@ -190,8 +191,10 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
     }
 
     // tile entry lists and halos
-    const int64_t tiles = (C + TILE - 1) / TILE;
-    L.Cp = (int32_t)(tiles * TILE);
+    const int64_t TL = L.tile, MAXH = 3 * L.tile;
+    if (TL < 32 || TL > TILE || TL % 32 != 0) return set_error(FL_E_INVALID, "tile size %lld is not a multiple of 32 in [32, %d]", (long long)TL, TILE);
+    const int64_t tiles = (C + TL - 1) / TL;
+    L.Cp = (int32_t)(tiles * TL);
     {
         uint32_t none = 0;
         float fz;
@@ -210,7 +213,7 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
     std::vector<uint32_t> ent_bits;
     std::vector<int32_t> halo;
     for (int64_t t = 0; t < tiles; ++t) {
-        const int64_t c0 = t * TILE, c1 = std::min<int64_t>(C, c0 + TILE);
+        const int64_t c0 = t * TL, c1 = std::min<int64_t>(C, c0 + TL);
         const size_t first = L.ent.size();
         ent_left.clear();
         ent_right.clear();
@@ -259,11 +262,11 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
         }
         std::sort(halo.begin(), halo.end());
         halo.erase(std::unique(halo.begin(), halo.end()), halo.end());
-        if ((int64_t)halo.size() > MAX_HALO)
-            return set_error(FL_E_INVALID, "tile %lld reads %zu outside cells (limit %d)", (long long)t, halo.size(), MAX_HALO);
+        if ((int64_t)halo.size() > MAXH)
+            return set_error(FL_E_INVALID, "tile %lld reads %zu outside cells (limit %lld)", (long long)t, halo.size(), (long long)MAXH);
         auto local = [&](int32_t g) -> uint32_t {
             if (g >= c0 && g < c1) return (uint32_t)(g - c0);
-            return (uint32_t)(TILE + (std::lower_bound(halo.begin(), halo.end(), g) - halo.begin()));
+            return (uint32_t)(TL + (std::lower_bound(halo.begin(), halo.end(), g) - halo.begin()));
         };
         for (size_t j = 0; j < ent_bits.size(); ++j) {
             uint32_t bits = ent_bits[j] | local(ent_left[j]);

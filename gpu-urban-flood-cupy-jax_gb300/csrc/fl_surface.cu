@@ -153,32 +153,8 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
         if (do_surface) {
             const int n_e = s_info[st_i].y;
 #pragma unroll 1
-            for (int e = tid; e < n_e; e += TILE) {
-                const float4 en = S.en[e];
-                const uint32_t f = __float_as_uint(en.w);
-                const uint32_t li = f & EB_IDX_MASK, ri = (f >> EB_RIGHT_SHIFT) & EB_IDX_MASK;
-                const bool ai = (f & EB_AI) != 0;
-                const int code = (int)(f >> EB_CODE_SHIFT) - 1;
-                float4 Ls = S.st[li];
-                if (!(f & EB_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
-                const float4 Rs = ai ? S.st[ri] : ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, en.x, en.y, code, a.stage);
-                EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, en.x, en.y, a.g, a.half_g, md);
-                const float len = en.z;
-                if (f & EB_LPRESENT) {
-                    if (!(f & EB_INTERIOR) && code == 4 && fl.h < 0.0f) {
-                        fl.h = 0.0f; fl.huL = 0.0f; fl.hvL = 0.0f;
-                    }
-                    s_flux[li * 3 + ((f >> EB_LSLOT_SHIFT) & 3u)] = make_float4((-fl.h) * len, (-fl.huL) * len,
-                                                                                (-fl.hvL) * len, 0.0f);
-                    if (!ai) {
-                        const float b = fl.h * len * dt;
-                        led[2] += fmax32(-b, 0.0f);
-                        led[3] += fmax32(b, 0.0f);
-                    }
-                }
-                if (f & EB_RPRESENT)
-                    s_flux[ri * 3 + ((f >> EB_RSLOT_SHIFT) & 3u)] = make_float4(fl.h * len, fl.huR * len, fl.hvR * len, 0.0f);
-            }
+            for (int e = tid; e < n_e; e += TILE)
+                tile_entry(S.en[e], S.st, s_flux, a.g, a.half_g, md, a.stage, dt, led[2], led[3]);
         }
         // the next tile's copies: wait for them here (they had all of phase 2)
         // and start its halo gathers, which then overlap phase 3
@@ -210,71 +186,16 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
             if (!do_surface) {
                 hn = st.x; hun = st.y; hvn = st.z;
             } else if (info & CELL_ACTIVE) {
-                // the reference's scatter order: left-side contributions, then right-side ones
-                float L0 = 0.0f, L1 = 0.0f, L2 = 0.0f, R0 = 0.0f, R1 = 0.0f, R2 = 0.0f;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const float4 v = s_flux[tid * 3 + k];
-                    if (info & (1u << (CELL_RIGHT_SHIFT + k))) {
-                        R0 = R0 + v.x; R1 = R1 + v.y; R2 = R2 + v.z;
-                    } else {
-                        L0 = L0 + v.x; L1 = L1 + v.y; L2 = L2 + v.z;
-                    }
-                }
-                const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
-                const float area = ci.x;
-                const float ia = rcp(area);
-                hn = fmax32(st.x + dt * d0 * ia, 0.0f);
-                hun = st.y + dt * d1 * ia;
-                hvn = st.z + dt * d2 * ia;
-                // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
-                const bool wet = hn > md;
-                const float hs = fmax32(hn, md);
-                const float ih = rcp(hs);
-                const float uu = hun * ih, vv = hvn * ih;
-                const float speed = fsqrt(uu * uu + vv * vv);
-                const float n = ci.y;
-                const float h43 = __expf(1.3333334f * __logf(hs));
-                const float damping = 1.0f + s.dtg_f * (n * n) * speed * rcp(h43);
-                const float idamp = rcp(damping);
-                hun = wet ? hun * idamp : 0.0f;
-                hvn = wet ? hvn * idamp : 0.0f;
-                // rainfall, infiltration, momentum rescale, dry zeroing
-                float rain, infil;
-                if (KIND == 1) {
-                    rain = s.rain_f * hz.w;
-                    infil = hz.y + (hz.x - hz.y) * __expf(-hz.z * wt);
-                } else {
-                    rain = s.rain_f;
-                    infil = a.infil_scalar;
-                }
-                const float rd = fmax32(rain, 0.0f) * dt;
-                const float h1 = hn + rd;
-                const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
-                const float h2 = h1 - id;
-                const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
-                const bool wet2 = h2 > md;
-                hn = h2;
-                hun = wet2 ? hun * scale : 0.0f;
-                hvn = wet2 ? hvn * scale : 0.0f;
-                led[0] += rd * area;
-                led[1] += id * area;
+                const float rain = KIND == 1 ? s.rain_f * hz.w : s.rain_f;
+                const float infil = KIND == 1 ? hz.y + (hz.x - hz.y) * __expf(-hz.z * wt) : a.infil_scalar;
+                const CellNew u = cell_update(st, ci, &s_flux[tid * 3], dt, s.dtg_f, md, rain, infil);
+                hn = u.h; hun = u.hu; hvn = u.hv;
+                led[0] += u.rd * ci.x;
+                led[1] += u.id * ci.x;
             }
 #pragma unroll
             for (int k = 0; k < 3; ++k) s_flux[tid * 3 + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (s.phases & FL_PHASE_CLAMP) {
-                // velocity clamp, rounded exactly as the reference computes it.  When
-                // |q|^2 < 0.9999 (vmax max(h, 1e-8))^2 the exact speed is below vmax,
-                // the exact scale is 1 and the momenta are unchanged: skip it.
-                const float hm = fmax32(hn, 1.0e-8f);
-                const float lim = a.vmax * hm;
-                if (!(hun * hun + hvn * hvn < 0.9999f * (lim * lim))) {
-                    const float speed = xdiv(xsqrt(xadd(xmul(hun, hun), xmul(hvn, hvn))), hm);
-                    const float scale = fmin32(1.0f, xdiv(a.vmax, fmax32(speed, 1.0e-12f)));
-                    hun = xmul(hun, scale);
-                    hvn = xmul(hvn, scale);
-                }
-            }
+            if (s.phases & FL_PHASE_CLAMP) clamp_velocity_exact(hn, hun, hvn, a.vmax);
             out[c] = make_float4(hn, hun, hvn, st.w);
             // requested inlet capture / surcharge of this cell's inlets, from the
             // depth the drainage step starts with, and the cell's capture limit
@@ -326,12 +247,8 @@ __global__ void __launch_bounds__(256) k_dt(const __grid_constant__ DtArgs a, in
     const float4 *__restrict__ st = a.run->parity ? a.state1 : a.state0;
     float best = CUDART_INF_F;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.C; c += gridDim.x * blockDim.x) {
-        // rounded exactly as the reference's float32 expression
         const float4 v = st[c];
-        const float hs = fmax32(v.x, a.md);
-        const float u = xdiv(v.y, hs), w = xdiv(v.z, hs);
-        const float speed = xadd(xsqrt(xadd(xmul(u, u), xmul(w, w))), xsqrt(xmul(a.g, hs)));
-        const float local = xdiv(xmul(a.cfl, a.char_len[c]), fmax32(speed, 1.0e-12f));
+        const float local = cfl_local(v.x, v.y, v.z, a.char_len[c], a.cfl, a.g, a.md);
         if (isfinite(local) && local < best) best = local;
     }
 #pragma unroll
