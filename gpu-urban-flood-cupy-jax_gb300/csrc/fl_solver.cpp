@@ -32,6 +32,8 @@ int set_error(int code, const char *fmt, ...) {
     return code;
 }
 
+void add_launches(int64_t n) { g_launches += n; }
+
 int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L);
 int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L);
 int surface_smem_layout(SurfArgs &a, int kind);

@@ -108,6 +108,11 @@ class FlProgress(C.Structure):
     ]
 
 
+class FlBatchShape(C.Structure):
+    _fields_ = [("tile_cells", C.c_int32), ("ctas_per_sm", C.c_int32), ("chunk_steps", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 _lib = None
 
 # symbol -> (restype, argtypes)
@@ -135,6 +140,20 @@ _SIGNATURES = {
     "fl_plan_tiles": (C.c_int, [C.POINTER(FlMeshDesc), C.POINTER(C.c_int64)]),
     "fl_time_kernel": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, f64p]),
     "fl_launch_count": (C.c_int64, []),
+    "fl_batch_create": (C.c_int, [C.c_int32, C.POINTER(FlMeshDesc), C.POINTER(FlForcingDesc), C.POINTER(FlParams),
+                                  C.POINTER(FlBatchShape), C.c_int32, C.POINTER(C.c_void_p)]),
+    "fl_batch_destroy": (None, [C.c_void_p]),
+    "fl_batch_set_state": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                     C.c_void_p]),
+    "fl_batch_run": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
+    "fl_batch_progress": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(FlProgress), C.c_void_p]),
+    "fl_batch_get_state": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                     C.c_void_p]),
+    "fl_batch_get_snapshots": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_int32, C.c_void_p]),
+    "fl_batch_read_ledger": (C.c_int, [C.c_void_p, C.c_int32, f64p, C.c_int32, C.c_void_p]),
+    "fl_batch_info": (C.c_int, [C.c_void_p, C.POINTER(FlBatchShape), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                i32p]),
     "fl_stable_timestep_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
                                              C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
 }

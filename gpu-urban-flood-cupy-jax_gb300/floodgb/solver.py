@@ -43,6 +43,92 @@ class Progress:
     last_dt_s: float
 
 
+@dataclass
+class Descriptors:
+    """The C-ABI descriptors of one scenario and the host arrays they point into."""
+
+    mesh: N.FlMeshDesc
+    drain: N.FlDrainDesc | None
+    forcing: N.FlForcingDesc
+    params: N.FlParams
+    keep: N.Keep
+    duration_s: float
+    max_snapshots: int
+    kind: int
+
+
+def build_descriptors(surface_topology, coupling_topology=None, pipe_topology=None, *, rainfall=None,
+                      infiltration_fields=None, infiltration_mps: float = 0.0, cfg: RunConfig | None = None,
+                      duration_s: float | None = None, centroids=None, boundary_stage_m: float | None = None,
+                      max_snapshots: int | None = None, gravity_mps2: float = 9.80665,
+                      min_depth_m: float = 1.0e-5) -> Descriptors:
+    """Mesh / drainage / forcing / parameter descriptors of one scenario."""
+
+    cfg = cfg or load_config()
+    s = cfg.solver
+    ph = cfg.physics
+    if duration_s is None:
+        if s.duration_min is not None:
+            duration_s = float(s.duration_min) * 60.0
+        elif rainfall is not None:
+            duration_s = float(rainfall.duration_min) * 60.0
+        else:
+            raise ValueError("duration_s, solver.duration_min or a rainfall event is needed")
+    duration_s = float(duration_s)
+    if surface_topology.has_stage_boundary and boundary_stage_m is None:
+        raise ValueError("dirichlet_stage triangular boundary requires boundary_stage_m.")
+    keep = N.Keep()
+    mesh = N.mesh_desc(surface_topology, keep, centroids, boundary_stage_m)
+    drain = None
+    if coupling_topology is not None and coupling_topology.node_count > 0:
+        drain = N.drain_desc(coupling_topology, pipe_topology, keep, ph.inlet_capture_rule,
+                             ph.inlet_orifice_area_m2, ph.inlet_orifice_coefficient,
+                             ph.inlet_weir_perimeter_m, ph.inlet_weir_coefficient)
+    if rainfall is not None:
+        hs, he, hr = hyetograph_arrays(rainfall)
+    else:
+        hs = he = hr = np.zeros(0)
+    kind = 1 if infiltration_fields is not None else 0
+    forcing = N.FlForcingDesc(
+        kind=kind,
+        rain_multiplier=keep.f32(infiltration_fields.rainfall_multiplier if kind else None),
+        horton_f0_mps=keep.f32(infiltration_fields.horton_f0_mps if kind else None),
+        horton_fc_mps=keep.f32(infiltration_fields.horton_fc_mps if kind else None),
+        horton_k_per_s=keep.f32(infiltration_fields.horton_k_per_s if kind else None),
+        infiltration_mps=float(np.float32(infiltration_mps)),
+        hyetograph_count=int(np.asarray(hs).size),
+        hyeto_start_s=keep.f64(hs), hyeto_end_s=keep.f64(he), hyeto_rate_mps=keep.f64(hr),
+    )
+    if max_snapshots is None:
+        max_snapshots = int(math.ceil(duration_s / (s.snapshot_interval_min * 60.0))) + 2
+    params = N.FlParams(
+        gravity_mps2=gravity_mps2, min_depth_m=min_depth_m, cfl=s.cfl,
+        cfl_update_interval_steps=int(s.cfl_update_interval_steps),
+        cfl_reuse_safety_factor=s.cfl_reuse_safety_factor, max_dt_s=s.max_dt_s, max_speed_mps=s.max_speed_mps,
+        finite_check_interval_steps=int(s.finite_check_interval_steps), duration_s=duration_s,
+        snapshot_interval_s=s.snapshot_interval_min * 60.0, max_snapshots=int(max_snapshots),
+    )
+    return Descriptors(mesh, drain, forcing, params, keep, duration_s, int(max_snapshots), kind)
+
+
+def city_infiltration(city, cfg: RunConfig):
+    """(per-cell Horton fields or None, scalar capacity) the engine derives for a city."""
+
+    ph = cfg.physics
+    fields = city.infiltration_fields if ph.infiltration_mode == "production_horton" else None
+    simple = city.simple_infiltration_mps if ph.infiltration_mode != "production_horton" else None
+    if fields is None and simple is not None and np.ndim(simple) > 0:
+        # per-cell constant capacity: Horton with f0 = fc = capacity, k = 0, unit rain multiplier
+        from .domain import ProductionInfiltrationFields
+
+        f = np.asarray(simple, np.float32)
+        fields = ProductionInfiltrationFields(
+            rainfall_multiplier=np.ones_like(f), horton_f0_mps=f, horton_fc_mps=f,
+            horton_k_per_s=np.zeros_like(f), open_fraction=np.ones_like(f), active_mask=np.ones(f.shape, bool))
+        simple = None
+    return fields, float(simple) if simple is not None else 0.0
+
+
 class FloodSolver:
     """Device solver for one city (surface mesh, optional drainage, forcing)."""
 
@@ -66,59 +152,20 @@ class FloodSolver:
     ):
         lib = N.load()
         cfg = cfg or load_config()
-        s = cfg.solver
-        ph = cfg.physics
-        if duration_s is None:
-            if s.duration_min is not None:
-                duration_s = float(s.duration_min) * 60.0
-            elif rainfall is not None:
-                duration_s = float(rainfall.duration_min) * 60.0
-            else:
-                raise ValueError("duration_s, solver.duration_min or a rainfall event is needed")
+        d = build_descriptors(surface_topology, coupling_topology, pipe_topology, rainfall=rainfall,
+                              infiltration_fields=infiltration_fields, infiltration_mps=infiltration_mps, cfg=cfg,
+                              duration_s=duration_s, centroids=centroids, boundary_stage_m=boundary_stage_m,
+                              max_snapshots=max_snapshots, gravity_mps2=gravity_mps2, min_depth_m=min_depth_m)
         self.cfg = cfg
-        self.duration_s = float(duration_s)
+        self.duration_s = d.duration_s
         self.cell_count = surface_topology.cell_count
         self.node_count = coupling_topology.node_count if coupling_topology is not None else 0
         self.link_count = pipe_topology.link_count if pipe_topology is not None else 0
-        if surface_topology.has_stage_boundary and boundary_stage_m is None:
-            raise ValueError("dirichlet_stage triangular boundary requires boundary_stage_m.")
-        keep = N.Keep()
-        self._keep = keep
-        mesh = N.mesh_desc(surface_topology, keep, centroids, boundary_stage_m)
-        drain = None
-        if coupling_topology is not None and coupling_topology.node_count > 0:
-            drain = N.drain_desc(coupling_topology, pipe_topology, keep, ph.inlet_capture_rule,
-                                 ph.inlet_orifice_area_m2, ph.inlet_orifice_coefficient,
-                                 ph.inlet_weir_perimeter_m, ph.inlet_weir_coefficient)
-        if rainfall is not None:
-            hs, he, hr = hyetograph_arrays(rainfall)
-        else:
-            hs = he = hr = np.zeros(0)
-        kind = 1 if infiltration_fields is not None else 0
-        forcing = N.FlForcingDesc(
-            kind=kind,
-            rain_multiplier=keep.f32(infiltration_fields.rainfall_multiplier if kind else None),
-            horton_f0_mps=keep.f32(infiltration_fields.horton_f0_mps if kind else None),
-            horton_fc_mps=keep.f32(infiltration_fields.horton_fc_mps if kind else None),
-            horton_k_per_s=keep.f32(infiltration_fields.horton_k_per_s if kind else None),
-            infiltration_mps=float(np.float32(infiltration_mps)),
-            hyetograph_count=int(np.asarray(hs).size),
-            hyeto_start_s=keep.f64(hs), hyeto_end_s=keep.f64(he), hyeto_rate_mps=keep.f64(hr),
-        )
-        self.kind = kind
-        if max_snapshots is None:
-            max_snapshots = int(math.ceil(self.duration_s / (s.snapshot_interval_min * 60.0))) + 2
-        params = N.FlParams(
-            gravity_mps2=gravity_mps2, min_depth_m=min_depth_m, cfl=s.cfl,
-            cfl_update_interval_steps=int(s.cfl_update_interval_steps),
-            cfl_reuse_safety_factor=s.cfl_reuse_safety_factor, max_dt_s=s.max_dt_s, max_speed_mps=s.max_speed_mps,
-            finite_check_interval_steps=int(s.finite_check_interval_steps), duration_s=self.duration_s,
-            snapshot_interval_s=s.snapshot_interval_min * 60.0, max_snapshots=int(max_snapshots),
-        )
-        self.max_snapshots = int(max_snapshots)
+        self.kind = d.kind
+        self.max_snapshots = d.max_snapshots
         handle = C.c_void_p()
-        rc = lib.fl_create(C.byref(mesh), C.byref(drain) if drain is not None else None, C.byref(forcing),
-                           C.byref(params), int(device), C.byref(handle))
+        rc = lib.fl_create(C.byref(d.mesh), C.byref(d.drain) if d.drain is not None else None, C.byref(d.forcing),
+                           C.byref(d.params), int(device), C.byref(handle))
         N.check(rc, "fl_create")
         self._h = handle
         self._lib = lib
@@ -260,21 +307,10 @@ def solver_for_city(city, rainfall, cfg: RunConfig, duration_s: float | None = N
     """FloodSolver for a CityDomain, with the forcing the engine would derive."""
 
     topo = city.topologies
-    ph = cfg.physics
-    fields = city.infiltration_fields if ph.infiltration_mode == "production_horton" else None
-    simple = city.simple_infiltration_mps if ph.infiltration_mode != "production_horton" else None
-    if fields is None and simple is not None and np.ndim(simple) > 0:
-        # per-cell constant capacity: Horton with f0 = fc = capacity, k = 0, unit rain multiplier
-        from .domain import ProductionInfiltrationFields
-
-        f = np.asarray(simple, np.float32)
-        fields = ProductionInfiltrationFields(
-            rainfall_multiplier=np.ones_like(f), horton_f0_mps=f, horton_fc_mps=f,
-            horton_k_per_s=np.zeros_like(f), open_fraction=np.ones_like(f), active_mask=np.ones(f.shape, bool))
-        simple = None
+    fields, simple = city_infiltration(city, cfg)
     s = FloodSolver(
         topo.surface_topology, topo.coupling_topology, topo.pipe_topology, rainfall=rainfall,
-        infiltration_fields=fields, infiltration_mps=float(simple) if simple is not None else 0.0, cfg=cfg,
+        infiltration_fields=fields, infiltration_mps=simple, cfg=cfg,
         duration_s=duration_s, centroids=city.mesh.centroids_xy, device=device, max_snapshots=max_snapshots,
     )
     s.set_state(topo.surface_state.h_m, topo.surface_state.hu_m2ps, topo.surface_state.hv_m2ps,

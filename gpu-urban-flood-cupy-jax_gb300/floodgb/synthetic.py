@@ -28,8 +28,9 @@ from pathlib import Path
 
 import numpy as np
 
+from .config import load_config
 from .domain import MMHR_TO_MPS, CityDomain, ProductionInfiltrationFields, ProductionTopologies, RealMesh, empty_drainage
-from .rainfall import RainfallEvent, hourly_rainfall, uniform_rainfall
+from .rainfall import RainfallEvent, hourly_rainfall, rainfall_event, uniform_rainfall
 from .topology import (
     TriangularNodeCouplingTopology,
     TriangularPipeNetworkState,
@@ -480,3 +481,48 @@ def production_workload(seed: int = 1, cache: bool = True) -> Scenario:
     except OSError:
         pass
     return sc
+
+
+# ---------------------------------------------------------------------------
+# batched ensemble: ragged meshes, seeded storms
+# ---------------------------------------------------------------------------
+ENSEMBLE_GRID_N = (71, 158, 224, 354)  # 10,082 / 49,928 / 100,352 / 250,632 triangles
+
+
+def storm_hyetograph(rng: np.random.Generator, peak_range=(20.0, 120.0), duration_h_range=(1.0, 6.0),
+                     block_min: float = 10.0) -> RainfallEvent:
+    """Seeded single-peak storm: triangular intensity in 10-minute blocks,
+    peak U(20, 120) mm/h at a random 20-50 % of a U(1, 6) h duration."""
+
+    peak = float(rng.uniform(*peak_range))
+    dur_min = float(np.round(rng.uniform(*duration_h_range) * 60.0 / block_min) * block_min)
+    dur_min = max(dur_min, block_min)
+    t_peak = float(rng.uniform(0.2, 0.5)) * dur_min
+    start = np.arange(0.0, dur_min, block_min)
+    mid = start + 0.5 * block_min
+    rise = np.clip(mid / max(t_peak, 1e-9), 0.0, 1.0)
+    fall = np.clip((dur_min - mid) / max(dur_min - t_peak, 1e-9), 0.0, 1.0)
+    inten = peak * np.where(mid <= t_peak, rise, fall)
+    return rainfall_event(start, start + block_min, np.round(inten, 3))
+
+
+def ensemble_workload(seed: int = 2, grid_n=ENSEMBLE_GRID_N, per_size: int = 16, size_m: float = 1000.0,
+                      duration_cap_h: float | None = None) -> list:
+    """Batched-ensemble members (mesh size cycles through grid_n, per_size each):
+    jittered-grid cities like the 20,000-triangle case with their own seeded
+    random-field beds and seeded storms; each runs for its storm's duration
+    (capped at duration_cap_h when given)."""
+
+    from .batch import Member
+
+    rng = np.random.default_rng(seed)
+    members = []
+    for n in grid_n:
+        for k in range(per_size):
+            mseed = int(rng.integers(1 << 30))
+            storm = storm_hyetograph(np.random.default_rng(mseed + 7))
+            dur_min = storm.duration_min if duration_cap_h is None else min(storm.duration_min, duration_cap_h * 60.0)
+            sc = make_grid_city(n=n, size_m=size_m, seed=mseed, hyetograph=storm, duration_min=dur_min)
+            cfg = load_config(None, sc.overrides)
+            members.append(Member(sc.city, sc.rainfall, cfg, dur_min * 60.0))
+    return members

@@ -240,6 +240,50 @@ FL_API int fl_stable_timestep_noalloc(const float *char_len, const float *h, con
                                       int32_t n, double cfl, double gravity_mps2, double min_depth_m,
                                       double *dt_out, void *stream);
 
+/* ------------------------------------------------------------------ batch
+ * Batched ensemble (no counterpart in the reference, which runs one scenario
+ * per process): n surface-only scenarios -- meshes of any sizes, each with
+ * its own forcing, hyetograph, duration and adaptive dt -- advanced together
+ * by one persistent surface launch per step over all active scenarios' tiles
+ * and one planning launch, captured in CUDA graphs.  Each scenario follows
+ * exactly the single-instance step of fl_run (same fluxes, dt rule, clamp,
+ * snapshot rule and ledger).  Besides the hourly depth snapshots, each
+ * snapshot also stores the per-cell maximum depth since the previous one.
+ * The surface kernel's tile size and CTAs per SM come from FlBatchShape
+ * (floodgb.autotune picks them by timing). */
+typedef struct FlBatch FlBatch;
+
+typedef struct {
+    int32_t tile_cells;   /* cells per tile: 128 or 256 (0: 256) */
+    int32_t ctas_per_sm;  /* persistent CTAs per SM (0: as many as fit) */
+    int32_t chunk_steps;  /* steps per CUDA-graph chunk (0: 32) */
+    int32_t reserved;
+} FlBatchShape;
+
+/* meshes/forcings/params: n entries each (no drainage; every mesh's stage
+ * boundary, if any, must use the same stage; at most 256 scenarios). */
+FL_API int fl_batch_create(int32_t n, const FlMeshDesc *meshes, const FlForcingDesc *forcings,
+                           const FlParams *params, const FlBatchShape *shape, int32_t device, FlBatch **out);
+FL_API void fl_batch_destroy(FlBatch *batch);
+/* Initial state of one scenario (reference cell order); default: dry. */
+FL_API int fl_batch_set_state(FlBatch *batch, int32_t scen, const float *h, const float *hu, const float *hv,
+                              int32_t mem, void *stream);
+/* Run every scenario from t = 0 to its own duration (or until max_steps
+ * lockstep steps, if > 0); restarts from the state last set. */
+FL_API int fl_batch_run(FlBatch *batch, int64_t max_steps, void *stream);
+FL_API int fl_batch_progress(FlBatch *batch, int32_t scen, FlProgress *out, void *stream);
+FL_API int fl_batch_get_state(FlBatch *batch, int32_t scen, float *h, float *hu, float *hv, int32_t mem,
+                              void *stream);
+/* Snapshots [first, first+count) of depth and of the maximum depth since the
+ * previous snapshot (count x cells each, reference order); times in s. */
+FL_API int fl_batch_get_snapshots(FlBatch *batch, int32_t scen, int32_t first, int32_t count, double *times_s,
+                                  float *h, float *hmax, int32_t mem, void *stream);
+/* Cumulative ledger of one scenario (FL_LEDGER_RAINFALL..BOUNDARY_OUT and
+ * FL_LEDGER_SURFACE_VOLUME are filled). */
+FL_API int fl_batch_read_ledger(FlBatch *batch, int32_t scen, double *out, int32_t n, void *stream);
+/* Shape in use, total cells (padded), tiles, and the persistent grid. */
+FL_API int fl_batch_info(FlBatch *batch, FlBatchShape *shape, int64_t *cells, int64_t *tiles, int32_t *grid);
+
 /* Number of kernel launches the library has issued in this process. */
 FL_API int64_t fl_launch_count(void);
 
