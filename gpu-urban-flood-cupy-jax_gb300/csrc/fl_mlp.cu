@@ -1,0 +1,380 @@
+// Dense layers of the learned surrogate on the 5th-generation tensor cores.
+//
+// k_gemm_bf16: C[M, N] = act(A[M, K] . B[N, K]^T + bias[N]) (+ residual), A and
+// B bf16, accumulation in fp32 in tensor memory (TMEM).  One CTA (4 warps)
+// computes a 128 x 128 tile of C:
+//   * A and B are staged in shared memory in 64-wide K chunks (128-byte rows)
+//     in the canonical K-major 128-byte-swizzle layout, four stages deep, by
+//     16-byte cp.async -- each A row of a chunk may come from a different
+//     source row ("gathered" A: the concatenated [receiver, sender, edge]
+//     input of a message MLP is never materialised);
+//   * one elected thread issues tcgen05.mma (kind::f16, M = 128, N = 128,
+//     K = 16 per instruction, four per chunk) and tcgen05.commit to the
+//     stage's mbarrier, which frees the stage for the next chunk's copies;
+//   * the epilogue reads the accumulator with tcgen05.ld (each warp its 32
+//     TMEM lanes = 32 rows), adds bias / ReLU / residual and stores fp32
+//     and/or bf16.
+// K is split into up to three segments {base, row index, leading dimension,
+// width}; a segment's chunk for output row r reads base + idx[r] * ld.
+// A grid z-dimension splits K (chunks) for the weight-gradient products,
+// each split writing its own fp32 partial tile.
+//
+// Every mbarrier wait is bounded in time; a wait that gives up records an
+// error flag, drains the outstanding MMAs (bounded again), frees TMEM and
+// returns.
+#include <cuda_bf16.h>
+
+#include "fl_device.cuh"
+
+namespace fl {
+
+constexpr int MM_BM = 128, MM_BN = 128, MM_BK = 64, MM_STAGES = 4, MM_THREADS = 128;
+constexpr int MM_CHUNK_BYTES = MM_BM * MM_BK * 2;  // 16 KB per operand per stage
+constexpr uint64_t MM_WAIT_NS = 1000000000ull;
+
+struct GemmSeg {
+    const __nv_bfloat16 *base;
+    const int32_t *idx;  // row map (nullptr: identity)
+    int64_t ld;          // elements between rows
+    int32_t width;       // K elements of this segment (multiple of 64)
+};
+
+struct GemmArgs {
+    GemmSeg a[3];
+    int32_t n_seg;
+    int32_t M, N, K;                 // K = sum of segment widths
+    const __nv_bfloat16 *b;          // [N, ldb] rows = output features, K contiguous
+    int64_t ldb;
+    const float *bias;               // [N] or nullptr
+    const float *residual;           // [M, ldr] fp32 or nullptr
+    int64_t ldr;
+    float *out_f32;                  // [M, ldo] or nullptr (split z writes out_f32 + z * M * ldo)
+    __nv_bfloat16 *out_bf16;         // [M, ldo] or nullptr
+    int64_t ldo;
+    int32_t relu;
+    int32_t k_chunks_per_split;      // chunks per z slice
+    int32_t *error;                  // set to FL_E_TIMEOUT if a wait gave up
+};
+
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address (16-byte units)
+    d |= (uint64_t)1 << 16;                    // leading byte offset (unused by swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                    // descriptor version
+    d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: fp32 accumulator, bf16 A and B, both
+// K-major, M = 128, N = 128.
+__device__ __forceinline__ uint32_t umma_idesc_bf16_128x128() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(MM_BN >> 3) << 17) | ((uint32_t)(MM_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "setp.ne.u32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Copy one 64-wide chunk (128 rows x 128 B) into the swizzled stage layout:
+// 16-byte piece c of row R lands at R * 128 + ((c ^ (R & 7)) * 16).
+__device__ __forceinline__ void load_chunk_a(const GemmArgs &g, int m0, int chunk, uint32_t sdst) {
+    int seg = 0, kin = chunk * MM_BK;
+    while (seg + 1 < g.n_seg && kin >= g.a[seg].width) {
+        kin -= g.a[seg].width;
+        ++seg;
+    }
+    const GemmSeg s = g.a[seg];
+    for (int p = threadIdx.x; p < MM_BM * 8; p += MM_THREADS) {
+        const int R = p >> 3, c = p & 7;
+        const uint32_t dst = sdst + (uint32_t)(R * 128 + ((c ^ (R & 7)) << 4));
+        const int r = m0 + R;
+        if (r < g.M) {
+            const int64_t row = s.idx ? (int64_t)s.idx[r] : (int64_t)r;
+            cp_async16(dst, s.base + row * s.ld + kin + c * 8);
+        } else {
+            asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(dst), "r"(0u) : "memory");
+        }
+    }
+}
+
+__device__ __forceinline__ void load_chunk_b(const GemmArgs &g, int n0, int chunk, uint32_t sdst) {
+    for (int p = threadIdx.x; p < MM_BN * 8; p += MM_THREADS) {
+        const int R = p >> 3, c = p & 7;
+        const uint32_t dst = sdst + (uint32_t)(R * 128 + ((c ^ (R & 7)) << 4));
+        const int n = n0 + R;
+        if (n < g.N) cp_async16(dst, g.b + (int64_t)n * g.ldb + chunk * MM_BK + c * 8);
+        else asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(dst), "r"(0u) : "memory");
+    }
+}
+
+__global__ void __launch_bounds__(MM_THREADS, 1) k_gemm_bf16(const __grid_constant__ GemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned stages: A0..A3, B0..B3, then barriers and the TMEM address
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA = smem_addr(smem), sB = sA + MM_STAGES * MM_CHUNK_BYTES;
+    uint64_t *bars = (uint64_t *)(smem + 2 * MM_STAGES * MM_CHUNK_BYTES);
+    uint32_t *tmem_slot = (uint32_t *)(bars + MM_STAGES);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * MM_BM, n0 = blockIdx.y * MM_BN;
+    const int total_chunks = g.K / MM_BK;
+    const int c_begin = blockIdx.z * g.k_chunks_per_split;
+    const int c_end = min(total_chunks, c_begin + g.k_chunks_per_split);
+    const int nk = c_end - c_begin;
+
+    if (tid == 0) {
+        for (int s = 0; s < MM_STAGES; ++s) mbar_init(smem_addr(&bars[s]), 1);
+        mbar_fence_init();
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(128u));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = umma_idesc_bf16_128x128();
+    bool bad = false;
+    uint32_t issued_mask = 0u;  // stages with an MMA batch not yet waited for (thread 0)
+    uint32_t par = 0u;          // bit s: parity of the next wait on stage s
+
+    // prologue: chunks 0 .. STAGES-2
+    for (int j = 0; j < MM_STAGES - 1; ++j) {
+        if (j < nk) {
+            load_chunk_a(g, m0, c_begin + j, sA + j * MM_CHUNK_BYTES);
+            load_chunk_b(g, n0, c_begin + j, sB + j * MM_CHUNK_BYTES);
+        }
+        cp_async_commit();
+    }
+    for (int kc = 0; kc < nk; ++kc) {
+        // refill the stage of chunk kc + STAGES - 1 once its previous MMAs are done
+        const int j = kc + MM_STAGES - 1;
+        const int sj = j % MM_STAGES;
+        if (j < nk) {
+            if (j >= MM_STAGES) {
+                if (!mbar_wait_bounded(smem_addr(&bars[sj]), (par >> sj) & 1u, MM_WAIT_NS)) bad = true;
+                par ^= 1u << sj;
+                issued_mask &= ~(1u << sj);
+            }
+            if (!bad) {
+                load_chunk_a(g, m0, c_begin + j, sA + sj * MM_CHUNK_BYTES);
+                load_chunk_b(g, n0, c_begin + j, sB + sj * MM_CHUNK_BYTES);
+            }
+        }
+        cp_async_commit();
+        asm volatile("cp.async.wait_group %0;" ::"n"(MM_STAGES - 1) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // copies -> tensor-core reads
+        if (__syncthreads_or(bad)) break;
+        const int s = kc % MM_STAGES;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = sA + s * MM_CHUNK_BYTES, b0 = sB + s * MM_CHUNK_BYTES;
+#pragma unroll
+            for (int k = 0; k < MM_BK / 16; ++k)
+                umma_bf16(tmem, umma_desc_sw128(a0 + k * 32), umma_desc_sw128(b0 + k * 32), idesc,
+                          (kc > 0 || k > 0) ? 1u : 0u);
+            umma_commit(smem_addr(&bars[s]));
+        }
+        issued_mask |= 1u << s;
+    }
+    cp_async_wait_all();
+    // the accumulator is complete when every stage's last batch is done
+    if (!bad) {
+        for (int s = 0; s < MM_STAGES; ++s) {
+            if (issued_mask & (1u << s)) {
+                if (!mbar_wait_bounded(smem_addr(&bars[s]), (par >> s) & 1u, MM_WAIT_NS)) bad = true;
+                par ^= 1u << s;
+                issued_mask &= ~(1u << s);
+            }
+        }
+    }
+    if (__syncthreads_or(bad)) {
+        if (tid == 0) {
+            atomicCAS(g.error, 0, FL_E_TIMEOUT);
+            for (int s = 0; s < MM_STAGES; ++s)
+                if (issued_mask & (1u << s)) (void)mbar_wait_bounded(smem_addr(&bars[s]), (par >> s) & 1u, MM_WAIT_NS);
+        }
+        __syncthreads();
+    } else if (nk > 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int r = m0 + warp * 32 + (tid & 31);
+        float *of = g.out_f32 ? g.out_f32 + (size_t)blockIdx.z * (size_t)g.M * (size_t)g.ldo : nullptr;
+#pragma unroll 1
+        for (int cb = 0; cb < MM_BN; cb += 32) {
+            uint32_t v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+            if (r < g.M) {
+                const int nb = n0 + cb;
+#pragma unroll
+                for (int q = 0; q < 32; q += 8) {
+                    if (nb + q >= g.N) break;
+                    float x[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        float y = __uint_as_float(v[q + u]);
+                        if (g.bias) y += g.bias[nb + q + u];
+                        if (g.relu) y = fmaxf(y, 0.0f);
+                        if (g.residual) y += g.residual[(int64_t)r * g.ldr + nb + q + u];
+                        x[u] = y;
+                    }
+                    if (of) {
+                        float4 *p = (float4 *)(of + (int64_t)r * g.ldo + nb + q);
+                        p[0] = make_float4(x[0], x[1], x[2], x[3]);
+                        p[1] = make_float4(x[4], x[5], x[6], x[7]);
+                    }
+                    if (g.out_bf16) {
+                        uint4 w;
+                        __nv_bfloat162 h0 = __floats2bfloat162_rn(x[0], x[1]), h1 = __floats2bfloat162_rn(x[2], x[3]);
+                        __nv_bfloat162 h2 = __floats2bfloat162_rn(x[4], x[5]), h3 = __floats2bfloat162_rn(x[6], x[7]);
+                        w.x = *(uint32_t *)&h0;
+                        w.y = *(uint32_t *)&h1;
+                        w.z = *(uint32_t *)&h2;
+                        w.w = *(uint32_t *)&h3;
+                        *(uint4 *)(g.out_bf16 + (int64_t)r * g.ldo + nb + q) = w;
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u));
+}
+
+constexpr int MM_SMEM_BYTES = 2 * MM_STAGES * MM_CHUNK_BYTES + 1024 + 128;
+
+cudaError_t launch_gemm_bf16(const GemmArgs &g, int splits, cudaStream_t stream) {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, MM_SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    dim3 grid((g.M + MM_BM - 1) / MM_BM, (g.N + MM_BN - 1) / MM_BN, splits);
+    k_gemm_bf16<<<grid, MM_THREADS, MM_SMEM_BYTES, stream>>>(g);
+    return cudaGetLastError();
+}
+
+}  // namespace fl
+
+// ------------------------------------------------------------------ C ABI
+#include <mutex>
+
+namespace fl {
+
+int set_error(int code, const char *fmt, ...);
+void add_launches(int64_t n);
+
+// Per-device error flag of the GEMM kernel's bounded waits.
+static int gemm_error_flag(int32_t **out) {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mu;
+    static int32_t *flag[MAX_DEVICES] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES)
+        return set_error(FL_E_NO_DEVICE, "no usable CUDA device");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!flag[dev]) {
+        cudaError_t e = cudaMalloc(&flag[dev], sizeof(int32_t));
+        if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc: %s", cudaGetErrorString(e));
+        e = cudaMemset(flag[dev], 0, sizeof(int32_t));
+        if (e != cudaSuccess) return set_error(FL_E_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
+    }
+    *out = flag[dev];
+    return FL_OK;
+}
+
+}  // namespace fl
+
+extern "C" FL_API int fl_gemm_bf16(const FlGemmDesc *d, void *stream) {
+    using namespace fl;
+    if (!d) return set_error(FL_E_INVALID, "fl_gemm_bf16: NULL descriptor");
+    if (d->m < 1 || d->n < 1 || d->n_seg < 1 || d->n_seg > 3 || !d->b)
+        return set_error(FL_E_INVALID, "fl_gemm_bf16: bad sizes or NULL B");
+    if (!d->out_f32 && !d->out_bf16) return set_error(FL_E_INVALID, "fl_gemm_bf16: no output");
+    if (d->ldb % 8 || (d->out_f32 || d->out_bf16 ? d->ldo % 8 : 0) || d->ldo < d->n || (d->residual && d->ldr < d->n))
+        return set_error(FL_E_INVALID, "fl_gemm_bf16: leading dimensions must be multiples of 8 and cover n");
+    if (d->n % 8) return set_error(FL_E_INVALID, "fl_gemm_bf16: n must be a multiple of 8");
+    GemmArgs g{};
+    int32_t K = 0;
+    for (int s = 0; s < d->n_seg; ++s) {
+        const FlGemmSegment &a = d->a[s];
+        if (!a.base || a.width < 64 || a.width % 64 || a.ld % 8 || a.ld < a.width)
+            return set_error(FL_E_INVALID, "fl_gemm_bf16: segment %d needs a base, a width that is a multiple of 64 "
+                                           "and a leading dimension that is a multiple of 8", s);
+        g.a[s].base = (const __nv_bfloat16 *)a.base;
+        g.a[s].idx = a.rows;
+        g.a[s].ld = a.ld;
+        g.a[s].width = a.width;
+        K += a.width;
+    }
+    if (d->ldb < K) return set_error(FL_E_INVALID, "fl_gemm_bf16: ldb %lld < K %d", (long long)d->ldb, K);
+    const int chunks = K / MM_BK;
+    const int splits = d->k_splits > 1 ? d->k_splits : 1;
+    if (splits > 1 && (d->out_bf16 || d->bias || d->residual || d->relu || !d->out_f32))
+        return set_error(FL_E_INVALID, "fl_gemm_bf16: split-K writes plain fp32 partials only");
+    const int per = (chunks + splits - 1) / splits;
+    if ((splits - 1) * per >= chunks) return set_error(FL_E_INVALID, "fl_gemm_bf16: more K splits than chunks");
+    g.n_seg = d->n_seg;
+    g.M = d->m;
+    g.N = d->n;
+    g.K = K;
+    g.b = (const __nv_bfloat16 *)d->b;
+    g.ldb = d->ldb;
+    g.bias = d->bias;
+    g.residual = d->residual;
+    g.ldr = d->ldr;
+    g.out_f32 = d->out_f32;
+    g.out_bf16 = (__nv_bfloat16 *)d->out_bf16;
+    g.ldo = d->ldo;
+    g.relu = d->relu;
+    g.k_chunks_per_split = per;
+    int rc = gemm_error_flag(&g.error);
+    if (rc) return rc;
+    cudaError_t e = launch_gemm_bf16(g, splits, (cudaStream_t)stream);
+    if (e != cudaSuccess) return set_error(FL_E_CUDA, "k_gemm_bf16 launch: %s", cudaGetErrorString(e));
+    add_launches(1);
+    return FL_OK;
+}
+
+extern "C" FL_API int fl_gemm_status(void *stream) {
+    using namespace fl;
+    int32_t *flag = nullptr;
+    int rc = gemm_error_flag(&flag);
+    if (rc) return rc;
+    int32_t v = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(&v, flag, sizeof(v), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return set_error(FL_E_CUDA, "fl_gemm_status: %s", cudaGetErrorString(e));
+    if (v) {
+        cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
+        return set_error(v, "a tensor-core GEMM wait gave up (device error %d)", v);
+    }
+    return FL_OK;
+}

@@ -113,6 +113,19 @@ class FlBatchShape(C.Structure):
                 ("reserved", C.c_int32)]
 
 
+class FlGemmSegment(C.Structure):
+    _fields_ = [("base", C.c_void_p), ("rows", C.c_void_p), ("ld", C.c_int64), ("width", C.c_int32)]
+
+
+class FlGemmDesc(C.Structure):
+    _fields_ = [
+        ("a", FlGemmSegment * 3), ("n_seg", C.c_int32), ("m", C.c_int32), ("n", C.c_int32),
+        ("b", C.c_void_p), ("ldb", C.c_int64), ("bias", C.c_void_p), ("residual", C.c_void_p), ("ldr", C.c_int64),
+        ("out_f32", C.c_void_p), ("out_bf16", C.c_void_p), ("ldo", C.c_int64), ("relu", C.c_int32),
+        ("k_splits", C.c_int32),
+    ]
+
+
 _lib = None
 
 # symbol -> (restype, argtypes)
@@ -140,6 +153,8 @@ _SIGNATURES = {
     "fl_plan_tiles": (C.c_int, [C.POINTER(FlMeshDesc), C.POINTER(C.c_int64)]),
     "fl_time_kernel": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, f64p]),
     "fl_launch_count": (C.c_int64, []),
+    "fl_gemm_bf16": (C.c_int, [C.POINTER(FlGemmDesc), C.c_void_p]),
+    "fl_gemm_status": (C.c_int, [C.c_void_p]),
     "fl_batch_create": (C.c_int, [C.c_int32, C.POINTER(FlMeshDesc), C.POINTER(FlForcingDesc), C.POINTER(FlParams),
                                   C.POINTER(FlBatchShape), C.c_int32, C.POINTER(C.c_void_p)]),
     "fl_batch_destroy": (None, [C.c_void_p]),

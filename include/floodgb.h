@@ -284,6 +284,43 @@ FL_API int fl_batch_read_ledger(FlBatch *batch, int32_t scen, double *out, int32
 /* Shape in use, total cells (padded), tiles, and the persistent grid. */
 FL_API int fl_batch_info(FlBatch *batch, FlBatchShape *shape, int64_t *cells, int64_t *tiles, int32_t *grid);
 
+/* ------------------------------------------------------------ surrogate
+ * Dense layers of the learned surrogate (no counterpart in the reference,
+ * whose AI code is not shipped): C[m, n] = act(A[m, K] . B[n, K]^T + bias)
+ * (+ residual) on the tensor cores, bf16 operands, fp32 accumulation.  A is
+ * the concatenation along K of up to three bf16 segments; row r of segment s
+ * is base_s + rows_s[r] * ld_s (rows_s NULL: row r), so gathered inputs need
+ * no copy.  Widths are multiples of 64; leading dimensions multiples of 8.
+ * k_splits > 1 splits K into that many slices, each writing a plain fp32
+ * partial [m, ldo] tile at out_f32 + slice * m * ldo. */
+typedef struct {
+    const void *base;     /* bf16 */
+    const int32_t *rows;  /* row map or NULL */
+    int64_t ld;
+    int32_t width;
+} FlGemmSegment;
+
+typedef struct {
+    FlGemmSegment a[3];
+    int32_t n_seg;
+    int32_t m, n;
+    const void *b;        /* bf16 [n, ldb], K contiguous */
+    int64_t ldb;
+    const float *bias;    /* [n] or NULL */
+    const float *residual; /* fp32 [m, ldr] or NULL */
+    int64_t ldr;
+    float *out_f32;       /* [m, ldo] or NULL */
+    void *out_bf16;       /* bf16 [m, ldo] or NULL */
+    int64_t ldo;
+    int32_t relu;
+    int32_t k_splits;
+} FlGemmDesc;
+
+FL_API int fl_gemm_bf16(const FlGemmDesc *desc, void *stream);
+/* Synchronises `stream`; FL_E_TIMEOUT if a GEMM's device wait gave up since
+ * the last call (the flag is then cleared). */
+FL_API int fl_gemm_status(void *stream);
+
 /* Number of kernel launches the library has issued in this process. */
 FL_API int64_t fl_launch_count(void);
 
