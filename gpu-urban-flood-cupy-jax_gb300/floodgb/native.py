@@ -155,6 +155,17 @@ _SIGNATURES = {
     "fl_launch_count": (C.c_int64, []),
     "fl_gemm_bf16": (C.c_int, [C.POINTER(FlGemmDesc), C.c_void_p]),
     "fl_gemm_status": (C.c_int, [C.c_void_p]),
+    "fl_transpose_bf16": (C.c_int, [C.POINTER(FlGemmSegment), C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                    C.c_void_p]),
+    "fl_segment_sum": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                 C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
+    "fl_relu_bwd": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p,
+                              C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]),
+    "fl_colsum": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                            C.c_void_p]),
+    "fl_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float,
+                          C.c_float, C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "fl_cast_bf16": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]),
     "fl_batch_create": (C.c_int, [C.c_int32, C.POINTER(FlMeshDesc), C.POINTER(FlForcingDesc), C.POINTER(FlParams),
                                   C.POINTER(FlBatchShape), C.c_int32, C.POINTER(C.c_void_p)]),
     "fl_batch_destroy": (None, [C.c_void_p]),

@@ -70,3 +70,50 @@ def gemm(segments, b, *, bias=None, residual=None, out_f32=None, out_bf16=None, 
 
 def status():
     N.check(N.load().fl_gemm_status(_stream()), "fl_gemm_status")
+
+
+def _seg_array(segments):
+    arr = (N.FlGemmSegment * 3)()
+    for i, (t, rows, width) in enumerate(segments):
+        arr[i] = N.FlGemmSegment(C.c_void_p(t.data_ptr()), _ptr(rows), t.stride(0), int(width))
+    return arr
+
+
+def transpose(segments, m, dst):
+    """dst[k, r] = cat_k(segments)[r, k]; dst columns m.. zeroed."""
+
+    N.check(N.load().fl_transpose_bf16(_seg_array(segments), len(segments), int(m), C.c_void_p(dst.data_ptr()),
+                                       dst.stride(0), _stream()), "fl_transpose_bf16")
+
+
+def segment_sum(src, col0, start, order, n_out, width, dst, dst_bf16=None, accumulate=False):
+    N.check(N.load().fl_segment_sum(C.c_void_p(src.data_ptr()), src.stride(0), int(col0), C.c_void_p(start.data_ptr()),
+                                    _ptr(order), int(n_out), int(width), C.c_void_p(dst.data_ptr()), dst.stride(0),
+                                    _ptr(dst_bf16), dst_bf16.stride(0) if dst_bf16 is not None else 0,
+                                    int(bool(accumulate)), _stream()), "fl_segment_sum")
+
+
+def relu_bwd(dx, z, out_bf16, out_f32=None):
+    m, n = dx.shape[0], out_bf16.shape[1]
+    N.check(N.load().fl_relu_bwd(C.c_void_p(dx.data_ptr()), dx.stride(0), _ptr(z), z.stride(0) if z is not None else 0,
+                                 int(m), int(n), C.c_void_p(out_bf16.data_ptr()), out_bf16.stride(0), _ptr(out_f32),
+                                 out_f32.stride(0) if out_f32 is not None else 0, _stream()), "fl_relu_bwd")
+
+
+def colsum(x, m, n, scratch, out, accumulate=False):
+    N.check(N.load().fl_colsum(C.c_void_p(x.data_ptr()), x.stride(0), int(m), int(n), C.c_void_p(scratch.data_ptr()),
+                               C.c_void_p(out.data_ptr()), int(bool(accumulate)), _stream()), "fl_colsum")
+
+
+def adam(w, m1, m2, g, lr, step, b1=0.9, b2=0.999, eps=1e-8, weight_decay=0.0, w_bf16=None, wt_bf16=None):
+    rows, cols = w.shape
+    N.check(N.load().fl_adam(C.c_void_p(w.data_ptr()), C.c_void_p(m1.data_ptr()), C.c_void_p(m2.data_ptr()),
+                             C.c_void_p(g.data_ptr()), int(rows), int(cols), float(lr), float(b1), float(b2),
+                             float(eps), int(step), float(weight_decay), _ptr(w_bf16), _ptr(wt_bf16),
+                             wt_bf16.stride(0) if wt_bf16 is not None else 0, _stream()), "fl_adam")
+
+
+def cast_bf16(src, dst):
+    m, n = dst.shape
+    N.check(N.load().fl_cast_bf16(C.c_void_p(src.data_ptr()), src.stride(0), int(m), int(n),
+                                  C.c_void_p(dst.data_ptr()), dst.stride(0), _stream()), "fl_cast_bf16")

@@ -321,6 +321,31 @@ FL_API int fl_gemm_bf16(const FlGemmDesc *desc, void *stream);
  * the last call (the flag is then cleared). */
 FL_API int fl_gemm_status(void *stream);
 
+/* Memory-bound companions of fl_gemm_bf16 for message passing and training
+ * (fixed-order sums: reproducible).
+ * fl_transpose_bf16: dst[k, r] = A[r, k] for the segment concatenation A
+ *   (as fl_gemm_bf16's A), columns m..ldd-1 of dst set to 0.
+ * fl_segment_sum: dst[i, :width] (+)= sum over p in [start[i], start[i+1]) of
+ *   src[order ? order[p] : p, col0 : col0+width]; optional bf16 copy.
+ * fl_relu_bwd: out = dx * (z > 0) (z NULL: no mask), bf16 (+ fp32).
+ * fl_colsum: out[c] (+)= sum_r x[r, c]; scratch holds 256 x n floats.
+ * fl_adam: Adam step on fp32 w[rows, cols]; refreshes w_bf16 and its
+ *   transpose wt_bf16[cols, ldt] when given.
+ * fl_cast_bf16: dst = bf16(src). */
+FL_API int fl_transpose_bf16(const FlGemmSegment *segs, int32_t n_seg, int32_t m, void *dst, int64_t ldd,
+                             void *stream);
+FL_API int fl_segment_sum(const float *src, int64_t lds, int32_t col0, const int32_t *start, const int32_t *order,
+                          int32_t n_out, int32_t width, float *dst, int64_t ldd, void *dst_bf16, int64_t ldb,
+                          int32_t accumulate, void *stream);
+FL_API int fl_relu_bwd(const float *dx, int64_t ldx, const void *z_bf16, int64_t ldz, int32_t m, int32_t n,
+                       void *out_bf16, int64_t ldo, float *out_f32, int64_t ldf, void *stream);
+FL_API int fl_colsum(const float *x, int64_t ldx, int32_t m, int32_t n, float *scratch, float *out, int32_t accumulate,
+                     void *stream);
+FL_API int fl_adam(float *w, float *m1, float *m2, const float *g, int32_t rows, int32_t cols, float lr, float b1,
+                   float b2, float eps, int32_t step, float weight_decay, void *w_bf16, void *wt_bf16, int64_t ldt,
+                   void *stream);
+FL_API int fl_cast_bf16(const float *src, int64_t lds, int32_t m, int32_t n, void *dst, int64_t ldd, void *stream);
+
 /* Number of kernel launches the library has issued in this process. */
 FL_API int64_t fl_launch_count(void);
 
