@@ -48,6 +48,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-ensemble", action="store_true", help="skip the ensemble / surrogate screening measurement")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--profile", choices=["loop", "kernels"], default=None,
                    help="ncu helper: open a profiler range around 64 solver steps of a wet run (loop) or "
@@ -186,6 +187,63 @@ def reference_arm(args):
     }), flush=True)
 
 
+SURROGATE_WEIGHTS = ROOT / "gpu-urban-flood-cupy-jax_gb300" / "floodgb" / "surrogate" / "weights" / "mpnn_grid224.npz"
+
+
+def ensemble_measure(per_size: int = 4, cap_h: float = 1.0, screen_members: int = 64):
+    """Second metric, ensemble scenario-hours/s: a ragged 16-member ensemble
+    (4 each of 10,082 / 49,928 / 100,352 / 250,632-triangle meshes, seeded
+    storms, 1 h each) through the batched solver against the same members run
+    one by one by the single-instance solver; then, with the trained
+    surrogate, screening of held-out storms on its 100,352-triangle mesh
+    (rollouts + solver re-runs of flagged and audited members) against the
+    plain single-instance solver."""
+
+    import torch
+
+    from floodgb.batch import BatchSolver
+    from floodgb.solver import solver_for_city
+    from floodgb.synthetic import ensemble_workload
+
+    members = ensemble_workload(seed=2, per_size=per_size, duration_cap_h=cap_h)
+    hours = sum(m.duration_s for m in members) / 3600.0
+    shape = {"tile_cells": 256, "ctas_per_sm": 0}
+    with BatchSolver(members, shape=shape) as b:
+        b.run(max_steps=64)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        b.run()
+        torch.cuda.synchronize()
+        batched_s = time.perf_counter() - t
+        cell_steps = sum(b.progress(k).step_count * c for k, c in enumerate(b.cell_counts))
+        info = b.info()
+    seq_s = 0.0
+    for m in members:
+        s = solver_for_city(m.city, m.rainfall, m.cfg, duration_s=m.duration_s)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.run()
+        torch.cuda.synchronize()
+        seq_s += time.perf_counter() - t
+        s.close()
+    out = {
+        "metric": "scenario-h/s", "workload": f"{len(members)} members, 4 mesh sizes, seeded storms, {cap_h:g} h each",
+        "batched": hours / batched_s, "sequential_single_instance": hours / seq_s,
+        "batched_over_single": seq_s / batched_s, "batched_cell_steps_per_s": cell_steps / batched_s,
+        "batch_shape": {k: info[k] for k in ("tile_cells", "ctas_per_sm", "grid", "tiles")},
+    }
+    if SURROGATE_WEIGHTS.exists():
+        from floodgb.surrogate.experiment import screen_saved
+
+        r = screen_saved(SURROGATE_WEIGHTS, n_eval=screen_members, plain_sample=2)
+        out["surrogate_screening"] = {
+            "members": r["members"], "mesh_cells": r["mesh_cells"], "scenario_hours": r["scenario_hours"],
+            "flagged": r["flagged"], "audited": r["audited"], "accepted": r["surrogate_accepted"],
+            "throughput_scenario_h_per_s": r["throughput_scenario_h_per_s"],
+        }
+    return out
+
+
 def our_arm(args):
     import numpy as np
     import torch
@@ -314,6 +372,9 @@ def our_arm(args):
     base = None
     if world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(sc, cfg, args.cpu_seconds)
+    ensemble = None
+    if world == 1 and not args.no_ensemble:
+        ensemble = ensemble_measure()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / len(ms), "higher_is_better": True, "scaling": "weak",
@@ -339,6 +400,7 @@ def our_arm(args):
         "gpu_launches": int(launches),
         "clocks": clk,
         "cpu_baseline": base,
+        "ensemble": ensemble,
     }
     print(json.dumps(line), flush=True)
 

@@ -118,3 +118,52 @@ extern "C" FL_API int fl_stable_timestep_noalloc(const float *char_len, const fl
     if (e != cudaSuccess) return set_error(FL_E_CUDA, "k_dt_noalloc launch: %s", cudaGetErrorString(e));
     return FL_OK;
 }
+
+// ------------------------------------------------------------------ wait self-test
+namespace fl {
+
+// One warp waits on an mbarrier that nothing arrives on, with the same bounded
+// wait the surface, batch and GEMM kernels use; it must give up after
+// limit_ns and report FL_E_TIMEOUT (the context stays usable).
+__global__ void k_wait_selftest(uint64_t limit_ns, int32_t *status, uint64_t *elapsed_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = smem_addr(&bar);
+    if (threadIdx.x == 0) {
+        mbar_init(b, 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+    const uint64_t t0 = global_ns();
+    const bool ok = mbar_wait_bounded(b, 0, limit_ns);
+    const uint64_t t1 = global_ns();
+    if (threadIdx.x == 0) {
+        *status = ok ? FL_OK : FL_E_TIMEOUT;
+        *elapsed_ns = t1 - t0;
+    }
+}
+
+}  // namespace fl
+
+extern "C" FL_API int fl_wait_selftest(double limit_s, int32_t *status, double *elapsed_s) {
+    using namespace fl;
+    if (!status || !elapsed_s || !(limit_s > 0.0) || limit_s > 5.0)
+        return set_error(FL_E_INVALID, "fl_wait_selftest: limit must be in (0, 5] s");
+    int32_t *d_status = nullptr;
+    uint64_t *d_el = nullptr;
+    cudaError_t e = cudaMalloc(&d_status, sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_el, sizeof(uint64_t));
+    if (e != cudaSuccess) {
+        cudaFree(d_status);
+        return set_error(FL_E_NOMEM, "fl_wait_selftest: %s", cudaGetErrorString(e));
+    }
+    k_wait_selftest<<<1, 32>>>((uint64_t)(limit_s * 1e9), d_status, d_el);
+    uint64_t el = 0;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(status, d_status, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&el, d_el, sizeof(uint64_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_status);
+    cudaFree(d_el);
+    if (e != cudaSuccess) return set_error(FL_E_CUDA, "fl_wait_selftest: %s", cudaGetErrorString(e));
+    *elapsed_s = (double)el * 1e-9;
+    return FL_OK;
+}

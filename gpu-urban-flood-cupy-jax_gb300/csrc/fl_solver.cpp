@@ -111,6 +111,9 @@ struct FlSolver {
     NetArgs nw{};
     int32_t *node_perm = nullptr;  // node_perm[new] = reference node
     float *stage_n = nullptr;      // [N] node-order staging
+    char *drain_base = nullptr;    // the drainage arena (L2 access-policy window)
+    size_t drain_bytes = 0;
+    bool l2_persist = false;
     HyetoView hy{};
     // host
     RunCtrl *run_h = nullptr;   // pinned mirror
@@ -122,12 +125,25 @@ struct FlSolver {
     bool has_drain() const { return N > 0; }
     int launches_per_step() const { return 1 + (has_drain() ? 4 : 0); }
 
+    // Drainage tables live in one arena so one L2 access-policy window can
+    // keep them resident across the surface kernel's stream of cell data.
+    char *arena = nullptr;
+    size_t arena_size = 0, arena_used = 0;
+
     template <class T>
     int alloc(T **p, size_t count) {
         if (count == 0) count = 1;
+        const size_t bytes = sizeof(T) * count;
+        if (arena) {
+            const size_t at = (arena_used + 255) & ~(size_t)255;
+            if (at + bytes > arena_size) return set_error(FL_E_NOMEM, "internal: drainage arena too small");
+            *p = (T *)(arena + at);
+            arena_used = at + bytes;
+            return FL_OK;
+        }
         void *q = nullptr;
-        cudaError_t e = cudaMalloc(&q, sizeof(T) * count);
-        if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * count, cudaGetErrorString(e));
+        cudaError_t e = cudaMalloc(&q, bytes);
+        if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
         allocs.push_back(q);
         *p = (T *)q;
         return FL_OK;
@@ -171,6 +187,58 @@ static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStr
     return FL_OK;
 }
 
+// Keep the drainage tables in L2: a persisting set-aside for this context
+// (released with it) and an access-policy window over the drainage arena on
+// every kernel of the step graph.  Best effort: without it the loop is only
+// slower.
+static void setup_l2_persistence(FlSolver *s) {
+    if (!s->drain_base || !s->drain_bytes) return;
+    int max_persist = 0, max_window = 0;
+    if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, s->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, s->device) != cudaSuccess ||
+        max_persist <= 0 || max_window <= 0) {
+        cudaGetLastError();
+        return;
+    }
+    const size_t want = std::min(s->drain_bytes, (size_t)std::min(max_persist, max_window));
+    size_t cur = 0;
+    cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+    if (cur < want && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    s->l2_persist = true;
+}
+
+static void set_drain_window(FlSolver *s, cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return;
+    }
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    int max_window = 0;
+    cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, s->device);
+    size_t persist = 0;
+    cudaDeviceGetLimit(&persist, cudaLimitPersistingL2CacheSize);
+    cudaKernelNodeAttrValue v = {};
+    v.accessPolicyWindow.base_ptr = s->drain_base;
+    v.accessPolicyWindow.num_bytes = std::min(s->drain_bytes, (size_t)max_window);
+    v.accessPolicyWindow.hitRatio = std::min(1.0f, (float)persist / (float)std::max<size_t>(v.accessPolicyWindow.num_bytes, 1));
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+            cudaGraphKernelNodeSetAttribute(nd, cudaKernelNodeAttributeAccessPolicyWindow, &v);
+    }
+    cudaGetLastError();
+}
+
 static int capture_graph(FlSolver *s) {
     if (s->graph) return FL_OK;
     cudaGraph_t g = nullptr;
@@ -188,6 +256,7 @@ static int capture_graph(FlSolver *s) {
         return rc;
     }
     if (e != cudaSuccess) return set_error(FL_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    if (s->l2_persist) set_drain_window(s, g);
     e = cudaGraphInstantiate(&s->graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_error(FL_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
@@ -277,6 +346,7 @@ FL_API void fl_destroy(FlSolver *s) {
     for (auto &e : s->ev)
         if (e) cudaEventDestroy(e);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    if (s->l2_persist) cudaCtxResetPersistingL2Cache();
     for (void *p : s->allocs) cudaFree(p);
     if (s->run_h) cudaFreeHost(s->run_h);
     if (s->poll_h) cudaFreeHost(s->poll_h);
@@ -400,6 +470,22 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
 
     // drainage
     if (with_drain) {
+        {
+            // arena for every drainage table (256-byte aligned pieces)
+            const size_t I = (size_t)std::max(s->I, 1), N = (size_t)std::max(s->N, 1), NL = (size_t)std::max(s->NL, 1);
+            const size_t K = (size_t)std::max(s->K, 1), G = (size_t)std::max(s->G, 1), S = L.nl.size() + 1;
+            const size_t bytes = I * (4 + 8 + 16 + 8 + 8) + (K + 1) * 4 + K * 4 + (N + 1) * 4 * 2 + N * (4 + 16 + 4) +
+                                 G * 16 + S * 8 + NL * (4 * 2 + 16 * 3 + 4 * 3) + N * (8 * 2 + 4 + 4 + 4) +
+                                 (size_t)(node_blocks(s->N) * 4 * D1_TERMS + network_blocks(s->G) * 4 * D2_TERMS) * 8 +
+                                 64 * 256;
+            void *q = nullptr;
+            cudaError_t e = cudaMalloc(&q, bytes);
+            if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+            s->allocs.push_back(q);
+            s->arena = (char *)q;
+            s->arena_size = bytes;
+            s->arena_used = 0;
+        }
         int32_t *in_node, *kcell_start, *node_in_start, *nls, *lf, *lt;
         float4 *in_par, *nd0, *lk0, *lk1, *lk2;
         float *node_area, *nd_capv;
@@ -510,7 +596,11 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         b.forcing_kind = s->kind;
         b.g = (float)p.gravity_mps2;
         b.md = (float)p.min_depth_m;
+        s->drain_base = s->arena;
+        s->drain_bytes = s->arena_used;
+        s->arena = nullptr;  // later allocations are separate
     }
+    setup_l2_persistence(s);
     SurfArgs &a = s->sa;
     a.cinfo = cinfo;
     a.tile_info = tile_info;

@@ -155,6 +155,7 @@ _SIGNATURES = {
     "fl_launch_count": (C.c_int64, []),
     "fl_gemm_bf16": (C.c_int, [C.POINTER(FlGemmDesc), C.c_void_p]),
     "fl_gemm_status": (C.c_int, [C.c_void_p]),
+    "fl_wait_selftest": (C.c_int, [C.c_double, i32p, f64p]),
     "fl_transpose_bf16": (C.c_int, [C.POINTER(FlGemmSegment), C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
                                     C.c_void_p]),
     "fl_segment_sum": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,

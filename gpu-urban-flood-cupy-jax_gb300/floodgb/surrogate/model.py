@@ -89,6 +89,38 @@ class DualGraph:
         self.indeg = t(self.indeg_h, torch.float32)
         self.ef_bf = t(ef, torch.float32).to(torch.bfloat16).contiguous()
 
+    def replicate(self, copies: int) -> "DualGraph":
+        """The disjoint union of `copies` copies of this graph (cell c of copy k
+        is cell k * C + c): many members of an ensemble in one forward pass."""
+
+        import torch
+
+        g = DualGraph.__new__(DualGraph)
+        C, E, k = self.C, self.E, int(copies)
+        off_c = (np.arange(k, dtype=np.int64) * C)[:, None]
+        off_e = (np.arange(k, dtype=np.int64) * E)[:, None]
+        g.C, g.E = C * k, E * k
+        g.src_h = (self.src_h[None, :] + off_c).reshape(-1).astype(np.int32)
+        g.dst_h = (self.dst_h[None, :] + off_c).reshape(-1).astype(np.int32)
+        rs = self.recv_start.cpu().numpy().astype(np.int64)
+        ss = self.send_start.cpu().numpy().astype(np.int64)
+        so = self.send_order.cpu().numpy().astype(np.int64)
+        recv = np.concatenate([(rs[:-1][None, :] + off_e).reshape(-1), [E * k]])
+        send = np.concatenate([(ss[:-1][None, :] + off_e).reshape(-1), [E * k]])
+        order = (so[None, :] + off_e).reshape(-1)
+        g.edge_features_h = np.tile(self.edge_features_h, (k, 1))
+        g.indeg_h = np.tile(self.indeg_h, k)
+        dev = self.src.device
+        t = lambda a, dt: torch.as_tensor(a, dtype=dt, device=dev).contiguous()  # noqa: E731
+        g.src, g.dst = t(g.src_h, torch.int32), t(g.dst_h, torch.int32)
+        g.recv_start = t(recv.astype(np.int32), torch.int32)
+        g.send_order = t(order.astype(np.int32), torch.int32)
+        g.send_start = t(send.astype(np.int32), torch.int32)
+        g.row_start = t(np.arange(g.E + 1, dtype=np.int32), torch.int32)
+        g.indeg = t(g.indeg_h, torch.float32)
+        g.ef_bf = self.ef_bf.repeat(k, 1).contiguous()
+        return g
+
 
 class Dense:
     """One linear layer: fp32 master weights, bf16 copy and transpose, Adam state."""
@@ -130,26 +162,30 @@ class Dense:
 
 
 class Workspace:
-    """Activations saved by the forward pass and backward scratch for one graph size."""
+    """Activations of the forward pass for one graph size; for training also
+    every layer's saved activations and the backward scratch."""
 
-    def __init__(self, C: int, E: int, n_layers: int, device: str = "cuda"):
+    def __init__(self, C: int, E: int, n_layers: int, train: bool = True, device: str = "cuda"):
         import torch
 
         bf = lambda *s: torch.empty(*s, device=device, dtype=torch.bfloat16)  # noqa: E731
         f32 = lambda *s: torch.empty(*s, device=device, dtype=torch.float32)  # noqa: E731
-        self.C, self.E = C, E
+        self.C, self.E, self.train = C, E, train
+        keep = n_layers if train else 1  # inference reuses one set of layer buffers
         self.zn, self.ze, self.e_bf = bf(C, H), bf(E, H), bf(E, H)
-        self.h_bf = [bf(C, H) for _ in range(n_layers + 1)]
+        self.h_bf = [bf(C, H) for _ in range(n_layers + 1 if train else 2)]
         self.h_f32 = [f32(C, H), f32(C, H)]
-        self.z1e = [bf(E, H) for _ in range(n_layers)]
-        self.agg_bf = [bf(C, H) for _ in range(n_layers)]
-        self.z1n = [bf(C, H) for _ in range(n_layers)]
+        self.z1e = [bf(E, H) for _ in range(keep)]
+        self.agg_bf = [bf(C, H) for _ in range(keep)]
+        self.z1n = [bf(C, H) for _ in range(keep)]
         self.zd = bf(C, H)
         self.y = f32(C, FOUT)
         self.m_f32 = f32(E, H)
         self.agg_f32 = f32(C, H)
+        if not train:
+            return
         # backward scratch
-        self.dz_f32_e, self.dz_bf_e = f32(E, 3 * H), bf(E, H)
+        self.dz_bf_e = bf(E, H)
         self.dzf_e = f32(E, H)
         self.dcat = f32(E, 3 * H)
         self.de = f32(E, H)
@@ -182,6 +218,7 @@ class MPNN:
         self.dec[1].w.mul_(0.1)
         self.dec[1].load(self.dec[1].state())
         self.ws = None
+        self._ws = {}
         self.t = 0
 
     def layers(self):
@@ -190,16 +227,19 @@ class MPNN:
             out += list(a) + list(b)
         return out
 
-    def workspace(self, g: DualGraph) -> Workspace:
-        if self.ws is None or self.ws.C != g.C or self.ws.E != g.E:
-            self.ws = Workspace(g.C, g.E, self.n_layers, self.device)
+    def workspace(self, g: DualGraph, train: bool) -> Workspace:
+        key = (g.C, g.E, train)
+        if key not in self._ws:
+            self._ws[key] = Workspace(g.C, g.E, self.n_layers, train, self.device)
+        self.ws = self._ws[key]
         return self.ws
 
     # -------------------------------------------------------------- forward
-    def forward(self, g: DualGraph, x_bf):
-        """x_bf: bf16 [C, 64] node inputs; returns fp32 [C, 64] outputs (view into the workspace)."""
+    def forward(self, g: DualGraph, x_bf, train: bool = True):
+        """x_bf: bf16 [C, 64] node inputs; returns fp32 [C, 64] outputs (view
+        into the workspace).  train=False keeps no activations for backward."""
 
-        ws = self.workspace(g)
+        ws = self.workspace(g, train)
         C, E = g.C, g.E
         a, b = self.enc_n
         ops.gemm([(x_bf, None, FIN)], a.w_bf, bias=a.b, out_bf16=ws.zn, relu=True)
@@ -208,20 +248,22 @@ class MPNN:
         ops.gemm([(g.ef_bf, None, FIN)], a.w_bf, bias=a.b, out_bf16=ws.ze, relu=True)
         ops.gemm([(ws.ze, None, H)], b.w_bf, bias=b.b, out_bf16=ws.e_bf)
         cur = 0
+        nh = len(ws.h_bf)
         for l in range(self.n_layers):
             e1, e2 = self.edge[l]
             n1, n2 = self.node[l]
-            hb = ws.h_bf[l]
-            ops.gemm([(hb, g.dst, H), (hb, g.src, H), (ws.e_bf, None, H)], e1.w_bf, bias=e1.b, out_bf16=ws.z1e[l],
+            k = l if train else 0
+            hb = ws.h_bf[l % nh]
+            ops.gemm([(hb, g.dst, H), (hb, g.src, H), (ws.e_bf, None, H)], e1.w_bf, bias=e1.b, out_bf16=ws.z1e[k],
                      relu=True)
-            ops.gemm([(ws.z1e[l], None, H)], e2.w_bf, bias=e2.b, out_f32=ws.m_f32)
-            ops.segment_sum(ws.m_f32, 0, g.recv_start, None, C, H, ws.agg_f32, dst_bf16=ws.agg_bf[l])
-            ops.gemm([(hb, None, H), (ws.agg_bf[l], None, H)], n1.w_bf, bias=n1.b, out_bf16=ws.z1n[l], relu=True)
-            ops.gemm([(ws.z1n[l], None, H)], n2.w_bf, bias=n2.b, residual=ws.h_f32[cur], out_f32=ws.h_f32[cur ^ 1],
-                     out_bf16=ws.h_bf[l + 1])
+            ops.gemm([(ws.z1e[k], None, H)], e2.w_bf, bias=e2.b, out_f32=ws.m_f32)
+            ops.segment_sum(ws.m_f32, 0, g.recv_start, None, C, H, ws.agg_f32, dst_bf16=ws.agg_bf[k])
+            ops.gemm([(hb, None, H), (ws.agg_bf[k], None, H)], n1.w_bf, bias=n1.b, out_bf16=ws.z1n[k], relu=True)
+            ops.gemm([(ws.z1n[k], None, H)], n2.w_bf, bias=n2.b, residual=ws.h_f32[cur], out_f32=ws.h_f32[cur ^ 1],
+                     out_bf16=ws.h_bf[(l + 1) % nh])
             cur ^= 1
         a, b = self.dec
-        ops.gemm([(ws.h_bf[self.n_layers], None, H)], a.w_bf, bias=a.b, out_bf16=ws.zd, relu=True)
+        ops.gemm([(ws.h_bf[self.n_layers % nh], None, H)], a.w_bf, bias=a.b, out_bf16=ws.zd, relu=True)
         ops.gemm([(ws.zd, None, H)], b.w_bf, bias=b.b, out_f32=ws.y)
         return ws.y
 

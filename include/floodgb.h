@@ -346,6 +346,12 @@ FL_API int fl_adam(float *w, float *m1, float *m2, const float *g, int32_t rows,
                    void *stream);
 FL_API int fl_cast_bf16(const float *src, int64_t lds, int32_t m, int32_t n, void *dst, int64_t ldd, void *stream);
 
+/* Self-test of the bounded device waits (no reference counterpart): one
+ * warp waits on an mbarrier that nothing arrives on; *status receives
+ * FL_E_TIMEOUT once the wait gives up after limit_s (at most 5 s), and the
+ * device stays usable. */
+FL_API int fl_wait_selftest(double limit_s, int32_t *status, double *elapsed_s);
+
 /* Number of kernel launches the library has issued in this process. */
 FL_API int64_t fl_launch_count(void);
 

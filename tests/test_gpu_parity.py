@@ -263,3 +263,17 @@ def test_step_cap_and_resume():
     prog, (t, h, hu, hv, v), state, led = run_device(sc, cfg)
     assert prog.step_count == p.step_count
     np.testing.assert_array_equal(paused, h)
+
+
+def test_bounded_device_wait_gives_up_and_reports():
+    """A wait on an mbarrier that nothing arrives on ends after its limit with
+    FL_E_TIMEOUT, and the device keeps working afterwards."""
+
+    import ctypes as C
+
+    st, el = C.c_int32(0), C.c_double(0.0)
+    native.check(native.load().fl_wait_selftest(0.2, C.byref(st), C.byref(el)), "fl_wait_selftest")
+    assert st.value == native.FL_E_TIMEOUT
+    assert 0.19 <= el.value < 2.0
+    native.check(native.load().fl_wait_selftest(0.05, C.byref(st), C.byref(el)), "fl_wait_selftest")
+    assert st.value == native.FL_E_TIMEOUT
