@@ -24,6 +24,8 @@
 // returns.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "fl_device.cuh"
 
 namespace fl {
@@ -53,6 +55,7 @@ struct GemmArgs {
     int64_t ldo;
     int32_t relu;
     int32_t k_chunks_per_split;      // chunks per z slice
+    int32_t stages;                  // A ring depth (persistent kernel)
     int32_t *error;                  // set to FL_E_TIMEOUT if a wait gave up
 };
 
@@ -266,7 +269,274 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_gemm_bf16(const __grid_consta
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u));
 }
 
+// ---------------------------------------------------------------------------
+// k_gemm_bf16_pers: the same product for K <= 512 as a persistent,
+// warp-specialised kernel.  Each CTA keeps its 128 x K slice of B resident in
+// shared memory and walks M tiles:
+//   warps 0-1   producers: gather the A chunks of its tiles (64 rows each)
+//               into a ring of as many 16 KB stages as shared memory holds
+//               next to B (cp.async, completion tracked by the stage's
+//               mbarrier)
+//   warp 2      MMA: one lane issues tcgen05.mma per chunk into one of two
+//               TMEM accumulators and commits to the stage's "empty" and
+//               the accumulator's "full" barriers
+//   warps 3-10  epilogue: drain the other accumulator (tcgen05.ld; two
+//               warps per TMEM lane quarter, 64 columns each), release it,
+//               and store with bias / ReLU / residual
+// so loads, tensor-core work and the epilogue of consecutive tiles overlap.
+constexpr int PG_PROD_WARPS = 2, PG_EPI_WARPS = 8, PG_THREADS = 32 * (PG_PROD_WARPS + 1 + PG_EPI_WARPS);
+constexpr int PG_MAX_STAGES = 8, PG_MAX_K = 512, PG_SMEM_LIMIT = 227 * 1024;
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_arrive_noinc(uint32_t bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// Source rows of the four tile rows (lane, lane + 32, ...) a producer lane
+// copies, per segment; -1 past the end.  Loaded once per tile so the chunk
+// copies do not wait on index loads.
+struct TileRows {
+    int64_t r[3][2];
+};
+
+// Producer warp pw copies tile rows 64 * pw + lane and 64 * pw + 32 + lane.
+__device__ __forceinline__ TileRows tile_rows(const GemmArgs &g, int m0, int pw, int lane) {
+    TileRows t;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int r = m0 + 64 * pw + lane + 32 * j;
+            int64_t v = -1;
+            if (s < g.n_seg && r < g.M) v = g.a[s].idx ? (int64_t)g.a[s].idx[r] : (int64_t)r;
+            t.r[s][j] = v;
+        }
+    }
+    return t;
+}
+
+// Copy one 64-wide A chunk of a tile with the 32 threads of one warp.
+__device__ __forceinline__ void warp_load_chunk_a(const GemmArgs &g, const TileRows &tr, int chunk, uint32_t sdst,
+                                                  int pw, int lane) {
+    int seg = 0, kin = chunk * MM_BK;
+    while (seg + 1 < g.n_seg && kin >= g.a[seg].width) {
+        kin -= g.a[seg].width;
+        ++seg;
+    }
+    const GemmSeg s = g.a[seg];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int R = 64 * pw + lane + 32 * j;
+        const int64_t row = seg == 0 ? tr.r[0][j] : (seg == 1 ? tr.r[1][j] : tr.r[2][j]);
+        const uint32_t row_dst = sdst + (uint32_t)(R * 128);
+        if (row >= 0) {
+            const __nv_bfloat16 *src = s.base + row * s.ld + kin;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) cp_async16(row_dst + (uint32_t)((c ^ (R & 7)) << 4), src + c * 8);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(row_dst + (uint32_t)(c << 4)), "r"(0u)
+                             : "memory");
+        }
+    }
+}
+
+__device__ __forceinline__ void epilogue_store(const GemmArgs &g, int r, int nb, const uint32_t (&v)[32]) {
+    if (r >= g.M) return;
+#pragma unroll
+    for (int q = 0; q < 32; q += 8) {
+        if (nb + q >= g.N) break;
+        float x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            float y = __uint_as_float(v[q + u]);
+            if (g.bias) y += g.bias[nb + q + u];
+            if (g.relu) y = fmaxf(y, 0.0f);
+            if (g.residual) y += g.residual[(int64_t)r * g.ldr + nb + q + u];
+            x[u] = y;
+        }
+        if (g.out_f32) {
+            float4 *p = (float4 *)(g.out_f32 + (int64_t)r * g.ldo + nb + q);
+            p[0] = make_float4(x[0], x[1], x[2], x[3]);
+            p[1] = make_float4(x[4], x[5], x[6], x[7]);
+        }
+        if (g.out_bf16) {
+            uint4 w;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(x[0], x[1]), h1 = __floats2bfloat162_rn(x[2], x[3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(x[4], x[5]), h3 = __floats2bfloat162_rn(x[6], x[7]);
+            w.x = *(uint32_t *)&h0;
+            w.y = *(uint32_t *)&h1;
+            w.z = *(uint32_t *)&h2;
+            w.w = *(uint32_t *)&h3;
+            *(uint4 *)(g.out_bf16 + (int64_t)r * g.ldo + nb + q) = w;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(PG_THREADS, 1) k_gemm_bf16_pers(const __grid_constant__ GemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int nK = g.K / MM_BK;
+    const int S = g.stages;  // A ring depth
+    const uint32_t sB = smem_addr(smem);
+    const uint32_t sA = sB + nK * MM_CHUNK_BYTES;
+    uint64_t *bars = (uint64_t *)(smem + (nK + S) * MM_CHUNK_BYTES);
+    uint64_t *full = bars, *empty = bars + PG_MAX_STAGES, *accf = bars + 2 * PG_MAX_STAGES, *acce = accf + 2;
+    uint64_t *drain = acce + 2;
+    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n0 = blockIdx.y * MM_BN;
+    const int tiles = (g.M + MM_BM - 1) / MM_BM;
+
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(smem_addr(&full[s]), 32 * PG_PROD_WARPS);
+            mbar_init(smem_addr(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_addr(&accf[b]), 1);
+            mbar_init(smem_addr(&acce[b]), PG_EPI_WARPS);
+        }
+        mbar_init(smem_addr(drain), 1);
+        mbar_fence_init();
+    }
+    if (warp == PG_PROD_WARPS) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(256u));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    // B slice resident for the whole kernel
+    for (int c = 0; c < nK; ++c) {
+        for (int p = tid; p < MM_BN * 8; p += PG_THREADS) {
+            const int R = p >> 3, cc = p & 7;
+            const uint32_t dst = sB + (uint32_t)(c * MM_CHUNK_BYTES + R * 128 + ((cc ^ (R & 7)) << 4));
+            const int n = n0 + R;
+            if (n < g.N) cp_async16(dst, g.b + (int64_t)n * g.ldb + c * MM_BK + cc * 8);
+            else asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(dst), "r"(0u) : "memory");
+        }
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    bool bad = false;
+
+    if (warp < PG_PROD_WARPS) {
+        // producers
+        int q = 0;
+        for (int t = blockIdx.x; t < tiles && !bad; t += gridDim.x) {
+            const TileRows tr = tile_rows(g, t * MM_BM, warp, lane);
+            for (int c = 0; c < nK && !bad; ++c, ++q) {
+                const int s = q % S, u = q / S;
+                if (u > 0 && !mbar_wait_bounded(smem_addr(&empty[s]), (u - 1) & 1, MM_WAIT_NS)) {
+                    bad = true;
+                    break;
+                }
+                warp_load_chunk_a(g, tr, c, sA + s * MM_CHUNK_BYTES, warp, lane);
+                cp_async_arrive_noinc(smem_addr(&full[s]));
+            }
+        }
+        cp_async_wait_all();
+    } else if (warp == PG_PROD_WARPS) {
+        // MMA issue (one lane)
+        if (lane == 0) {
+            const uint32_t idesc = umma_idesc_bf16_128x128();
+            int q = 0, i = 0;
+            for (int t = blockIdx.x; t < tiles && !bad; t += gridDim.x, ++i) {
+                const int b = i & 1, v = i >> 1;
+                if (v > 0 && !mbar_wait_bounded(smem_addr(&acce[b]), (v - 1) & 1, MM_WAIT_NS)) {
+                    bad = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                for (int c = 0; c < nK; ++c, ++q) {
+                    const int s = q % S;
+                    if (!mbar_wait_bounded(smem_addr(&full[s]), (q / S) & 1, MM_WAIT_NS)) {
+                        bad = true;
+                        break;
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t a0 = sA + s * MM_CHUNK_BYTES, b0 = sB + c * MM_CHUNK_BYTES;
+#pragma unroll
+                    for (int k = 0; k < MM_BK / 16; ++k)
+                        umma_bf16(tmem + (uint32_t)(b * MM_BN), umma_desc_sw128(a0 + k * 32),
+                                  umma_desc_sw128(b0 + k * 32), idesc, (c > 0 || k > 0) ? 1u : 0u);
+                    umma_commit(smem_addr(&empty[s]));
+                }
+                if (bad) break;
+                umma_commit(smem_addr(&accf[b]));
+            }
+            // every MMA issued so far has completed before TMEM is released
+            umma_commit(smem_addr(drain));
+            (void)mbar_wait_bounded(smem_addr(drain), 0, MM_WAIT_NS);
+        }
+        __syncwarp();
+    } else {
+        // epilogue: warp w reads TMEM lanes 32 * (w % 4) .., columns 64 * ((w - 3) / 4) ..
+        const int quad = warp & 3, half = (warp - PG_PROD_WARPS - 1) >> 2;
+        int i = 0;
+        for (int t = blockIdx.x; t < tiles && !bad; t += gridDim.x, ++i) {
+            const int b = i & 1, v = i >> 1;
+            if (!mbar_wait_bounded(smem_addr(&accf[b]), v & 1, MM_WAIT_NS)) {
+                bad = true;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int r = t * MM_BM + quad * 32 + lane;
+            const uint32_t base = tmem + (uint32_t)(b * MM_BN + half * 64) + ((uint32_t)(quad * 32) << 16);
+            uint32_t v0[32], v1[32];
+            tmem_ld32(base, v0);
+            tmem_ld32(base + 32, v1);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_addr(&acce[b]));
+            epilogue_store(g, r, n0 + half * 64, v0);
+            epilogue_store(g, r, n0 + half * 64 + 32, v1);
+        }
+    }
+    if (bad) atomicCAS(g.error, 0, FL_E_TIMEOUT);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == PG_PROD_WARPS) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256u));
+}
+
 constexpr int MM_SMEM_BYTES = 2 * MM_STAGES * MM_CHUNK_BYTES + 1024 + 128;
+
+// A ring depth that fits next to the resident B slice.
+int pers_stages(int K) {
+    const int free_bytes = PG_SMEM_LIMIT - 1024 - 512 - (K / MM_BK) * MM_CHUNK_BYTES;
+    return std::max(2, std::min(PG_MAX_STAGES, free_bytes / MM_CHUNK_BYTES));
+}
+
+int pers_smem_bytes(int K) { return (K / MM_BK + pers_stages(K)) * MM_CHUNK_BYTES + 1024 + 512; }
+
+cudaError_t launch_gemm_bf16_pers(const GemmArgs &g, cudaStream_t stream) {
+    static int configured_bytes = 0;
+    const int bytes = PG_SMEM_LIMIT;
+    if (configured_bytes != bytes) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16_pers, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        configured_bytes = bytes;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int gy = (g.N + MM_BN - 1) / MM_BN;
+    const int tiles = (g.M + MM_BM - 1) / MM_BM;
+    const int gx = std::max(1, std::min(tiles, std::max(1, sms / gy)));
+    GemmArgs a = g;
+    a.stages = pers_stages(g.K);
+    k_gemm_bf16_pers<<<dim3(gx, gy, 1), PG_THREADS, pers_smem_bytes(g.K), stream>>>(a);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_gemm_bf16(const GemmArgs &g, int splits, cudaStream_t stream) {
     static bool configured = false;
@@ -356,7 +626,9 @@ extern "C" FL_API int fl_gemm_bf16(const FlGemmDesc *d, void *stream) {
     g.k_chunks_per_split = per;
     int rc = gemm_error_flag(&g.error);
     if (rc) return rc;
-    cudaError_t e = launch_gemm_bf16(g, splits, (cudaStream_t)stream);
+    // K <= 512 without split: the persistent kernel with B resident
+    cudaError_t e = (splits == 1 && K <= PG_MAX_K && !d->force_tiled) ? launch_gemm_bf16_pers(g, (cudaStream_t)stream)
+                                                                       : launch_gemm_bf16(g, splits, (cudaStream_t)stream);
     if (e != cudaSuccess) return set_error(FL_E_CUDA, "k_gemm_bf16 launch: %s", cudaGetErrorString(e));
     add_launches(1);
     return FL_OK;

@@ -122,7 +122,7 @@ class FlGemmDesc(C.Structure):
         ("a", FlGemmSegment * 3), ("n_seg", C.c_int32), ("m", C.c_int32), ("n", C.c_int32),
         ("b", C.c_void_p), ("ldb", C.c_int64), ("bias", C.c_void_p), ("residual", C.c_void_p), ("ldr", C.c_int64),
         ("out_f32", C.c_void_p), ("out_bf16", C.c_void_p), ("ldo", C.c_int64), ("relu", C.c_int32),
-        ("k_splits", C.c_int32),
+        ("k_splits", C.c_int32), ("force_tiled", C.c_int32),
     ]
 
 

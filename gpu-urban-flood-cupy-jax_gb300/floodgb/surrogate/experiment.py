@@ -203,7 +203,16 @@ def main():
     p.add_argument("--train-seconds", type=float, default=None)
     p.add_argument("--out", default=None)
     p.add_argument("--weights", default=None)
+    p.add_argument("--screen-only", default=None, help="screen with saved weights (no training)")
     a = p.parse_args()
+    if a.screen_only:
+        res = screen_saved(a.screen_only, n_eval=a.eval, plain_sample=8, duration_cap_h=a.duration_cap_h)
+        text = json.dumps(res, indent=1)
+        if a.out:
+            with open(a.out, "w") as f:
+                f.write(text)
+        print(text)
+        return
     res = run(a.grid_n, a.train, a.eval, a.seed, a.epochs, n_layers=a.layers, duration_cap_h=a.duration_cap_h,
               train_seconds=a.train_seconds, weights_out=a.weights)
     text = json.dumps(res, indent=1)

@@ -21,7 +21,8 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else None
 
 
-def gemm(segments, b, *, bias=None, residual=None, out_f32=None, out_bf16=None, relu=False, k_splits=1):
+def gemm(segments, b, *, bias=None, residual=None, out_f32=None, out_bf16=None, relu=False, k_splits=1,
+         force_tiled=False):
     """out = act(cat_k(seg_rows) . b^T + bias) (+ residual) on the tensor cores.
 
     segments: list of (tensor bf16 [rows, >= width], row_index int32 [m] or None, width);
@@ -65,6 +66,7 @@ def gemm(segments, b, *, bias=None, residual=None, out_f32=None, out_bf16=None, 
     d.ldo = out.stride(-2)
     d.relu = int(bool(relu))
     d.k_splits = int(k_splits)
+    d.force_tiled = int(bool(force_tiled))
     N.check(lib.fl_gemm_bf16(C.byref(d), _stream()), "fl_gemm_bf16")
 
 

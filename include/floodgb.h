@@ -314,6 +314,7 @@ typedef struct {
     int64_t ldo;
     int32_t relu;
     int32_t k_splits;
+    int32_t force_tiled;  /* 1: one-tile-per-CTA kernel even when K <= 512 (tests) */
 } FlGemmDesc;
 
 FL_API int fl_gemm_bf16(const FlGemmDesc *desc, void *stream);

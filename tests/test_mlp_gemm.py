@@ -31,19 +31,22 @@ def close(got, ref, rtol=2e-3):
     assert err <= tol, f"max error {err:.3e} > {tol:.3e}"
 
 
-@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (1000, 128, 384), (300, 256, 128), (77, 384, 192)])
-def test_gemm_plain(m, n, k):
+@pytest.mark.parametrize("tiled", [False, True])
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (1000, 128, 384), (300, 256, 128), (77, 384, 192),
+                                   (40000, 128, 512), (129, 64, 256)])
+def test_gemm_plain(m, n, k, tiled):
     from floodgb.surrogate import ops
 
     a = bf16(m, k, seed=1)
     b = bf16(n, k, scale=0.1, seed=2)
     out = torch.empty(m, n, device="cuda", dtype=torch.float32)
-    ops.gemm([(a, None, k)], b, out_f32=out)
+    ops.gemm([(a, None, k)], b, out_f32=out, force_tiled=tiled)
     ops.status()
     close(out, a.float() @ b.float().T)
 
 
-def test_gemm_gathered_segments_bias_relu_residual():
+@pytest.mark.parametrize("tiled", [False, True])
+def test_gemm_gathered_segments_bias_relu_residual(tiled):
     from floodgb.surrogate import ops
 
     nodes, edges, h = 500, 1700, 128
@@ -58,7 +61,7 @@ def test_gemm_gathered_segments_bias_relu_residual():
     out = torch.empty(edges, h, device="cuda", dtype=torch.float32)
     outb = torch.empty(edges, h, device="cuda", dtype=torch.bfloat16)
     ops.gemm([(x, dst, h), (x, src, h), (e, None, h)], w, bias=bias, residual=res, out_f32=out, out_bf16=outb,
-             relu=True)
+             relu=True, force_tiled=tiled)
     ops.status()
     cat = torch.cat([x[dst.long()], x[src.long()], e], dim=1).float()
     ref = torch.relu(cat @ w.float().T + bias) + res
