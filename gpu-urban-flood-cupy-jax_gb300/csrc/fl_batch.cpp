@@ -143,6 +143,8 @@ static int batch_create_impl(int32_t n, const FlMeshDesc *meshes, const FlForcin
         if (!(p.cfl > 0.0 && p.cfl <= 1.0) || p.cfl_update_interval_steps < 1 || !(p.max_dt_s > 0.0) ||
             !(p.duration_s > 0.0) || !(p.snapshot_interval_s > 0.0) || p.max_snapshots < 1)
             return set_error(FL_E_INVALID, "scenario %d: invalid solver parameters", s);
+        if (p.surface_step_mode != 0)
+            return set_error(FL_E_UNSUPPORTED, "scenario %d: the batched ensemble runs the full-SWE surface step only", s);
         if (p.gravity_mps2 != params[0].gravity_mps2 || p.min_depth_m != params[0].min_depth_m ||
             p.cfl != params[0].cfl || p.max_speed_mps != params[0].max_speed_mps)
             return set_error(FL_E_INVALID, "scenario %d: gravity, min depth, cfl and max speed must match the batch", s);

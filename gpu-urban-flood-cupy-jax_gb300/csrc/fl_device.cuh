@@ -225,6 +225,13 @@ __device__ __forceinline__ float cfl_local(float h, float hu, float hv, float ch
     return xdiv(xmul(cfl, char_len), fmax32(speed, 1.0e-12f));
 }
 
+// Local-inertial CFL of one cell (reference equations.py:181-210): gravity-
+// wave speed only, correctly rounded as the reference's float32 arrays.
+__device__ __forceinline__ float cfl_local_li(float h, float char_len, float cfl, float g, float md) {
+    const float c = xsqrt(xmul(g, fmax32(h, md)));
+    return xdiv(xmul(cfl, char_len), fmax32(c, 1.0e-12f));
+}
+
 // --------------------------------------------------------------- inlets
 // Requested capture and surcharge volume of inlet i for one step (reference
 // inlet_exchange_request_kernel, triangular_inlet_exchange_cuda_kernels.py:52-131).

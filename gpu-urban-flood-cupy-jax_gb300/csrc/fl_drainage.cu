@@ -166,9 +166,12 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs
         const int4 gr = a.grp[g];
         const int c = gr.x, k = gr.y;
         float h = 0.0f, area = 1.0f;
+        uint32_t cflags = 0u;
         if (c >= 0) {
             h = hs[c].x;
-            area = a.cinfo[c].x;
+            const float4 ci = a.cinfo[c];
+            area = ci.x;
+            cflags = __float_as_uint(ci.z);
             if (k >= 0) {  // the cell's inlet exchange, in its inlets' order
                 float dh = 0.0f;
                 for (int q = a.kcell_start[k]; q < a.kcell_start[k + 1]; ++q) {
@@ -179,6 +182,7 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs
             }
         }
         float hd = 0.0f;
+        double hd64 = 0.0;  // table mode: the fallback return depth in float64
         for (int n = gr.z; n < gr.w; ++n) {
             const float2 Vp = ff_clamp0(a.Vb[n]);
             const float fn = a.fac[n];
@@ -227,26 +231,205 @@ __global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs
                 V = ff_add(V, -out);
                 led[0] += out;
             }
-            // overflow return (reference node_overflow_return_kernel :179-207)
             const float capv = a.nd_capv[n];
-            const float ovf = fmax32(ff_val(V) - capv, 0.0f);
-            if (c >= 0 && ovf > 0.0f) {
-                V = ff_add(V, -ovf);
-                hd += ovf / area;
-                led[1] += ovf;
+            if (a.table) {
+                // weighted return (reference triangular_backend.py:1424-1474) in
+                // float64: a node with table entries returns overflow x weight
+                // through them (at most its overflow); the others fall back to
+                // their cell
+                const double ovf = fmax((double)V.x + (double)V.y - (double)capv, 0.0);
+                const int e0 = a.node_tstart[n], e1 = a.node_tstart[n + 1];
+                double r = 0.0;
+                if (e1 > e0) {
+                    for (int e = e0; e < e1; ++e) r += ovf * (double)a.node_tw[e];
+                    r = fmin(r, ovf);
+                    a.ovf_node[n] = ovf;
+                } else if (c >= 0) {
+                    r = ovf;
+                    hd64 += r / (double)area;
+                }
+                if (r > 0.0) {
+                    const float rh = (float)r;
+                    V = ff_add(ff_add(V, -rh), -(float)(r - (double)rh));
+                    led[1] += rh;
+                }
+            } else {
+                // overflow return (reference node_overflow_return_kernel :179-207)
+                const float ovf = fmax32(ff_val(V) - capv, 0.0f);
+                if (c >= 0 && ovf > 0.0f) {
+                    V = ff_add(V, -ovf);
+                    hd += ovf / area;
+                    led[1] += ovf;
+                }
             }
             led[2] += fmax32(ff_val(V) - capv, 0.0f);
             a.Va[n] = V;
             if (s.snap_slot >= 0) a.snap_v[(size_t)s.snap_slot * (size_t)a.N + n] = ff_val(V);
         }
-        if (c >= 0) {
-            const float hf = h + hd;
+        if (c >= 0 && a.table && (cflags & CELL_SURCHARGE)) {
+            // k_surcharge adds the table's return first, then this fallback
+            hs[c].x = h;
+            int lo = 0, hi = a.U;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (a.tcell[mid] < c) lo = mid + 1; else hi = mid;
+            }
+            a.s2[lo] = hd64;
+        } else if (c >= 0) {
+            const float hf = a.table ? (float)((double)h + hd64) : h + hd;
             hs[c].x = hf;
-            if ((s.phases & FL_PHASE_SURFACE) && a.forcing_kind == 1) a.wet[c] = a.wet[c] + dt * (float)(hf > a.md);
-            if (s.snap_slot >= 0) a.snap_h[(size_t)s.snap_slot * (size_t)a.C + c] = hf;
+            // a recharge cell is finished by k_recharge
+            const bool fin = !(a.has_recharge && (s.phases & FL_PHASE_RECHARGE) && (cflags & CELL_RECHARGE));
+            if (fin) {
+                if ((s.phases & FL_PHASE_SURFACE) && a.forcing_kind == 1) a.wet[c] = a.wet[c] + dt * (float)(hf > a.md);
+                if (s.snap_slot >= 0) a.snap_h[(size_t)s.snap_slot * (size_t)a.C + c] = hf;
+            }
         }
     }
     warp_add_ledger<D2_TERMS>(led, a.ledger);
+}
+
+// Weighted surcharge return into the table cells (reference
+// triangular_backend.py:1424-1474), after k_network: h = float32((h + sum
+// over the cell's entries, in entry order, of overflow x weight / area) +
+// the fallback return of the cell's own nodes), then the cell is finished.
+__global__ void __launch_bounds__(128) k_surcharge(const __grid_constant__ SurchargeArgs a, int slot) {
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= a.U) return;
+    float4 *hs = s.parity ? a.state0 : a.state1;
+    const int c = a.cell[u];
+    const double area = (double)a.cinfo[c].x;
+    double s1 = 0.0;
+    for (int k = a.start[u]; k < a.start[u + 1]; ++k) {
+        const int2 e = a.ent[k];
+        s1 += a.ovf_node[e.x] * (double)__int_as_float(e.y) / area;
+    }
+    const float hf = (float)(((double)hs[c].x + s1) + a.s2[u]);
+    hs[c].x = hf;
+    const bool fin = !(a.has_recharge && (s.phases & FL_PHASE_RECHARGE) &&
+                       (__float_as_uint(a.cinfo[c].z) & CELL_RECHARGE));
+    if (fin) {
+        const float dt = s.dt_f;
+        if ((s.phases & FL_PHASE_SURFACE) && a.forcing_kind == 1) a.wet[c] = a.wet[c] + dt * (float)(hf > a.md);
+        if (s.snap_slot >= 0) a.snap_h[(size_t)s.snap_slot * (size_t)a.C + c] = hf;
+    }
+}
+
+int surcharge_blocks(int32_t U) { return (U + 127) / 128 > 0 ? (U + 127) / 128 : 1; }
+
+cudaError_t launch_surcharge(const SurchargeArgs &a, int slot, cudaStream_t stream) {
+    k_surcharge<<<surcharge_blocks(a.U), 128, 0, stream>>>(a, slot);
+    return cudaGetLastError();
+}
+
+// Receiver j's hydrograph at time t (reference production_event_support.py
+// :169-178): the first / last value outside the table, else np.interp's
+// linear interpolation in float64 (slope over the bracketing interval, the
+// exact value at a table time, the other end's form if the first gives NaN),
+// rounded to float32.
+__device__ __forceinline__ float inflow_q(const InflowArgs &a, int j, int k, double t) {
+    const size_t J = (size_t)a.J;
+    if (k < 0) return a.q[j];
+    if (k >= a.T - 1) return a.q[(size_t)(a.T - 1) * J + j];
+    const double x0 = a.times[k], x1 = a.times[k + 1];
+    const double y0 = (double)a.q[(size_t)k * J + j], y1 = (double)a.q[(size_t)(k + 1) * J + j];
+    if (x0 == t) return (float)y0;
+    const double slope = __ddiv_rn(__dsub_rn(y1, y0), __dsub_rn(x1, x0));
+    double r = __dadd_rn(__dmul_rn(slope, __dsub_rn(t, x0)), y0);
+    if (isnan(r)) {
+        r = __dadd_rn(__dmul_rn(slope, __dsub_rn(t, x1)), y1);
+        if (isnan(r) && y0 == y1) r = y0;
+    }
+    return (float)r;
+}
+
+// External boundary inflow of the step (reference production_event_support.py
+// :181-196, applied at t + dt/2 after the clamp, engine.py:263-273): each
+// receiver adds float32(q) * dt / area into its cell's sum (np.add.at on
+// zeros, receivers in index order); the surface kernel then adds the sum to
+// the cell's depth.  Each receiver's volume goes to its own ledger slot.
+__global__ void __launch_bounds__(128) k_inflow(const __grid_constant__ InflowArgs a, int slot) {
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_INFLOW)) return;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= a.U) return;
+    const double t = __dadd_rn(s.t0, __dmul_rn(0.5, s.dt));
+    // k: -1 before the table, T - 1 at or after its end, else times[k] <= t < times[k + 1]
+    int k;
+    if (t <= a.times[0]) {
+        k = -1;
+    } else if (t >= a.times[a.T - 1]) {
+        k = a.T - 1;
+    } else {
+        int lo = 0, hi = a.T - 1;  // times[lo] < t < times[hi]
+        while (hi - lo > 1) {
+            const int m = (lo + hi) >> 1;
+            if (a.times[m] <= t) lo = m; else hi = m;
+        }
+        k = lo;
+    }
+    const int c = a.cell[u];
+    const float area = a.cinfo[c].x;
+    float sum = 0.0f;
+    for (int e = a.start[u]; e < a.start[u + 1]; ++e) {
+        const int j = a.recv[e];
+        const float added = __fmul_rn(inflow_q(a, j, k, t), s.dt_f);
+        sum = __fadd_rn(sum, __fdiv_rn(added, area));
+        ff_accumulate(&a.led[j], added);
+    }
+    a.add[c] = sum;
+}
+
+int inflow_blocks(int32_t U) { return (U + 127) / 128 > 0 ? (U + 127) / 128 : 1; }
+
+cudaError_t launch_inflow(const InflowArgs &a, int slot, cudaStream_t stream) {
+    k_inflow<<<inflow_blocks(a.U), 128, 0, stream>>>(a, slot);
+    return cudaGetLastError();
+}
+
+// Surface recharge (reference june5_production_drainage.py:543-572), after
+// the drainage step: one thread per recharge cell runs the cell's rows in
+// table order on the depth the step left (every row sees that depth), keeps
+// the last row's capture for the cell's final depth (NumPy's assignment with
+// repeated indices), and finishes the cell (wet time, depth snapshot).
+__global__ void __launch_bounds__(128) k_recharge(const __grid_constant__ RechargeArgs a, int slot) {
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_RECHARGE)) return;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= a.U) return;
+    float4 *hs = s.parity ? a.state0 : a.state1;
+    const float dt = s.dt_f;
+    const int c = a.cell[u];
+    const float h = hs[c].x;
+    const float area = fmax32(a.cinfo[c].x, 1.0e-6f);
+    float hf = h;
+    for (int k = a.row_start[u]; k < a.row_start[u + 1]; ++k) {
+        const int r = a.rows[k];
+        const float4 p = a.par[r];  // {storage capacity, capture capacity, recharge capacity, stop depth}
+        const float available = __fmul_rn(fmax32(__fsub_rn(h, p.w), 0.0f), area);
+        const float request = __fmul_rn(p.y, dt);
+        float st = a.storage[r];
+        const float remaining = fmax32(__fsub_rn(p.x, st), 0.0f);
+        const float cap = fmin32(fmin32(available, request), remaining);
+        hf = fmax32(__fsub_rn(h, __fdiv_rn(cap, area)), 0.0f);
+        st = __fadd_rn(st, cap);
+        const float loss = fmin32(st, __fmul_rn(p.z, dt));
+        a.storage[r] = __fsub_rn(st, loss);
+        ff_accumulate(&a.led[2 * r], cap);
+        ff_accumulate(&a.led[2 * r + 1], loss);
+    }
+    hs[c].x = hf;
+    if ((s.phases & FL_PHASE_SURFACE) && a.forcing_kind == 1) a.wet[c] = a.wet[c] + dt * (float)(hf > a.md);
+    if (s.snap_slot >= 0) a.snap_h[(size_t)s.snap_slot * (size_t)a.C + c] = hf;
+}
+
+int recharge_blocks(int32_t U) { return (U + 127) / 128 > 0 ? (U + 127) / 128 : 1; }
+
+cudaError_t launch_recharge(const RechargeArgs &a, int slot, cudaStream_t stream) {
+    k_recharge<<<recharge_blocks(a.U), 128, 0, stream>>>(a, slot);
+    return cudaGetLastError();
 }
 
 int node_blocks(int32_t N) { return (N + 127) / 128 > 0 ? (N + 127) / 128 : 1; }

@@ -42,7 +42,10 @@ constexpr int64_t MAX_CELLS = 0x7FFFFFFE;
 // cinfo[c] = {area, manning, flags (bits), inlet-cell index + 1 (bits, 0 = none)}
 constexpr uint32_t CELL_ACTIVE = 1u;
 constexpr uint32_t CELL_COUPLED = 2u;       // drainage writes this cell's final depth
+constexpr uint32_t CELL_SURCHARGE = 4u;     // a weighted surcharge-return cell (k_surcharge finishes it)
 constexpr int CELL_RIGHT_SHIFT = 3;         // bits 3-5: slot k is a right-side slot
+constexpr uint32_t CELL_RECEIVER = 1u << 6; // an external boundary inflow receiver
+constexpr uint32_t CELL_RECHARGE = 1u << 7; // the recharge step writes this cell's final depth
 
 // Per-step control, double-buffered by launch slot.  Written by the planner
 // (one thread) of the previous launch, read by every kernel of the step.
@@ -120,6 +123,22 @@ struct InletReqView {
     float g2;                     // 2 g (float32)
 };
 
+// External boundary inflow: one thread per receiver cell sums its receivers'
+// depths for the step into add[cell], which the surface kernel adds after
+// the clamp.
+struct InflowArgs {
+    const int32_t *cell;          // [U] receiver cells (new order)
+    const int32_t *start;         // [U + 1] receivers of cell u: recv[start[u] .. start[u + 1])
+    const int32_t *recv;          // receiver indices grouped by cell, ascending within a cell
+    const double *times;          // [T] strictly increasing
+    const float *q;               // [T * J] row-major
+    float2 *led;                  // [J] float-float volume added by each receiver
+    float *add;                   // [Cp] the step's added depth of receiver cells
+    const float4 *cinfo;
+    StepCtrl *ctrl;
+    int32_t U, J, T;
+};
+
 struct SurfArgs {
     const float4 *cinfo;          // [Cp] {area, manning, flags, inlet cell + 1}
     const int4 *tile_info;        // [tiles]
@@ -146,6 +165,40 @@ struct SurfArgs {
     int32_t has_stage;
     int32_t has_inlets;
     InletReqView inl;
+    const float *ext_add;         // [Cp] external inflow depth of receiver cells this step
+};
+
+// Local-inertial surface step (three launches: edge discharge, donor scale,
+// cell update).  Edges are renumbered by their first cell (new order).
+constexpr uint32_t LI_INTERIOR = 1u;  // the edge has a right cell
+constexpr uint32_t LI_AI = 2u;        // active interior (both cells active)
+constexpr uint32_t LI_BEDGE = 4u;     // routable boundary edge (left active, outflow / transmissive)
+constexpr uint32_t LI_LACTIVE = 8u;
+constexpr uint32_t LI_RACTIVE = 16u;
+
+struct LiArgs {
+    const int2 *e_lr;             // [E] {left, right or -1}
+    const float4 *e_geo;          // [E] {nx, ny, length, flags (bits)}
+    const int4 *c_edges;          // [Cp] the cell's edges in slot order, -1 = none
+    const float4 *cinfo;
+    const float *char_len;
+    const float4 *horton;         // kind 1
+    float *wet;
+    float4 *state0, *state1;
+    float *Q;                     // [E] discharge of the step
+    float *scale;                 // [Cp] donor limit factor
+    StepCtrl *ctrl;
+    RunCtrl *run;
+    HyetoView hy;
+    double *snap_t;
+    float2 *ledger;               // [warps * SURF_TERMS] of the cell kernel
+    float *snap_h, *snap_hu, *snap_hv;
+    const float *ext_add;
+    InletReqView inl;
+    int32_t E, C;
+    int32_t forcing_kind;
+    int32_t has_inlets;
+    float infil_scalar, g, md, vmax;
 };
 
 struct DtArgs {
@@ -160,6 +213,7 @@ struct DtArgs {
     int32_t C;
     float cfl, g, md;
     double *dt_out;               // optional: fl_stable_timestep result
+    int32_t li;                   // local-inertial CFL (gravity-wave speed only)
 };
 
 // k_nodes: one thread per node, the inlet exchange of its volume.
@@ -223,6 +277,53 @@ struct NetArgs {
     int32_t G, C, N;
     int32_t forcing_kind;
     float g, md;
+    int32_t has_recharge;         // recharge cells are finished by k_recharge
+    // weighted surcharge-return table (table != 0): nodes with entries return
+    // through it, the others fall back to their cell; float64 as the reference
+    int32_t table;
+    const int32_t *node_tstart;   // [N + 1] valid entries of each node, entry order
+    const float *node_tw;         // their normalized weights
+    double *ovf_node;             // [N] overflow of nodes with entries (for k_surcharge)
+    const int32_t *tcell;         // [U] table cells (new order, ascending)
+    double *s2;                   // [U] fallback return depth of table cells that are group cells
+    int32_t U;
+};
+
+// Weighted surcharge return into the table cells, after k_network:
+// h = float32((h + sum over entries of overflow x weight / area) + fallback).
+struct SurchargeArgs {
+    const int32_t *cell;          // [U] table cells (new order)
+    const int32_t *start;         // [U + 1]
+    const int2 *ent;              // {node (new order), weight bits} in entry order per cell
+    const double *ovf_node;
+    const double *s2;
+    const float4 *cinfo;
+    float4 *state0, *state1;
+    float *wet;
+    float *snap_h;
+    StepCtrl *ctrl;
+    int32_t U, C;
+    int32_t forcing_kind;
+    float md;
+    int32_t has_recharge;
+};
+
+// Surface recharge: one thread per recharge cell, its rows in table order.
+struct RechargeArgs {
+    const int32_t *cell;          // [U] recharge cells (new order)
+    const int32_t *row_start;     // [U + 1] rows of cell u: rows[row_start[u] .. row_start[u + 1])
+    const int32_t *rows;          // table rows grouped by cell, in table order within a cell
+    const float4 *par;            // [R] {storage capacity, capture capacity, recharge capacity, stop depth}
+    float *storage;               // [R] stored volume (table order)
+    float2 *led;                  // [2R] float-float capture, recharge loss per row
+    const float4 *cinfo;
+    float4 *state0, *state1;
+    float *wet;
+    float *snap_h;
+    StepCtrl *ctrl;
+    int32_t U, C;
+    int32_t forcing_kind;
+    float md;
 };
 
 // Host-side renumbered layout (fl_plan.cpp).
@@ -233,6 +334,12 @@ struct HostLayout {
     std::vector<int32_t> inv;         // inv[reference] = new
     int32_t Cp = 0;                   // C rounded up to whole tiles
     std::vector<float4> cinfo;        // [Cp]
+    std::vector<int32_t> inc;         // [C * 3] reference cell -> its edges in slot order (-1 none)
+    // weighted surcharge-return table (empty without one)
+    std::vector<int32_t> node_tstart; // [N + 1]
+    std::vector<float> node_tw;
+    std::vector<int32_t> tcell, tcell_start;
+    std::vector<int2> tcell_ent;
     std::vector<int4> tile_info;
     std::vector<float4> ent;
     std::vector<int32_t> halo_src;

@@ -123,6 +123,7 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
     for (int64_t c = 0; c < C; ++c) {
         if (!(m.cell_area_m2[c] > 0.0f)) return set_error(FL_E_INVALID, "cell %lld has a non-positive area", (long long)c);
     }
+    L.inc = inc;
 
     // renumbering
     L.perm.resize(C);
@@ -340,6 +341,22 @@ static int validate_drain(const HostLayout &L) {
         prev = g.w;
     }
     if (prev != N) return set_error(FL_E_INVALID, "internal: drainage groups do not cover the nodes");
+    if (!L.node_tstart.empty()) {
+        const int32_t U = (int32_t)L.tcell.size();
+        if ((int32_t)L.node_tstart.size() != N + 1 || L.node_tstart[0] != 0 ||
+            L.node_tstart[N] != (int32_t)L.node_tw.size() || (int32_t)L.tcell_start.size() != U + 1 ||
+            L.tcell_start[0] != 0 || L.tcell_start[U] != (int32_t)L.tcell_ent.size() ||
+            L.tcell_ent.size() != L.node_tw.size())
+            return set_error(FL_E_INVALID, "internal: surcharge table sizes");
+        for (int32_t n = 0; n < N; ++n)
+            if (L.node_tstart[n + 1] < L.node_tstart[n]) return set_error(FL_E_INVALID, "internal: surcharge CSR");
+        for (int32_t u = 0; u < U; ++u)
+            if (L.tcell[u] < 0 || L.tcell[u] >= C || (u > 0 && L.tcell[u] <= L.tcell[u - 1]) ||
+                L.tcell_start[u + 1] <= L.tcell_start[u])
+                return set_error(FL_E_INVALID, "internal: surcharge cell %d", u);
+        for (const int2 &e : L.tcell_ent)
+            if (e.x < 0 || e.x >= N) return set_error(FL_E_INVALID, "internal: surcharge entry node");
+    }
     return FL_OK;
 }
 
@@ -524,6 +541,62 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
                 L.nl[fill[t]++] = make_int2(l, (int32_t)((uint32_t)f | NL_TO));
             }
         }
+    }
+    // weighted surcharge-return table: normalized weights (float32, the
+    // per-node sum in entry order), each node's valid entries and each table
+    // cell's entries, both in entry order
+    L.node_tstart.clear();
+    L.node_tw.clear();
+    L.tcell.clear();
+    L.tcell_start.clear();
+    L.tcell_ent.clear();
+    const int32_t E = d.surcharge_entry_count;
+    if (E < 0) return set_error(FL_E_INVALID, "surcharge_entry_count must be >= 0");
+    if (E > 0) {
+        if (!d.surcharge_cell_index || !d.surcharge_node_index || !d.surcharge_return_weight)
+            return set_error(FL_E_INVALID, "the surcharge table needs cell, node and weight arrays");
+        std::vector<float> wsum(N, 0.0f), w(E, 0.0f);
+        std::vector<uint8_t> valid(E, 0);
+        for (int32_t e = 0; e < E; ++e) {
+            const int32_t n = d.surcharge_node_index[e], c = d.surcharge_cell_index[e];
+            if (n >= N || c >= C) return set_error(FL_E_INVALID, "surcharge entry %d is out of range", e);
+            valid[e] = n >= 0 && c >= 0;
+            if (valid[e]) {
+                w[e] = std::max(d.surcharge_return_weight[e], 0.0f);
+                wsum[n] += w[e];
+            }
+        }
+        if (!d.surcharge_return_weight_is_normalized)
+            for (int32_t e = 0; e < E; ++e)
+                if (valid[e]) w[e] = w[e] / std::max(wsum[d.surcharge_node_index[e]], 1.0e-12f);
+        L.node_tstart.assign(N + 1, 0);
+        for (int32_t e = 0; e < E; ++e)
+            if (valid[e]) L.node_tstart[L.node_inv[d.surcharge_node_index[e]] + 1]++;
+        for (int32_t n = 0; n < N; ++n) L.node_tstart[n + 1] += L.node_tstart[n];
+        L.node_tw.assign(L.node_tstart[N], 0.0f);
+        std::vector<int32_t> fill(L.node_tstart.begin(), L.node_tstart.end() - 1);
+        std::vector<std::pair<int32_t, int32_t>> byc;  // (cell new, entry)
+        for (int32_t e = 0; e < E; ++e) {
+            if (!valid[e]) continue;
+            L.node_tw[fill[L.node_inv[d.surcharge_node_index[e]]]++] = w[e];
+            byc.push_back({L.inv[d.surcharge_cell_index[e]], e});
+        }
+        std::sort(byc.begin(), byc.end());
+        for (size_t k = 0; k < byc.size(); ++k) {
+            const int32_t c = byc[k].first, e = byc[k].second;
+            if (L.tcell.empty() || L.tcell.back() != c) {
+                L.tcell.push_back(c);
+                L.tcell_start.push_back((int32_t)k);
+                uint32_t f;
+                memcpy(&f, &L.cinfo[c].z, 4);
+                f |= CELL_COUPLED | CELL_SURCHARGE;
+                memcpy(&L.cinfo[c].z, &f, 4);
+            }
+            int32_t wb;
+            memcpy(&wb, &w[e], 4);
+            L.tcell_ent.push_back(make_int2(L.node_inv[d.surcharge_node_index[e]], wb));
+        }
+        L.tcell_start.push_back((int32_t)byc.size());
     }
     return validate_drain(L);
 }

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -62,6 +63,11 @@ cudaError_t launch_nodes(const NodeArgs &a, int slot, cudaStream_t stream);
 cudaError_t launch_links(const LinkArgs &a, int slot, cudaStream_t stream);
 cudaError_t launch_donor(const DonorArgs &a, int slot, cudaStream_t stream);
 cudaError_t launch_network(const NetArgs &a, int slot, cudaStream_t stream);
+cudaError_t launch_recharge(const RechargeArgs &a, int slot, cudaStream_t stream);
+cudaError_t launch_inflow(const InflowArgs &a, int slot, cudaStream_t stream);
+cudaError_t launch_surcharge(const SurchargeArgs &a, int slot, cudaStream_t stream);
+cudaError_t launch_li(const LiArgs &a, int kind, int slot, int plan_next, int sms, cudaStream_t stream);
+int li_cell_blocks(int32_t C);
 int node_blocks(int32_t N);
 int network_blocks(int32_t G);
 cudaError_t launch_f64_to_ff_perm(const double *src, float2 *dst, const int32_t *perm, int32_t n, cudaStream_t stream);
@@ -122,8 +128,26 @@ struct FlSolver {
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    // cell info: the host copy keeps the flag bits that inflow / recharge set
+    std::vector<float4> cinfo_h;
+    float4 *cinfo_d = nullptr;
+    void *ext_mem = nullptr;  // external inflow tables (one allocation)
+    void *rch_mem = nullptr;  // recharge tables (one allocation)
+    InflowArgs ext{};
+    LiArgs li{};
+    bool li_mode = false;     // surface_step_mode = local_inertial
+    int sms = 1;
+    SurchargeArgs sur{};
+    RechargeArgs rch{};
+    int32_t R = 0;            // recharge rows
     bool has_drain() const { return N > 0; }
-    int launches_per_step() const { return 1 + (has_drain() ? 4 : 0); }
+    bool has_inflow() const { return ext.U > 0; }
+    bool has_table() const { return sur.U > 0; }
+    bool has_recharge() const { return rch.U > 0; }
+    int launches_per_step() const {
+        return (li_mode ? 3 : 1) + (has_drain() ? 4 : 0) + (has_table() ? 1 : 0) + (has_inflow() ? 1 : 0) +
+               (has_recharge() ? 1 : 0);
+    }
 
     // Drainage tables live in one arena so one L2 access-policy window can
     // keep them resident across the surface kernel's stream of cell data.
@@ -175,14 +199,31 @@ static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStr
         FL_CUDA(launch_dt(s->da, s->dt_blocks, slot, 1, st));
         g_launches++;
     }
-    FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, s->surf_grid, s->surf_smem, st));
-    g_launches++;
+    if (s->has_inflow()) {
+        FL_CUDA(launch_inflow(s->ext, slot, st));
+        g_launches++;
+    }
+    if (s->li_mode) {
+        FL_CUDA(launch_li(s->li, s->kind, slot, plan_next ? 1 : 0, s->sms, st));
+        g_launches += 3;
+    } else {
+        FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, s->surf_grid, s->surf_smem, st));
+        g_launches++;
+    }
     if (s->has_drain()) {
         FL_CUDA(launch_nodes(s->nd, slot, st));
         FL_CUDA(launch_links(s->lk, slot, st));
         FL_CUDA(launch_donor(s->dn, slot, st));
         FL_CUDA(launch_network(s->nw, slot, st));
         g_launches += 4;
+    }
+    if (s->has_table()) {
+        FL_CUDA(launch_surcharge(s->sur, slot, st));
+        g_launches++;
+    }
+    if (s->has_recharge()) {
+        FL_CUDA(launch_recharge(s->rch, slot, st));
+        g_launches++;
     }
     return FL_OK;
 }
@@ -348,6 +389,8 @@ FL_API void fl_destroy(FlSolver *s) {
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     if (s->l2_persist) cudaCtxResetPersistingL2Cache();
     for (void *p : s->allocs) cudaFree(p);
+    if (s->ext_mem) cudaFree(s->ext_mem);
+    if (s->rch_mem) cudaFree(s->rch_mem);
     if (s->run_h) cudaFreeHost(s->run_h);
     if (s->poll_h) cudaFreeHost(s->poll_h);
     delete s;
@@ -453,9 +496,14 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     s->sa.e_cap = L.e_cap;
     s->sa.h_cap = L.h_cap;
     FL_CUDA(plan_surface_launch(s->sa, s->kind, device, &s->surf_grid, &s->surf_smem));
-    s->n_led_s = (size_t)surface_warps(s->surf_grid) * SURF_TERMS;
     int sms = 0;
     FL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    s->sms = sms;
+    if (p.surface_step_mode != 0 && p.surface_step_mode != 1)
+        return set_error(FL_E_INVALID, "solver.surface_step_mode must be 'full_swe' or 'local_inertial'");
+    s->li_mode = p.surface_step_mode == 1;
+    // the surface ledger: per warp of the surface kernel (or of the local-inertial cell kernel)
+    s->n_led_s = (size_t)std::max(surface_warps(s->surf_grid), s->li_mode ? li_cell_blocks(C) * 8 : 0) * SURF_TERMS;
     s->dt_blocks = std::max(1, std::min(sms * 4, (C + 255) / 256));
     float *dt_partial = nullptr;
     unsigned int *counter = nullptr;
@@ -477,7 +525,9 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
             const size_t bytes = I * (4 + 8 + 16 + 8 + 8) + (K + 1) * 4 + K * 4 + (N + 1) * 4 * 2 + N * (4 + 16 + 4) +
                                  G * 16 + S * 8 + NL * (4 * 2 + 16 * 3 + 4 * 3) + N * (8 * 2 + 4 + 4 + 4) +
                                  (size_t)(node_blocks(s->N) * 4 * D1_TERMS + network_blocks(s->G) * 4 * D2_TERMS) * 8 +
-                                 64 * 256;
+                                 (L.node_tstart.size() + L.node_tw.size()) * 4 + N * 8 +
+                                 (L.tcell.size() + L.tcell_start.size()) * 4 + L.tcell_ent.size() * 8 +
+                                 L.tcell.size() * 8 + 64 * 256;
             void *q = nullptr;
             cudaError_t e = cudaMalloc(&q, bytes);
             if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
@@ -596,6 +646,46 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         b.forcing_kind = s->kind;
         b.g = (float)p.gravity_mps2;
         b.md = (float)p.min_depth_m;
+        b.has_recharge = 0;
+        b.table = 0;
+        b.U = 0;
+        if (!L.node_tstart.empty()) {
+            int32_t *tstart, *tcell, *tcs;
+            float *tw;
+            int2 *tent;
+            double *ovf, *s2;
+            const size_t U = L.tcell.size();
+            if ((rc = s->upload(&tstart, L.node_tstart)) || (rc = s->upload(&tw, L.node_tw)) ||
+                (rc = s->upload(&tcell, L.tcell)) || (rc = s->upload(&tcs, L.tcell_start)) ||
+                (rc = s->upload(&tent, L.tcell_ent)) || (rc = s->alloc(&ovf, (size_t)s->N)) || (rc = s->alloc(&s2, U)))
+                return rc;
+            FL_CUDA(cudaMemset(ovf, 0, sizeof(double) * s->N));
+            FL_CUDA(cudaMemset(s2, 0, sizeof(double) * std::max<size_t>(U, 1)));
+            b.table = 1;
+            b.node_tstart = tstart;
+            b.node_tw = tw;
+            b.ovf_node = ovf;
+            b.tcell = tcell;
+            b.s2 = s2;
+            b.U = (int32_t)U;
+            SurchargeArgs &sg = s->sur;
+            sg.cell = tcell;
+            sg.start = tcs;
+            sg.ent = tent;
+            sg.ovf_node = ovf;
+            sg.s2 = s2;
+            sg.cinfo = cinfo;
+            sg.state0 = s->state[0];
+            sg.state1 = s->state[1];
+            sg.wet = s->wet;
+            sg.snap_h = s->snap_h;
+            sg.ctrl = s->ctrl;
+            sg.U = (int32_t)U;
+            sg.C = C;
+            sg.forcing_kind = s->kind;
+            sg.md = (float)p.min_depth_m;
+            sg.has_recharge = 0;
+        }
         s->drain_base = s->arena;
         s->drain_bytes = s->arena_used;
         s->arena = nullptr;  // later allocations are separate
@@ -603,6 +693,8 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     setup_l2_persistence(s);
     SurfArgs &a = s->sa;
     a.cinfo = cinfo;
+    s->cinfo_d = cinfo;
+    s->cinfo_h = L.cinfo;
     a.tile_info = tile_info;
     a.ent = ent;
     a.halo_src = halo_src;
@@ -642,6 +734,80 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     d.g = (float)p.gravity_mps2;
     d.md = (float)p.min_depth_m;
     d.dt_out = nullptr;
+    d.li = s->li_mode ? 1 : 0;
+    if (s->li_mode) {
+        // local-inertial tables: edges renumbered by their left cell (new
+        // order), each cell's edges in the reference's slot order
+        const int32_t E = mesh->edge_count;
+        std::vector<int32_t> eord(E), enew(E);
+        std::iota(eord.begin(), eord.end(), 0);
+        std::stable_sort(eord.begin(), eord.end(), [&](int32_t x, int32_t y) {
+            return L.inv[mesh->edge_left_cell[x]] < L.inv[mesh->edge_left_cell[y]];
+        });
+        for (int32_t k = 0; k < E; ++k) enew[eord[k]] = k;
+        auto act = [&](int32_t c) { return mesh->active_mask ? mesh->active_mask[c] > 0.5f : true; };
+        std::vector<int2> lr(E);
+        std::vector<float4> geo(E);
+        for (int32_t k = 0; k < E; ++k) {
+            const int32_t e = eord[k], l = mesh->edge_left_cell[e], r = mesh->edge_right_cell[e];
+            const bool interior = r >= 0, la = act(l), ra = interior ? act(r) : la;
+            const int32_t code = (interior && la && !ra) ? 0 : mesh->boundary_code[e];
+            uint32_t f = 0;
+            if (interior) f |= LI_INTERIOR;
+            if (interior && la && ra) f |= LI_AI;
+            if (!interior && la && (code == 1 || code == 4)) f |= LI_BEDGE;
+            if (la) f |= LI_LACTIVE;
+            if (ra) f |= LI_RACTIVE;
+            float fb;
+            memcpy(&fb, &f, 4);
+            lr[k] = make_int2(L.inv[l], interior ? L.inv[r] : -1);
+            geo[k] = make_float4(mesh->edge_normal_x[e], mesh->edge_normal_y[e], mesh->edge_length_m[e], fb);
+        }
+        std::vector<int4> ce(Cp, make_int4(-1, -1, -1, -1));
+        for (int32_t i = 0; i < C; ++i) {
+            const int32_t c = L.perm[i];
+            int32_t v[3];
+            for (int j = 0; j < 3; ++j) v[j] = L.inc[(size_t)c * 3 + j] >= 0 ? enew[L.inc[(size_t)c * 3 + j]] : -1;
+            ce[i] = make_int4(v[0], v[1], v[2], -1);
+        }
+        int2 *d_lr;
+        float4 *d_geo;
+        int4 *d_ce;
+        float *d_q, *d_scale;
+        if ((rc = s->upload(&d_lr, lr)) || (rc = s->upload(&d_geo, geo)) || (rc = s->upload(&d_ce, ce)) ||
+            (rc = s->alloc(&d_q, (size_t)E)) || (rc = s->alloc(&d_scale, (size_t)Cp)))
+            return rc;
+        LiArgs &q = s->li;
+        q.e_lr = d_lr;
+        q.e_geo = d_geo;
+        q.c_edges = d_ce;
+        q.cinfo = cinfo;
+        q.char_len = char_len;
+        q.horton = horton;
+        q.wet = s->wet;
+        q.state0 = s->state[0];
+        q.state1 = s->state[1];
+        q.Q = d_q;
+        q.scale = d_scale;
+        q.ctrl = s->ctrl;
+        q.run = s->run;
+        q.hy = s->hy;
+        q.snap_t = s->snap_t;
+        q.ledger = s->led_s;
+        q.snap_h = s->snap_h;
+        q.snap_hu = s->snap_hu;
+        q.snap_hv = s->snap_hv;
+        q.ext_add = nullptr;
+        q.inl = s->sa.inl;
+        q.E = E;
+        q.C = C;
+        q.forcing_kind = s->kind;
+        q.has_inlets = s->sa.has_inlets;
+        q.infil_scalar = forcing->infiltration_mps;
+        q.g = (float)p.gravity_mps2;
+        q.md = (float)p.min_depth_m;
+        q.vmax = (float)p.max_speed_mps;
+    }
 
     // host side
     FL_CUDA(cudaHostAlloc((void **)&s->run_h, sizeof(RunCtrl), cudaHostAllocDefault));
@@ -708,6 +874,11 @@ FL_API int fl_reset_clock(FlSolver *s, void *stream) {
     if (s->has_drain()) {
         FL_CUDA(cudaMemsetAsync(s->led_1, 0, sizeof(float2) * s->n_led_1, st));
         FL_CUDA(cudaMemsetAsync(s->led_2, 0, sizeof(float2) * s->n_led_2, st));
+    }
+    if (s->has_inflow()) FL_CUDA(cudaMemsetAsync(s->ext.led, 0, sizeof(float2) * s->ext.J, st));
+    if (s->has_recharge()) {
+        FL_CUDA(cudaMemsetAsync(s->rch.storage, 0, sizeof(float) * s->R, st));
+        FL_CUDA(cudaMemsetAsync(s->rch.led, 0, sizeof(float2) * 2 * (size_t)s->R, st));
     }
     FL_CUDA(cudaStreamSynchronize(st));
     s->slot = 0;
@@ -881,18 +1052,35 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
     r.last_dt = dt_s;
     FL_CUDA(cudaMemcpyAsync(&s->ctrl[s->slot], &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, st));
     FL_CUDA(cudaMemcpyAsync(s->run, s->run_h, sizeof(RunCtrl), cudaMemcpyHostToDevice, st));
-    FL_CUDA(launch_surface(s->sa, s->kind, s->slot, 0, s->surf_grid, s->surf_smem, st));
-    g_launches++;
+    if (s->has_inflow() && (phases & FL_PHASE_INFLOW)) {
+        FL_CUDA(launch_inflow(s->ext, s->slot, st));
+        g_launches++;
+    }
+    if (s->li_mode) {
+        FL_CUDA(launch_li(s->li, s->kind, s->slot, 0, s->sms, st));
+        g_launches += 3;
+    } else {
+        FL_CUDA(launch_surface(s->sa, s->kind, s->slot, 0, s->surf_grid, s->surf_smem, st));
+        g_launches++;
+    }
     if (s->has_drain() && (phases & FL_PHASE_DRAINAGE)) {
         FL_CUDA(launch_nodes(s->nd, s->slot, st));
         FL_CUDA(launch_links(s->lk, s->slot, st));
         FL_CUDA(launch_donor(s->dn, s->slot, st));
         FL_CUDA(launch_network(s->nw, s->slot, st));
-        g_launches += 3;
+        g_launches += 4;
+        if (s->has_table()) {
+            FL_CUDA(launch_surcharge(s->sur, s->slot, st));
+            g_launches++;
+        }
     } else if (s->has_drain()) {
         // no drainage this step: carry link flow to the other parity buffer
         FL_CUDA(cudaMemcpyAsync(s->Q[r.parity], s->Q[c.parity], sizeof(float) * std::max(s->NL, 1),
                                 cudaMemcpyDeviceToDevice, st));
+    }
+    if (s->has_recharge() && (phases & FL_PHASE_RECHARGE)) {
+        FL_CUDA(launch_recharge(s->rch, s->slot, st));
+        g_launches++;
     }
     s->slot ^= 1;
     FL_CUDA(cudaStreamSynchronize(st));
@@ -925,7 +1113,12 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
     FL_CUDA(cudaMemcpyAsync(&s->ctrl[0], &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, st));
     auto launch = [&]() -> int {
         switch (kernel) {
-            case 0: FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, s->surf_grid, s->surf_smem, st)); break;
+            case 0:
+                if (s->li_mode)
+                    FL_CUDA(launch_li(s->li, s->kind, 0, 0, s->sms, st));
+                else
+                    FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, s->surf_grid, s->surf_smem, st));
+                break;
             case 1: FL_CUDA(launch_nodes(s->nd, 0, st)); break;
             case 2: FL_CUDA(launch_network(s->nw, 0, st)); break;
             case 4: FL_CUDA(launch_links(s->lk, 0, st)); break;
@@ -979,6 +1172,7 @@ FL_API int fl_update_forcing(FlSolver *s, const float *rain_multiplier, const fl
     if (s->kind == 0) {
         if (s->sa.infil_scalar != infiltration_mps) {
             s->sa.infil_scalar = infiltration_mps;
+            s->li.infil_scalar = infiltration_mps;
             if (s->graph) {  // the graph holds the kernel arguments by value
                 cudaGraphExecDestroy(s->graph);
                 s->graph = nullptr;
@@ -1042,6 +1236,18 @@ FL_API int fl_read_ledger(FlSolver *s, double *out, int32_t n, void *stream) {
         sum_blocks(v1, D1_TERMS, all + FL_LEDGER_CAPTURE);
         sum_blocks(v2, D2_TERMS, all + FL_LEDGER_OUTFALL);
     }
+    if (s->has_inflow()) {
+        std::vector<float2> ve(s->ext.J);
+        FL_CUDA(cudaMemcpyAsync(ve.data(), s->ext.led, sizeof(float2) * ve.size(), cudaMemcpyDeviceToHost, st));
+        FL_CUDA(cudaStreamSynchronize(st));
+        sum_blocks(ve, 1, all + FL_LEDGER_EXTERNAL_INFLOW);
+    }
+    if (s->has_recharge()) {
+        std::vector<float2> vr(2 * (size_t)s->R);
+        FL_CUDA(cudaMemcpyAsync(vr.data(), s->rch.led, sizeof(float2) * vr.size(), cudaMemcpyDeviceToHost, st));
+        FL_CUDA(cudaStreamSynchronize(st));
+        sum_blocks(vr, 2, all + FL_LEDGER_RECHARGE_CAPTURE);
+    }
     FL_CUDA(cudaMemsetAsync(s->vol_out, 0, 2 * sizeof(double), st));
     FL_CUDA(launch_volumes(s->state[0], s->state[1], s->sa.cinfo, s->Va, s->run, s->C, s->N, s->vol_out, st));
     g_launches++;
@@ -1083,6 +1289,212 @@ FL_API int fl_get_snapshots(FlSolver *s, int32_t first, int32_t count, double *t
             FL_CUDA(cudaStreamSynchronize(st));
         }
     }
+    FL_CUDA(cudaStreamSynchronize(st));
+    return FL_OK;
+}
+
+// ------------------------------------------------- inflow and recharge tables
+static uint32_t cell_flags(const float4 &ci) {
+    uint32_t f;
+    memcpy(&f, &ci.z, 4);
+    return f;
+}
+
+static void set_cell_flags(float4 &ci, uint32_t f) { memcpy(&ci.z, &f, 4); }
+
+// Replace one flag bit on the given cells (new order) and upload the cell info.
+static int put_flag(FlSolver *s, uint32_t bit, const std::vector<int32_t> &cells) {
+    for (float4 &ci : s->cinfo_h) set_cell_flags(ci, cell_flags(ci) & ~bit);
+    for (int32_t c : cells) set_cell_flags(s->cinfo_h[c], cell_flags(s->cinfo_h[c]) | bit);
+    FL_CUDA(cudaMemcpy(s->cinfo_d, s->cinfo_h.data(), sizeof(float4) * s->cinfo_h.size(), cudaMemcpyHostToDevice));
+    return FL_OK;
+}
+
+// Drop the captured step graph (it holds kernel arguments by value).
+static void drop_graph(FlSolver *s) {
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+}
+
+static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+FL_API int fl_set_boundary_inflow(FlSolver *s, int32_t J, const int32_t *cells, int32_t T, const double *times,
+                                  const float *q) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    if (J < 0) return set_error(FL_E_INVALID, "receiver_count must be >= 0");
+    if (J > 0 && (!cells || !times || !q || T < 1))
+        return set_error(FL_E_INVALID, "external inflow needs receiver cells, at least one time and the flow table");
+    std::vector<int32_t> inv(s->C);
+    for (int32_t i = 0; i < s->C; ++i) inv[s->perm_h[i]] = i;
+    // receivers grouped by cell (cells in new order, receivers ascending)
+    std::vector<std::pair<int32_t, int32_t>> byc(J);
+    for (int32_t j = 0; j < J; ++j) {
+        const int32_t c = cells[j];
+        if (c < 0 || c >= s->C) return set_error(FL_E_INVALID, "External boundary inflow cell_index is outside mesh range.");
+        if (!(cell_flags(s->cinfo_h[inv[c]]) & CELL_ACTIVE))
+            return set_error(FL_E_INVALID, "External boundary inflow cell_index contains inactive cells.");
+        byc[j] = {inv[c], j};
+    }
+    for (int32_t k = 0; k < T && J > 0; ++k) {
+        if (!std::isfinite(times[k]) || (k > 0 && !(times[k] > times[k - 1])))
+            return set_error(FL_E_INVALID, "external inflow times must be finite and strictly increasing");
+    }
+    std::sort(byc.begin(), byc.end());
+    std::vector<int32_t> ucell, start, recv(J);
+    for (int32_t k = 0; k < J; ++k) {
+        if (k == 0 || byc[k].first != byc[k - 1].first) {
+            ucell.push_back(byc[k].first);
+            start.push_back(k);
+        }
+        recv[k] = byc[k].second;
+    }
+    start.push_back(J);
+    const int32_t U = (int32_t)ucell.size();
+    FL_CUDA(cudaSetDevice(s->device));
+    FL_CUDA(cudaDeviceSynchronize());  // no launch in flight still reads the old tables
+    drop_graph(s);
+    if (s->ext_mem) {
+        cudaFree(s->ext_mem);
+        s->ext_mem = nullptr;
+    }
+    s->ext = InflowArgs{};
+    s->sa.ext_add = nullptr;
+    s->li.ext_add = nullptr;
+    int rc = put_flag(s, CELL_RECEIVER, ucell);
+    if (rc || J == 0) return rc;
+    const size_t o_s = up256(sizeof(int32_t) * U), o_r = o_s + up256(sizeof(int32_t) * (U + 1)),
+                 o_t = o_r + up256(sizeof(int32_t) * J), o_q = o_t + up256(sizeof(double) * T),
+                 o_l = o_q + up256(sizeof(float) * (size_t)T * J), o_a = o_l + up256(sizeof(float2) * J),
+                 bytes = o_a + sizeof(float) * (size_t)s->Cp;
+    void *m = nullptr;
+    cudaError_t e = cudaMalloc(&m, bytes);
+    if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    s->ext_mem = m;
+    char *b = (char *)m;
+    FL_CUDA(cudaMemcpy(b, ucell.data(), sizeof(int32_t) * U, cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemcpy(b + o_s, start.data(), sizeof(int32_t) * (U + 1), cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemcpy(b + o_r, recv.data(), sizeof(int32_t) * J, cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemcpy(b + o_t, times, sizeof(double) * T, cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemcpy(b + o_q, q, sizeof(float) * (size_t)T * J, cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemset(b + o_l, 0, sizeof(float2) * J));
+    FL_CUDA(cudaMemset(b + o_a, 0, sizeof(float) * (size_t)s->Cp));
+    InflowArgs &x = s->ext;
+    x.cell = (const int32_t *)b;
+    x.start = (const int32_t *)(b + o_s);
+    x.recv = (const int32_t *)(b + o_r);
+    x.times = (const double *)(b + o_t);
+    x.q = (const float *)(b + o_q);
+    x.led = (float2 *)(b + o_l);
+    x.add = (float *)(b + o_a);
+    x.cinfo = s->cinfo_d;
+    x.ctrl = s->ctrl;
+    x.U = U;
+    x.J = J;
+    x.T = T;
+    s->sa.ext_add = x.add;
+    s->li.ext_add = x.add;
+    return FL_OK;
+}
+
+FL_API int fl_set_recharge(FlSolver *s, int32_t R, const int32_t *cells, const float *storage_cap,
+                           const float *capture_cap, const float *recharge_cap, const float *stop_depth) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    if (R < 0) return set_error(FL_E_INVALID, "row_count must be >= 0");
+    if (R > 0 && (!cells || !storage_cap || !capture_cap || !recharge_cap || !stop_depth))
+        return set_error(FL_E_INVALID, "recharge needs cells and the four per-row arrays");
+    std::vector<int32_t> inv(s->C);
+    for (int32_t i = 0; i < s->C; ++i) inv[s->perm_h[i]] = i;
+    // rows grouped by cell (cells in new order, rows in table order)
+    std::vector<std::pair<int32_t, int32_t>> byc(R);
+    for (int32_t r = 0; r < R; ++r) {
+        if (cells[r] < 0 || cells[r] >= s->C) return set_error(FL_E_INVALID, "recharge source_cell_index is outside mesh range");
+        byc[r] = {inv[cells[r]], r};
+    }
+    std::sort(byc.begin(), byc.end());
+    std::vector<int32_t> ucell, start, rows(R);
+    std::vector<float4> par(R);
+    for (int32_t k = 0; k < R; ++k) {
+        if (k == 0 || byc[k].first != byc[k - 1].first) {
+            ucell.push_back(byc[k].first);
+            start.push_back(k);
+        }
+        rows[k] = byc[k].second;
+    }
+    start.push_back(R);
+    for (int32_t r = 0; r < R; ++r) par[r] = make_float4(storage_cap[r], capture_cap[r], recharge_cap[r], stop_depth[r]);
+    const int32_t U = (int32_t)ucell.size();
+    FL_CUDA(cudaSetDevice(s->device));
+    FL_CUDA(cudaDeviceSynchronize());
+    drop_graph(s);
+    if (s->rch_mem) {
+        cudaFree(s->rch_mem);
+        s->rch_mem = nullptr;
+    }
+    s->rch = RechargeArgs{};
+    s->R = 0;
+    s->nw.has_recharge = 0;
+    s->sur.has_recharge = 0;
+    int rc = put_flag(s, CELL_RECHARGE, ucell);
+    if (rc || R == 0) return rc;
+    const size_t o_s = up256(sizeof(int32_t) * U), o_r = o_s + up256(sizeof(int32_t) * (U + 1)),
+                 o_p = o_r + up256(sizeof(int32_t) * R), o_st = o_p + up256(sizeof(float4) * R),
+                 o_l = o_st + up256(sizeof(float) * R), bytes = o_l + sizeof(float2) * 2 * (size_t)R;
+    void *m = nullptr;
+    cudaError_t e = cudaMalloc(&m, bytes);
+    if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    s->rch_mem = m;
+    char *b = (char *)m;
+    FL_CUDA(cudaMemcpy(b, ucell.data(), sizeof(int32_t) * U, cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemcpy(b + o_s, start.data(), sizeof(int32_t) * (U + 1), cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemcpy(b + o_r, rows.data(), sizeof(int32_t) * R, cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemcpy(b + o_p, par.data(), sizeof(float4) * R, cudaMemcpyHostToDevice));
+    FL_CUDA(cudaMemset(b + o_st, 0, sizeof(float) * R));
+    FL_CUDA(cudaMemset(b + o_l, 0, sizeof(float2) * 2 * (size_t)R));
+    RechargeArgs &a = s->rch;
+    a.cell = (const int32_t *)b;
+    a.row_start = (const int32_t *)(b + o_s);
+    a.rows = (const int32_t *)(b + o_r);
+    a.par = (const float4 *)(b + o_p);
+    a.storage = (float *)(b + o_st);
+    a.led = (float2 *)(b + o_l);
+    a.cinfo = s->cinfo_d;
+    a.state0 = s->state[0];
+    a.state1 = s->state[1];
+    a.wet = s->wet;
+    a.snap_h = s->snap_h;
+    a.ctrl = s->ctrl;
+    a.U = U;
+    a.C = s->C;
+    a.forcing_kind = s->kind;
+    a.md = (float)s->params.min_depth_m;
+    s->R = R;
+    s->nw.has_recharge = 1;
+    s->sur.has_recharge = 1;
+    return FL_OK;
+}
+
+FL_API int fl_get_recharge_storage(FlSolver *s, float *out, int32_t n, int32_t mem, void *stream) {
+    if (!s || !out) return set_error(FL_E_INVALID, "solver or output is NULL");
+    if (n != s->R) return set_error(FL_E_INVALID, "recharge storage has %d rows, %d requested", s->R, n);
+    if (n == 0) return FL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    FL_CUDA(cudaMemcpyAsync(out, s->rch.storage, sizeof(float) * n,
+                            mem == FL_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    return FL_OK;
+}
+
+FL_API int fl_set_recharge_storage(FlSolver *s, const float *in, int32_t n, int32_t mem, void *stream) {
+    if (!s || !in) return set_error(FL_E_INVALID, "solver or input is NULL");
+    if (n != s->R) return set_error(FL_E_INVALID, "recharge storage has %d rows, %d given", s->R, n);
+    if (n == 0) return FL_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    FL_CUDA(cudaSetDevice(s->device));
+    FL_CUDA(cudaMemcpyAsync(s->rch.storage, in, sizeof(float) * n,
+                            mem == FL_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
     FL_CUDA(cudaStreamSynchronize(st));
     return FL_OK;
 }

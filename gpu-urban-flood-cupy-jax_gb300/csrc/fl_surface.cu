@@ -110,6 +110,7 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
     const float md = a.md;
     const bool do_surface = (s.phases & FL_PHASE_SURFACE) != 0;
     const bool drain_finishes = (s.phases & FL_PHASE_DRAINAGE) != 0;
+    const bool recharge_finishes = (s.phases & FL_PHASE_RECHARGE) != 0;
     float led[SURF_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
 
     const uint32_t bar0 = smem_addr(&s_bar[0]), bar1 = smem_addr(&s_bar[1]);
@@ -196,6 +197,8 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
 #pragma unroll
             for (int k = 0; k < 3; ++k) s_flux[tid * 3 + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             if (s.phases & FL_PHASE_CLAMP) clamp_velocity_exact(hn, hun, hvn, a.vmax);
+            // external boundary inflow after the clamp (reference engine.py:263-273)
+            if ((info & CELL_RECEIVER) && (s.phases & FL_PHASE_INFLOW)) hn = __fadd_rn(hn, a.ext_add[c]);
             out[c] = make_float4(hn, hun, hvn, st.w);
             // requested inlet capture / surcharge of this cell's inlets, from the
             // depth the drainage step starts with, and the cell's capture limit
@@ -212,7 +215,8 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
                 }
                 v.capf[kc - 1] = fmin32(1.0f, (fmax32(hn, 0.0f) * ci.x) / fmax32(sum, 1.0e-12f));
             }
-            const bool final_here = !(drain_finishes && (info & CELL_COUPLED));
+            const bool final_here = !(drain_finishes && (info & CELL_COUPLED)) &&
+                                    !(recharge_finishes && (info & CELL_RECHARGE));
             if (KIND == 1 && do_surface && final_here) a.wet[c] = wt + dt * (float)(hn > md);
             if (s.snap_slot >= 0) {
                 const size_t o = (size_t)s.snap_slot * (size_t)a.C + (size_t)c;
@@ -248,7 +252,8 @@ __global__ void __launch_bounds__(256) k_dt(const __grid_constant__ DtArgs a, in
     float best = CUDART_INF_F;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.C; c += gridDim.x * blockDim.x) {
         const float4 v = st[c];
-        const float local = cfl_local(v.x, v.y, v.z, a.char_len[c], a.cfl, a.g, a.md);
+        const float local = a.li ? cfl_local_li(v.x, a.char_len[c], a.cfl, a.g, a.md)
+                                 : cfl_local(v.x, v.y, v.z, a.char_len[c], a.cfl, a.g, a.md);
         if (isfinite(local) && local < best) best = local;
     }
 #pragma unroll

@@ -4,6 +4,8 @@ Same names, arguments, return shapes and errors as the public step functions
 of ``gurugram_flood.kernels.triangular_backend``:
 
 * ``step_triangular_surface``              (``triangular_backend.py:478-528``)
+* ``step_triangular_surface_local_inertial`` (``:531-590``)
+* ``stable_local_inertial_triangular_timestep_s`` (``:975-994``)
 * ``step_triangular_dynamic_pipe_network`` (``:665-830``)
 * ``stable_triangular_timestep_s``         (``:955-972``)
 * ``clamp_velocity``                       (``gurugram_flood/solver/stabilizers.py:8-27``)
@@ -83,32 +85,46 @@ def clear_cache() -> None:
 
 
 def _cfg(cfl=0.85, max_speed=5.0, capture_rule="orifice", orifice_area=0.04, orifice_coef=0.62, weir_perimeter=0.0,
-         weir_coef=0.45):
+         weir_coef=0.45, mode="full_swe"):
     return load_config(None, {
         "solver.cfl": cfl, "solver.max_speed_mps": max_speed, "solver.duration_min": 1.0e9,
+        "solver.surface_step_mode": mode,
         "physics.inlet_capture_rule": capture_rule, "physics.inlet_orifice_area_m2": orifice_area,
         "physics.inlet_orifice_coefficient": orifice_coef, "physics.inlet_weir_perimeter_m": weir_perimeter,
         "physics.inlet_weir_coefficient": weir_coef,
     })
 
 
-def _surface_solver(topology, stage, per_cell, cfl=0.85, max_speed=5.0):
+def _surface_solver(topology, stage, per_cell, cfl=0.85, max_speed=5.0, mode="full_swe"):
     def make():
         c = topology.cell_count
         fields = None
         if per_cell:
             ones = np.ones(c, np.float32)
             fields = ProductionInfiltrationFields(ones, ones * 0, ones * 0, ones * 0, ones, ones > 0)
-        return FloodSolver(topology, rainfall=None, infiltration_fields=fields, cfg=_cfg(cfl, max_speed),
+        return FloodSolver(topology, rainfall=None, infiltration_fields=fields, cfg=_cfg(cfl, max_speed, mode=mode),
                            duration_s=1.0e12, boundary_stage_m=stage, max_snapshots=1)
 
-    return _solver([topology], ("surface", stage, per_cell, cfl, max_speed), make)
+    return _solver([topology], ("surface", stage, per_cell, cfl, max_speed, mode), make)
 
 
 def step_triangular_surface(state: TriangularSurfaceState, topology: TriangularSurfaceTopology,
                             forcing: TriangularSurfaceForcing, timestep_s: float):
     """One explicit FV step: fluxes, cell update + Manning, rain, infiltration."""
 
+    return _surface_step(state, topology, forcing, timestep_s, "full_swe")
+
+
+def step_triangular_surface_local_inertial(state: TriangularSurfaceState, topology: TriangularSurfaceTopology,
+                                           forcing: TriangularSurfaceForcing, timestep_s: float):
+    """One local-inertial routing step: face discharges from water-surface
+    slopes, donor-limited volume transfer, momentum from the face discharges,
+    rain and infiltration."""
+
+    return _surface_step(state, topology, forcing, timestep_s, "local_inertial")
+
+
+def _surface_step(state, topology, forcing, timestep_s, mode):
     if timestep_s <= 0.0:
         raise ValueError("timestep_s must be positive.")
     if topology.has_stage_boundary and forcing.boundary_stage_m is None:
@@ -116,7 +132,7 @@ def step_triangular_surface(state: TriangularSurfaceState, topology: TriangularS
     stage = None if forcing.boundary_stage_m is None else float(forcing.boundary_stage_m)
     rain, infil = forcing.rainfall_rate_mps, forcing.infiltration_capacity_mps
     per_cell = np.ndim(rain) > 0 or np.ndim(infil) > 0
-    s = _surface_solver(topology, stage, per_cell)
+    s = _surface_solver(topology, stage, per_cell, mode=mode)
     if per_cell:
         c = topology.cell_count
         r = np.broadcast_to(np.asarray(rain, np.float32), (c,))
@@ -171,6 +187,18 @@ def stable_triangular_timestep_s(topology: TriangularSurfaceTopology, state: Tri
 
     stage = 0.0 if topology.has_stage_boundary else None  # the stage does not enter the CFL dt
     s = _surface_solver(topology, stage, False, cfl=float(cfl))
+    s.set_state(state.h_m, state.hu_m2ps, state.hv_m2ps)
+    return s.stable_timestep()
+
+
+def stable_local_inertial_triangular_timestep_s(topology: TriangularSurfaceTopology, state: TriangularSurfaceState,
+                                                cfl: float = 0.45, gravity_mps2: float = 9.80665,
+                                                min_depth_m: float = 1.0e-5) -> float:
+    """Global dt from the gravity-wave speed only: min over cells of
+    cfl * l / sqrt(g max(h, min_depth))."""
+
+    stage = 0.0 if topology.has_stage_boundary else None
+    s = _surface_solver(topology, stage, False, cfl=float(cfl), mode="local_inertial")
     s.set_state(state.h_m, state.hu_m2ps, state.hv_m2ps)
     return s.stable_timestep()
 

@@ -63,7 +63,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         obj = BUILD / (src.stem + ".o")
         # the drainage kernels evaluate the same request/transfer at several call
         # sites and rely on uncontracted arithmetic for bit-identical results
-        fmad = "-fmad=false" if src.stem == "fl_drainage" else "-fmad=true"
+        fmad = "-fmad=false" if src.stem in ("fl_drainage", "fl_inertial") else "-fmad=true"
         cmd = [nvcc, "-c", str(src), "-o", str(obj), *ARCH, "-O3", "-lineinfo", "-std=c++17", fmad,
                "-Xcompiler", "-fPIC,-fvisibility=hidden", "-Xptxas", "-v" if verbose else "-O3", *inc]
         jobs.append((obj, cmd))

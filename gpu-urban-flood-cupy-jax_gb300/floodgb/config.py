@@ -86,8 +86,9 @@ class RunConfig:
             raise ConfigError(
                 f"production solver is GPU-only; solver.backend must be 'cupy' (or 'floodgb'), got {s.backend!r}"
             )
-        if s.surface_step_mode != "full_swe":
-            raise ConfigError(f"solver.surface_step_mode must be 'full_swe', got {s.surface_step_mode!r}")
+        if s.surface_step_mode not in ("full_swe", "local_inertial"):
+            raise ConfigError(
+                f"solver.surface_step_mode must be 'full_swe' or 'local_inertial', got {s.surface_step_mode!r}")
         if p.infiltration_mode not in ("production_horton", "simple_constant"):
             raise ConfigError(
                 f"physics.infiltration_mode must be 'production_horton' or 'simple_constant', got {p.infiltration_mode!r}"

@@ -67,6 +67,39 @@ class ProductionTopologies:
 
 
 @dataclass
+class ExternalBoundaryInflowSurface:
+    """Hydrographs entering at receiver cells (reference
+    ``gurugram_flood/domain/production_event_support.py:24-29``):
+    ``q_m3ps_by_receiver`` is [times x receivers] float32, ``times_s``
+    strictly increasing float64."""
+
+    receiver_cell_index: np.ndarray
+    times_s: np.ndarray
+    q_m3ps_by_receiver: np.ndarray
+    peak_total_m3ps: float = 0.0
+    report: dict | None = None
+
+
+@dataclass
+class June5RechargeTopology:
+    """Pond / rain-water-harvesting rows (reference
+    ``gurugram_flood/domain/june5_production_drainage.py:99-111``); the
+    recharge step reads the source cell, capacities and stop depth."""
+
+    source_cell_index: np.ndarray
+    overflow_cell_index: np.ndarray
+    storage_capacity_m3: np.ndarray
+    capture_capacity_m3ps: np.ndarray
+    recharge_capacity_m3ps: np.ndarray
+    activation_depth_m: np.ndarray
+    stop_depth_m: np.ndarray
+
+    @property
+    def row_count(self) -> int:
+        return int(np.asarray(self.source_cell_index).size)
+
+
+@dataclass
 class CityDomain:
     topologies: ProductionTopologies
     topology_mode: str

@@ -9,8 +9,10 @@ otherwise, snapshots at the first step whose end time reaches each
 host touches the device only between snapshot intervals (when a progress
 callback is given) or once at the end.
 
-Not supported (raise ``NotImplementedError``): the local-inertial surface
-mode, external boundary inflow and surface recharge.
+External boundary inflow (``city.external_boundary``), surface recharge
+(``city.recharge_topology``), the weighted surcharge-return table and
+``solver.surface_step_mode = "local_inertial"`` all run inside the device
+loop.
 """
 
 from __future__ import annotations
@@ -69,10 +71,6 @@ def snapshot_speed(h: np.ndarray, hu: np.ndarray, hv: np.ndarray) -> np.ndarray:
 def run_simulation(city, rainfall, cfg: RunConfig, progress_callback: ProgressCallback | None = None,
                    device: int = 0) -> SimulationResult:
     s, ph = cfg.solver, cfg.physics
-    if s.surface_step_mode != "full_swe":
-        raise NotImplementedError("only solver.surface_step_mode='full_swe' is implemented")
-    if city.external_boundary is not None or city.recharge_topology is not None:
-        raise NotImplementedError("external boundary inflow and surface recharge are not implemented")
     duration_min = s.duration_min if s.duration_min is not None else rainfall.duration_min
     if duration_min <= 0:
         raise SimulationError(f"Simulation duration must be positive, got {duration_min} min")
@@ -125,9 +123,9 @@ def run_simulation(city, rainfall, cfg: RunConfig, progress_callback: ProgressCa
         "outfall_discharge_m3": led["outfall_discharge_m3"],
         "overflow_surcharge_m3": led["overflow_surcharge_m3"],
         "unreturned_overflow_m3": led["unreturned_overflow_m3"],
-        "external_boundary_inflow_m3": 0.0,
-        "surface_recharge_capture_m3": 0.0,
-        "surface_recharge_loss_m3": 0.0,
+        "external_boundary_inflow_m3": led["external_boundary_inflow_m3"],
+        "surface_recharge_capture_m3": led["surface_recharge_capture_m3"],
+        "surface_recharge_loss_m3": led["surface_recharge_loss_m3"],
     }
     final_surface = float(np.sum(final_h.astype(np.float64) * area))
     final_node = float(final_v.astype(np.float32).astype(np.float64).sum())

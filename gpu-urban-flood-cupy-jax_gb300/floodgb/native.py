@@ -31,7 +31,9 @@ FL_E_TIMEOUT = -9
 FL_PHASE_SURFACE = 1
 FL_PHASE_CLAMP = 2
 FL_PHASE_DRAINAGE = 4
-FL_PHASE_ALL = 7
+FL_PHASE_INFLOW = 8
+FL_PHASE_RECHARGE = 16
+FL_PHASE_ALL = 31
 FL_MEM_HOST = 0
 FL_MEM_DEVICE = 1
 
@@ -40,6 +42,7 @@ LEDGER_NAMES = [
     "rainfall_input_m3", "infiltration_loss_m3", "boundary_inflow_m3", "boundary_outflow_m3",
     "surface_capture_m3", "surface_surcharge_m3", "outfall_discharge_m3", "overflow_surcharge_m3",
     "unreturned_overflow_m3", "link_abs_flow_m3", "surface_volume_m3", "node_volume_m3",
+    "external_boundary_inflow_m3", "surface_recharge_capture_m3", "surface_recharge_loss_m3",
 ]
 
 f32p = C.POINTER(C.c_float)
@@ -76,6 +79,8 @@ class FlDrainDesc(C.Structure):
         ("inlet_capture_rule", C.c_int32),
         ("inlet_orifice_area_m2", C.c_float), ("inlet_orifice_coefficient", C.c_float),
         ("inlet_weir_perimeter_m", C.c_float), ("inlet_weir_coefficient", C.c_float),
+        ("surcharge_entry_count", C.c_int32), ("surcharge_cell_index", i32p), ("surcharge_node_index", i32p),
+        ("surcharge_return_weight", f32p), ("surcharge_return_weight_is_normalized", C.c_int32),
     ]
 
 
@@ -96,7 +101,7 @@ class FlParams(C.Structure):
         ("max_dt_s", C.c_double), ("max_speed_mps", C.c_double),
         ("finite_check_interval_steps", C.c_int32),
         ("duration_s", C.c_double), ("snapshot_interval_s", C.c_double),
-        ("max_snapshots", C.c_int32),
+        ("max_snapshots", C.c_int32), ("surface_step_mode", C.c_int32),
     ]
 
 
@@ -181,6 +186,10 @@ _SIGNATURES = {
     "fl_batch_read_ledger": (C.c_int, [C.c_void_p, C.c_int32, f64p, C.c_int32, C.c_void_p]),
     "fl_batch_info": (C.c_int, [C.c_void_p, C.POINTER(FlBatchShape), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 i32p]),
+    "fl_set_boundary_inflow": (C.c_int, [C.c_void_p, C.c_int32, i32p, C.c_int32, f64p, f32p]),
+    "fl_set_recharge": (C.c_int, [C.c_void_p, C.c_int32, i32p, f32p, f32p, f32p, f32p]),
+    "fl_get_recharge_storage": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "fl_set_recharge_storage": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
     "fl_stable_timestep_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
                                              C.c_double, C.c_double, C.c_void_p, C.c_void_p]),
 }
@@ -292,13 +301,10 @@ def mesh_desc(topo, keep: Keep, centroids=None, boundary_stage_m=None) -> FlMesh
 
 def drain_desc(coupling, pipe, keep: Keep, capture_rule="orifice", orifice_area=0.04, orifice_coef=0.62,
                weir_perimeter=0.0, weir_coef=0.45) -> FlDrainDesc:
-    if (coupling.surcharge_cell_index is not None or coupling.surcharge_node_index is not None
-            or coupling.surcharge_return_weight is not None):
-        raise NotImplementedError("the weighted surcharge-return table path is not implemented")
     if capture_rule not in CAPTURE_RULES:
         raise ValueError("inlet_capture_rule must be 'orifice', 'weir_orifice', 'capacity', or 'head_limited_capacity'.")
     rect = pipe.link_geometry_code is not None and pipe.link_rect_width_m is not None and pipe.link_rect_height_m is not None
-    return FlDrainDesc(
+    d = FlDrainDesc(
         node_count=coupling.node_count, link_count=pipe.link_count, inlet_count=coupling.inlet_count,
         inlet_cell_index=keep.i32(coupling.inlet_cell_index), inlet_node_index=keep.i32(coupling.inlet_node_index),
         node_surface_cell_index=keep.i32(coupling.node_surface_cell_index),
@@ -325,6 +331,18 @@ def drain_desc(coupling, pipe, keep: Keep, capture_rule="orifice", orifice_area=
         inlet_orifice_area_m2=float(orifice_area), inlet_orifice_coefficient=float(orifice_coef),
         inlet_weir_perimeter_m=float(weir_perimeter), inlet_weir_coefficient=float(weir_coef),
     )
+    # the weighted return table is used when all three arrays are given (reference :1424-1428)
+    sc, sn, sw = coupling.surcharge_cell_index, coupling.surcharge_node_index, coupling.surcharge_return_weight
+    if sc is not None and sn is not None and sw is not None:
+        n = int(np.asarray(sc).size)
+        if np.asarray(sn).size != n or np.asarray(sw).size != n:
+            raise ValueError("surcharge_cell_index, surcharge_node_index and surcharge_return_weight differ in length")
+        d.surcharge_entry_count = n
+        d.surcharge_cell_index = keep.i32(sc)
+        d.surcharge_node_index = keep.i32(sn)
+        d.surcharge_return_weight = keep.f32(sw)
+        d.surcharge_return_weight_is_normalized = int(bool(coupling.surcharge_return_weight_is_normalized))
+    return d
 
 
 def plan_check(topo, coupling=None, pipe=None, centroids=None):

@@ -107,6 +107,7 @@ def build_descriptors(surface_topology, coupling_topology=None, pipe_topology=No
         cfl_reuse_safety_factor=s.cfl_reuse_safety_factor, max_dt_s=s.max_dt_s, max_speed_mps=s.max_speed_mps,
         finite_check_interval_steps=int(s.finite_check_interval_steps), duration_s=duration_s,
         snapshot_interval_s=s.snapshot_interval_min * 60.0, max_snapshots=int(max_snapshots),
+        surface_step_mode=1 if s.surface_step_mode == "local_inertial" else 0,
     )
     return Descriptors(mesh, drain, forcing, params, keep, duration_s, int(max_snapshots), kind)
 
@@ -246,6 +247,56 @@ class FloodSolver:
                                          float(np.float32(infiltration_mps)))
         N.check(rc, "fl_update_forcing")
 
+    # ------------------------------------------------- inflow and recharge
+    def set_boundary_inflow(self, external) -> None:
+        """External boundary inflow from an ExternalBoundaryInflowSurface
+        (receiver_cell_index, times_s, q_m3ps_by_receiver [times x receivers]);
+        None removes it.  Reference production_event_support.py:169-196."""
+
+        keep = N.Keep()
+        if external is None or np.asarray(external.receiver_cell_index).size == 0:
+            rc = self._lib.fl_set_boundary_inflow(self._h, 0, None, 0, None, None)
+        else:
+            cells = np.asarray(external.receiver_cell_index, np.int32)
+            times = np.asarray(external.times_s, np.float64)
+            q = np.asarray(external.q_m3ps_by_receiver, np.float32)
+            if q.shape != (times.size, cells.size):
+                raise ValueError(f"q_m3ps_by_receiver has shape {q.shape}, expected {(times.size, cells.size)}")
+            rc = self._lib.fl_set_boundary_inflow(self._h, cells.size, keep.i32(cells), times.size, keep.f64(times),
+                                                  keep.f32(q))
+        N.check(rc, "fl_set_boundary_inflow")
+        self.inflow_receivers = 0 if external is None else int(np.asarray(external.receiver_cell_index).size)
+
+    def set_recharge(self, topo) -> None:
+        """Surface recharge rows from a June5RechargeTopology (float32 rows);
+        None removes it.  Reference june5_production_drainage.py:543-572."""
+
+        keep = N.Keep()
+        n = 0 if topo is None else int(np.asarray(topo.source_cell_index).size)
+        if n == 0:
+            rc = self._lib.fl_set_recharge(self._h, 0, None, None, None, None, None)
+        else:
+            rc = self._lib.fl_set_recharge(self._h, n, keep.i32(topo.source_cell_index),
+                                           keep.f32(topo.storage_capacity_m3), keep.f32(topo.capture_capacity_m3ps),
+                                           keep.f32(topo.recharge_capacity_m3ps), keep.f32(topo.stop_depth_m))
+        N.check(rc, "fl_set_recharge")
+        self.recharge_rows = n
+
+    def recharge_storage(self, stream=None) -> np.ndarray:
+        n = getattr(self, "recharge_rows", 0)
+        out = np.zeros(n, np.float32)
+        if n:
+            rc = self._lib.fl_get_recharge_storage(self._h, C.c_void_p(out.ctypes.data), n, N.FL_MEM_HOST,
+                                                   _stream_handle(stream))
+            N.check(rc, "fl_get_recharge_storage")
+        return out
+
+    def set_recharge_storage(self, storage, stream=None) -> None:
+        a = np.ascontiguousarray(storage, np.float32)
+        rc = self._lib.fl_set_recharge_storage(self._h, C.c_void_p(a.ctypes.data), a.size, N.FL_MEM_HOST,
+                                               _stream_handle(stream))
+        N.check(rc, "fl_set_recharge_storage")
+
     # ------------------------------------------------------------- stepping
     def reset_clock(self, stream=None):
         N.check(self._lib.fl_reset_clock(self._h, _stream_handle(stream)), "fl_reset_clock")
@@ -316,5 +367,9 @@ def solver_for_city(city, rainfall, cfg: RunConfig, duration_s: float | None = N
     s.set_state(topo.surface_state.h_m, topo.surface_state.hu_m2ps, topo.surface_state.hv_m2ps,
                 topo.pipe_state.node_volume_m3 if s.node_count else None,
                 topo.pipe_state.link_flow_m3ps if s.link_count else None)
+    if getattr(city, "external_boundary", None) is not None:
+        s.set_boundary_inflow(city.external_boundary)
+    if getattr(city, "recharge_topology", None) is not None:
+        s.set_recharge(city.recharge_topology)
     s.reset_clock()
     return s

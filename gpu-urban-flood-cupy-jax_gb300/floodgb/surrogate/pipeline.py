@@ -230,8 +230,11 @@ def rollout_batch(model: MPNN, mf: MeshFeatures, storms, durations_s, copies: in
 
     out = [None] * len(storms)
     graphs = {}
+    # members of one forward pass run for the longest one's windows: group
+    # members of equal window count so few passes are padding
+    order = sorted(range(len(storms)), key=lambda i: (len(windows(durations_s[i])), i))
     for k0 in range(0, len(storms), copies):
-        idx = list(range(k0, min(len(storms), k0 + copies)))
+        idx = order[k0:k0 + copies]
         B = len(idx)
         if B not in graphs:
             graphs[B] = mf.graph.replicate(B)

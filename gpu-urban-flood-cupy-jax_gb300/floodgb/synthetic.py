@@ -424,6 +424,94 @@ def _drainage(rng, pts, tri, cen, bed, active, road, n_nodes, n_links, n_inlets,
 
 
 # ---------------------------------------------------------------------------
+# external boundary inflow and surface recharge
+# ---------------------------------------------------------------------------
+
+def add_boundary_forcing(sc: Scenario, n_receivers: int = 6, n_recharge: int = 40, seed: int = 0,
+                         peak_m3ps: float = 2.0, step_s: float = 300.0) -> Scenario:
+    """Seeded external inflow and recharge rows on a scenario's city.
+
+    Receivers sit on active cells nearest the upstream (low-x) edge, two of
+    them on one cell; each hydrograph is triangular with a random peak up to
+    ``peak_m3ps`` at ``step_s`` spacing over the run (plus one step).
+    Recharge rows sit on random active cells (two rows share a cell), with
+    storage 5-500 m^3, capture 0.01-0.5 m^3/s, recharge 0.001-0.05 m^3/s,
+    stop depth 1-5 cm and activation depth 5 cm (the reference's default).
+    """
+
+    from .domain import ExternalBoundaryInflowSurface, June5RechargeTopology
+
+    rng = np.random.default_rng(seed)
+    mesh = sc.city.mesh
+    active = np.flatnonzero(np.asarray(mesh.active_mask, bool))
+    dur_s = float(sc.overrides.get("solver.duration_min") or sc.rainfall.duration_min) * 60.0
+    if n_receivers > 0:
+        x = np.asarray(mesh.centroids_xy)[active, 0]
+        near = active[np.argsort(x, kind="stable")[: max(4 * n_receivers, 8)]]
+        cells = rng.choice(near, size=n_receivers, replace=False).astype(np.int32)
+        if n_receivers > 1:
+            cells[1] = cells[0]
+        times = np.arange(0.0, dur_s + 2 * step_s, step_s)
+        q = np.zeros((times.size, n_receivers), np.float32)
+        for j in range(n_receivers):
+            peak = rng.uniform(0.1, 1.0) * peak_m3ps
+            tp = rng.uniform(0.2, 0.6) * dur_s
+            shape = np.where(times <= tp, times / max(tp, 1.0), np.maximum(0.0, 1.0 - (times - tp) / max(dur_s - tp, 1.0)))
+            q[:, j] = (peak * shape).astype(np.float32)
+        sc.city.external_boundary = ExternalBoundaryInflowSurface(
+            receiver_cell_index=cells, times_s=times.astype(np.float64), q_m3ps_by_receiver=q,
+            peak_total_m3ps=float(q.sum(axis=1).max()))
+    if n_recharge > 0:
+        cells = rng.choice(active, size=n_recharge, replace=False).astype(np.int32)
+        if n_recharge > 2:
+            cells[2] = cells[1]
+        sc.city.recharge_topology = June5RechargeTopology(
+            source_cell_index=cells, overflow_cell_index=cells.copy(),
+            storage_capacity_m3=rng.uniform(5.0, 500.0, n_recharge).astype(np.float32),
+            capture_capacity_m3ps=rng.uniform(0.01, 0.5, n_recharge).astype(np.float32),
+            recharge_capacity_m3ps=rng.uniform(0.001, 0.05, n_recharge).astype(np.float32),
+            activation_depth_m=np.full(n_recharge, 0.05, np.float32),
+            stop_depth_m=rng.uniform(0.01, 0.05, n_recharge).astype(np.float32))
+    return sc
+
+
+def add_surcharge_table(sc: Scenario, frac: float = 0.6, seed: int = 0, normalized: bool = False) -> Scenario:
+    """A seeded weighted surcharge-return table on a coupled scenario: ``frac``
+    of the nodes get one to three entries on active cells near their own
+    surface cell (weights U(0, 2), normalized per node if asked); the other
+    nodes keep the per-node return to their cell."""
+
+    from .topology import TriangularNodeCouplingTopology
+
+    rng = np.random.default_rng(seed)
+    topo = sc.city.topologies
+    cp = topo.coupling_topology
+    mesh = sc.city.mesh
+    active = np.flatnonzero(np.asarray(mesh.active_mask, bool))
+    cen = np.asarray(mesh.centroids_xy)
+    nodes = np.sort(rng.choice(cp.node_count, size=int(frac * cp.node_count), replace=False))
+    cells, owner, weight = [], [], []
+    for n in nodes:
+        c0 = int(cp.node_surface_cell_index[n])
+        if c0 < 0:
+            continue
+        d2 = np.sum((cen[active] - cen[c0]) ** 2, axis=1)
+        near = active[np.argsort(d2)[:8]]
+        k = int(rng.integers(1, 4))
+        w = rng.uniform(0.0, 2.0, k)
+        if normalized:
+            w = w / w.sum()
+        cells.extend(rng.choice(near, size=k, replace=False).tolist())
+        owner.extend([int(n)] * k)
+        weight.extend(w.tolist())
+    topo.coupling_topology = TriangularNodeCouplingTopology(**{
+        **cp.__dict__, "surcharge_cell_index": np.array(cells, np.int32),
+        "surcharge_node_index": np.array(owner, np.int32), "surcharge_return_weight": np.array(weight, np.float32),
+        "surcharge_return_weight_is_normalized": normalized})
+    return sc
+
+
+# ---------------------------------------------------------------------------
 # named workloads
 # ---------------------------------------------------------------------------
 

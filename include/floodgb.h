@@ -45,7 +45,9 @@ enum {
     FL_PHASE_SURFACE = 1,  /* fluxes, cell update + Manning, rain and infiltration */
     FL_PHASE_CLAMP = 2,    /* velocity clamp */
     FL_PHASE_DRAINAGE = 4, /* inlet exchange, links, outfalls, overflow return */
-    FL_PHASE_ALL = 7
+    FL_PHASE_INFLOW = 8,   /* external boundary inflow (after the clamp) */
+    FL_PHASE_RECHARGE = 16, /* surface recharge capture (after the drainage) */
+    FL_PHASE_ALL = 31
 };
 
 /* Memory kind of caller buffers in state / snapshot transfers. */
@@ -86,6 +88,15 @@ typedef struct {
     float pressurized_wave_speed_mps;
     int32_t inlet_capture_rule;
     float inlet_orifice_area_m2, inlet_orifice_coefficient, inlet_weir_perimeter_m, inlet_weir_coefficient;
+    /* Weighted surcharge-return table (surcharge_cell_index / _node_index /
+     * _return_weight / _return_weight_is_normalized, used when all three
+     * arrays are given: triangular_backend.py:1424-1474).  Entries with a
+     * negative node or cell are ignored; entry_count 0 = the per-node return
+     * to node_surface_cell_index. */
+    int32_t surcharge_entry_count;
+    const int32_t *surcharge_cell_index, *surcharge_node_index;
+    const float *surcharge_return_weight;
+    int32_t surcharge_return_weight_is_normalized;
 } FlDrainDesc;
 
 /* Forcing: kind 0 = uniform (scalar rain from the hyetograph, scalar
@@ -110,6 +121,10 @@ typedef struct {
     int32_t finite_check_interval_steps;
     double duration_s, snapshot_interval_s;
     int32_t max_snapshots;
+    /* 0: full_swe (step_triangular_surface); 1: local_inertial
+     * (step_triangular_surface_local_inertial, triangular_backend.py:531-590,
+     * with stable_local_inertial_triangular_timestep_s, :975-994). */
+    int32_t surface_step_mode;
 } FlParams;
 
 typedef struct {
@@ -136,6 +151,9 @@ enum {
     FL_LEDGER_LINK_ABS,
     FL_LEDGER_SURFACE_VOLUME, /* current sum(h * area) */
     FL_LEDGER_NODE_VOLUME,    /* current sum(node volume) */
+    FL_LEDGER_EXTERNAL_INFLOW,  /* external_boundary_inflow_m3 */
+    FL_LEDGER_RECHARGE_CAPTURE, /* surface_recharge_capture_m3 */
+    FL_LEDGER_RECHARGE_LOSS,    /* surface_recharge_loss_m3 */
     FL_LEDGER_COUNT
 };
 
@@ -166,8 +184,9 @@ FL_API int fl_set_state(FlSolver *solver, const float *h, const float *hu, const
 FL_API int fl_get_state(FlSolver *solver, float *h, float *hu, float *hv, double *node_volume,
                         double *link_flow, float *wet_time, int32_t mem, void *stream);
 
-/* Rewind the clock: t = 0, no cached CFL dt, ledger, snapshots and Horton
- * wet time cleared (the start of run_simulation's loop, engine.py:186-215). */
+/* Rewind the clock: t = 0, no cached CFL dt, ledger, snapshots, Horton wet
+ * time and recharge storage cleared (the start of run_simulation's loop,
+ * engine.py:165-215). */
 FL_API int fl_reset_clock(FlSolver *solver, void *stream);
 
 /* Advance the adaptive loop of run_simulation (engine.py:219-344) until the
@@ -179,7 +198,9 @@ FL_API int fl_run(FlSolver *solver, double t_target_s, int64_t max_steps, void *
 /* One step with an explicit dt and a phase set: step_triangular_surface
  * (triangular_backend.py:478-528) for FL_PHASE_SURFACE, clamp_velocity
  * (stabilizers.py:8-27) for FL_PHASE_CLAMP, step_triangular_dynamic_pipe_network
- * (triangular_backend.py:665-830) for FL_PHASE_DRAINAGE.  rain_rate_mps is
+ * (triangular_backend.py:665-830) for FL_PHASE_DRAINAGE, the external
+ * boundary inflow at the step's mid time for FL_PHASE_INFLOW and the surface
+ * recharge for FL_PHASE_RECHARGE (engine.py:263-289).  rain_rate_mps is
  * the base rainfall rate for the step (multiplied per cell in kind 1). */
 FL_API int fl_step(FlSolver *solver, double dt_s, int32_t phases, double rain_rate_mps, void *stream);
 
@@ -198,6 +219,34 @@ FL_API int fl_get_progress(FlSolver *solver, FlProgress *out, void *stream);
 
 /* Cumulative ledger, FL_LEDGER_COUNT doubles (n may be smaller). */
 FL_API int fl_read_ledger(FlSolver *solver, double *out, int32_t n, void *stream);
+
+/* External boundary inflow: ExternalBoundaryInflowSurface
+ * (gurugram_flood/domain/production_event_support.py:24-29), applied every
+ * step after the velocity clamp as apply_external_boundary_inflow_depth
+ * (:169-196): q_j at t + dt/2 by linear interpolation of the hydrograph
+ * (held at the first / last value outside it), h += sum_j float32(q_j) * dt
+ * / area over the receivers of each cell.  receiver_cell_index: reference
+ * cell order, active cells only; times_s strictly increasing; q_m3ps is
+ * [time_count x receiver_count] row-major.  receiver_count 0 removes it.
+ * Host pointers; takes effect from the next step. */
+FL_API int fl_set_boundary_inflow(FlSolver *solver, int32_t receiver_count, const int32_t *receiver_cell_index,
+                                  int32_t time_count, const double *times_s, const float *q_m3ps);
+
+/* Surface recharge: June5RechargeTopology
+ * (gurugram_flood/domain/june5_production_drainage.py:99-111), applied every
+ * step after the drainage step as apply_june5_surface_recharge (:543-572):
+ * capture = min(removable depth above stop_depth x area, capture capacity x
+ * dt, remaining storage), then a recharge loss of min(storage, recharge
+ * capacity x dt).  Rows sharing a cell all see the same depth and the last
+ * row's capture sets it (the reference's NumPy assignment).  row_count 0
+ * removes it.  Host pointers; the stored volumes start at zero. */
+FL_API int fl_set_recharge(FlSolver *solver, int32_t row_count, const int32_t *source_cell_index,
+                           const float *storage_capacity_m3, const float *capture_capacity_m3ps,
+                           const float *recharge_capacity_m3ps, const float *stop_depth_m);
+
+/* Stored recharge volume per row (float32, row order), read or replaced. */
+FL_API int fl_get_recharge_storage(FlSolver *solver, float *storage_m3, int32_t n, int32_t mem, void *stream);
+FL_API int fl_set_recharge_storage(FlSolver *solver, const float *storage_m3, int32_t n, int32_t mem, void *stream);
 
 /* Snapshots [first, first+count) of depth, hu, hv (count x cell_count, reference
  * order) and node volume (count x node_count, float32 as engine.py:321 stores

@@ -200,6 +200,133 @@ int orc_surface_step(const OrcMesh *m, const float *h, const float *hu, const fl
     return 0;
 }
 
+/* Local-inertial surface step: the reference's fused CUDA path
+ * (triangular_local_inertial_cuda_kernels.py:59-262: edge discharge, donor
+ * scale, cell gather) then _apply_sources (triangular_backend.py:1330-1379).
+ * The donor request of a cell is summed over its cell_edges slots in order
+ * (the reference adds them with atomicAdd in an unspecified order). */
+int orc_li_step(const OrcMesh *m, const float *h, const float *hu, const float *hv, const OrcForcing *f, double dt,
+                double g_d, float md, float *h_out, float *hu_out, float *hv_out, double *diag) {
+    const int C = m->cell_count, E = m->edge_count;
+    const float dtf = (float)dt, g = (float)g_d;
+    float *Q = (float *)malloc(sizeof(float) * (size_t)(E > 0 ? E : 1));
+    float *scale = (float *)malloc(sizeof(float) * (size_t)(C > 0 ? C : 1));
+    if (!Q || !scale) { free(Q); free(scale); return -1; }
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < E; ++e) {
+        const int L = m->left[e], R0 = m->right[e];
+        const int interior = R0 >= 0, R = interior ? R0 : L;
+        const int la = m->active ? m->active[L] > 0.5f : 1, ra = m->active ? m->active[R] > 0.5f : 1;
+        const int ai = interior && la && ra;
+        const int code = (interior && la && !ra) ? 0 : m->bcode[e];
+        const float hl = la ? h[L] : 0.0f, hul = la ? hu[L] : 0.0f, hvl = la ? hv[L] : 0.0f;
+        const float hr = ra ? h[R] : 0.0f, hur = ra ? hu[R] : 0.0f, hvr = ra ? hv[R] : 0.0f;
+        const float bl = m->bed[L], br = m->bed[R];
+        const float etal = bl + hl;
+        const float etar = ai ? br + hr : bl;
+        const float bstar = ai ? fmax32(bl, br) : bl;
+        const float hflow = fmax32(fmax32(etal, etar) - bstar, 0.0f);
+        const float dist = fmax32(0.5f * (m->char_len[L] + m->char_len[R]), 1.0e-6f);
+        const float slope = (etar - etal) / dist;
+        const float nx = m->nx[e], ny = m->ny[e], len = m->len[e];
+        const float nl = hul * nx + hvl * ny, nr = hur * nx + hvr * ny;
+        const float qold = (ai ? 0.5f * (nl + nr) : nl) * len;
+        const float mn = ai ? 0.5f * (m->manning[L] + m->manning[R]) : m->manning[L];
+        const int bedge = !interior && la && (code == 1 || code == 4);
+        const float area = fmax32(hflow * len, 1.0e-8f);
+        const float radius = fmax32(hflow, 1.0e-6f);
+        const float r43 = radius * cbrtf(radius);
+        const float numer = qold - g * area * dtf * slope;
+        const float fric = 1.0f + g * dtf * mn * mn * fabsf(qold) / (r43 * area);
+        float q = numer / fric;
+        if (!(ai || bedge)) q = 0.0f;
+        if (bedge) q = fmax32(q, 0.0f);
+        Q[e] = q;
+    }
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < C; ++c) {
+        float req = 0.0f;
+        for (int s = 0; s < 3; ++s) {
+            const int e = m->cell_edges[3 * (size_t)c + s];
+            if (e < 0 || m->right[e] < 0) continue;
+            const int L = m->left[e], R = m->right[e];
+            const int ai = m->active ? (m->active[L] > 0.5f && m->active[R] > 0.5f) : 1;
+            const float q = Q[e];
+            if (!ai || q == 0.0f) continue;
+            if ((q >= 0.0f ? L : R) == c) req += fabsf(q) * dtf;
+        }
+        const float vol = fmax32(h[c], 0.0f) * m->area[c];
+        scale[c] = req > 1.0e-12f ? fmin32(1.0f, vol / req) : 1.0f;
+    }
+    double rain_m3 = 0.0, infil_m3 = 0.0, bout = 0.0, vtot = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rain_m3, infil_m3, bout, vtot)
+    for (int c = 0; c < C; ++c) {
+        const int act = m->active ? m->active[c] > 0.5f : 1;
+        if (!act) { h_out[c] = hu_out[c] = hv_out[c] = 0.0f; continue; }
+        float hd = 0.0f, hs = 0.0f, vs = 0.0f, bf = 0.0f;
+        for (int s = 0; s < 3; ++s) {
+            const int e = m->cell_edges[3 * (size_t)c + s];
+            if (e < 0) continue;
+            const float q = Q[e];
+            if (q == 0.0f) continue;
+            if (m->right[e] >= 0) {
+                const int donor = q >= 0.0f ? m->left[e] : m->right[e];
+                const float lim = q * scale[donor] * dtf;
+                hd += (c == m->left[e]) ? -lim : lim;
+            } else {
+                const float b = q * dtf;
+                hd -= b;
+                bf += b;
+            }
+            hs += q * m->nx[e];
+            vs += q * m->ny[e];
+        }
+        const float area = m->area[c];
+        const float hn = fmax32(h[c] + hd / area, 0.0f);
+        const float per = 2.0f * area / fmax32(m->char_len[c], 1.0e-12f);
+        const int wet = hn > md;
+        float hun = wet ? hs / fmax32(per, 1.0e-12f) : 0.0f;
+        float hvn = wet ? vs / fmax32(per, 1.0e-12f) : 0.0f;
+        /* _apply_sources */
+        const float rain = f->rain_kind ? f->rain_cell[c] : f->rain_scalar;
+        const float infc = f->infil_kind ? f->infil_cell[c] : f->infil_scalar;
+        const float rd = fmax32(rain, 0.0f) * dtf;
+        const float h1 = hn + rd;
+        const float id = fmin32(h1, fmax32(infc, 0.0f) * dtf);
+        const float h2 = h1 - id;
+        const float sc = (h1 > md) ? h2 / fmax32(h1, md) : 0.0f;
+        hun = hun * sc;
+        hvn = hvn * sc;
+        const int wet2 = h2 > md;
+        h_out[c] = h2;
+        hu_out[c] = wet2 ? hun : 0.0f;
+        hv_out[c] = wet2 ? hvn : 0.0f;
+        rain_m3 += (double)(rd * area);
+        infil_m3 += (double)(id * area);
+        bout += (double)bf;
+        vtot += (double)(h2 * area);
+    }
+    free(Q);
+    free(scale);
+    if (diag) {
+        diag[0] = rain_m3; diag[1] = infil_m3; diag[2] = -bout;
+        diag[3] = 0.0; diag[4] = bout; diag[5] = vtot;
+    }
+    return 0;
+}
+
+/* stable_local_inertial_timestep_s (equations.py:181-210): gravity-wave
+ * speed only, float32 per cell; the global min as a double, < 0 if none. */
+double orc_li_stable_dt(int32_t n, const float *cl, const float *h, float cfl, float g, float md) {
+    float best = INFINITY;
+    for (int i = 0; i < n; ++i) {
+        const float c = sqrtf(g * fmax32(h[i], md));
+        const float d = cfl * cl[i] / fmax32(c, 1.0e-12f);
+        if (isfinite(d) && d < best) best = d;
+    }
+    return isfinite(best) ? (double)best : -1.0;
+}
+
 void orc_clamp_velocity(int32_t n, const float *h, float *hu, float *hv, float vmax) {
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
@@ -227,6 +354,65 @@ double orc_stable_dt(int32_t n, const float *cl, const float *h, const float *hu
 /* ---------------------------------------------------------------- drainage */
 
 static inline double dsign(double x) { return (double)((x > 0.0) - (x < 0.0)); }
+
+/* Weighted surcharge return (triangular_backend.py:1424-1474), the NumPy
+ * path's float64 arithmetic: overflow above the float32 capacity product;
+ * each valid entry (node >= 0, cell >= 0) returns overflow x weight (weights
+ * clipped at 0 and, unless already normalized, divided by their float32
+ * per-node sum in entry order) to its cell; a node returns at most its
+ * overflow; nodes without a valid entry return their residual overflow to
+ * their node_surface_cell.  h = float32((h + sum over entries) + sum over
+ * fallbacks), the per-cell sums formed in entry / node order first.
+ * Returns the returned volume. */
+static double weighted_overflow_return(const OrcMesh *m, const OrcDrain *d, float *h, double *V) {
+    const int N = d->node_count, C = m->cell_count, E = d->sur_count;
+    double *ovf = (double *)calloc((size_t)N, sizeof(double));
+    double *cap = (double *)calloc((size_t)N, sizeof(double));
+    double *by_node = (double *)calloc((size_t)N, sizeof(double));
+    double *s1 = (double *)calloc((size_t)C, sizeof(double));
+    double *s2 = (double *)calloc((size_t)C, sizeof(double));
+    float *wsum = (float *)calloc((size_t)N, sizeof(float));
+    char *expl = (char *)calloc((size_t)N, 1);
+    if (!ovf || !cap || !by_node || !s1 || !s2 || !wsum || !expl) return 0.0;
+    for (int n = 0; n < N; ++n) {
+        cap[n] = (double)(d->node_area[n] * fmax32(d->node_maxdepth[n], 0.0f));
+        ovf[n] = fmax(V[n] - cap[n], 0.0);
+    }
+    for (int e = 0; e < E; ++e) {
+        const int n = d->sur_node[e], c = d->sur_cell[e];
+        const int valid = n >= 0 && c >= 0;
+        const float raw = valid ? fmax32(d->sur_weight[e], 0.0f) : 0.0f;
+        wsum[valid ? n : 0] += raw;
+        if (valid) expl[n] = 1;
+    }
+    for (int e = 0; e < E; ++e) {
+        const int n = d->sur_node[e], c = d->sur_cell[e];
+        const int valid = n >= 0 && c >= 0;
+        const int sn = valid ? n : 0, sc = valid ? c : 0;
+        const float raw = valid ? fmax32(d->sur_weight[e], 0.0f) : 0.0f;
+        const float w = d->sur_normalized ? raw : (valid ? raw / fmax32(wsum[sn], 1.0e-12f) : 0.0f);
+        const double ret = ovf[sn] * (double)w;
+        s1[sc] += ret / (double)m->area[sc];
+        by_node[sn] += ret;
+    }
+    double total = 0.0;
+    for (int n = 0; n < N; ++n) {
+        const double r = fmin(by_node[n], ovf[n]);
+        V[n] = V[n] - r;
+        total += r;
+    }
+    for (int n = 0; n < N; ++n) {
+        const int c = d->node_cell[n];
+        const int fb = !expl[n] && c >= 0;
+        const double r = fb ? fmax(V[n] - cap[n], 0.0) : 0.0;
+        s2[fb ? c : 0] += r / (double)m->area[fb ? c : 0];
+        V[n] = V[n] - r;
+        total += r;
+    }
+    for (int c = 0; c < C; ++c) h[c] = (float)(((double)h[c] + s1[c]) + s2[c]);
+    free(ovf); free(cap); free(by_node); free(s1); free(s2); free(wsum); free(expl);
+    return total;
+}
 
 int orc_pipe_step(const OrcMesh *m, const OrcDrain *d, float *h, double *V, double *Q, double dt,
                   float g, double *diag) {
@@ -389,16 +575,20 @@ int orc_pipe_step(const OrcMesh *m, const OrcDrain *d, float *h, double *V, doub
             V[n] = vol - out;
             out_sum += out;
         }
-        for (int n = 0; n < N; ++n) {
-            double capv = (double)d->node_area[n] * (double)fmax32(d->node_maxdepth[n], 0.0f);
-            double ovf = fmax(V[n] - capv, 0.0);
-            int c = d->node_cell[n];
-            double ret = c >= 0 ? ovf : 0.0;
-            if (c >= 0) hd[c] += (float)(ret / (double)m->area[c]);
-            V[n] = V[n] - ret;
-            ovf_sum += ret;
+        if (d->sur_count > 0) {
+            ovf_sum = weighted_overflow_return(m, d, h, V);
+        } else {
+            for (int n = 0; n < N; ++n) {
+                double capv = (double)d->node_area[n] * (double)fmax32(d->node_maxdepth[n], 0.0f);
+                double ovf = fmax(V[n] - capv, 0.0);
+                int c = d->node_cell[n];
+                double ret = c >= 0 ? ovf : 0.0;
+                if (c >= 0) hd[c] += (float)(ret / (double)m->area[c]);
+                V[n] = V[n] - ret;
+                ovf_sum += ret;
+            }
+            for (int c = 0; c < C; ++c) h[c] = h[c] + hd[c];
         }
-        for (int c = 0; c < C; ++c) h[c] = h[c] + hd[c];
         free(hd);
         for (int n = 0; n < N; ++n) {
             float capf = d->node_area[n] * fmax32(d->node_maxdepth[n], 0.0f);
@@ -414,6 +604,69 @@ int orc_pipe_step(const OrcMesh *m, const OrcDrain *d, float *h, double *V, doub
 }
 
 /* ---------------------------------------------------------------- run loop */
+
+float orc_inflow_q(const OrcInflow *x, int32_t j, double t) {
+    const int T = x->time_count, J = x->receiver_count;
+    if (t <= x->times_s[0]) return x->q_m3ps[j];
+    if (t >= x->times_s[T - 1]) return x->q_m3ps[(size_t)(T - 1) * J + j];
+    int lo = 0, hi = T - 1; /* times[lo] < t < times[hi] */
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (x->times_s[mid] <= t) lo = mid; else hi = mid;
+    }
+    const double x0 = x->times_s[lo], x1 = x->times_s[lo + 1];
+    const double y0 = x->q_m3ps[(size_t)lo * J + j], y1 = x->q_m3ps[(size_t)(lo + 1) * J + j];
+    if (x0 == t) return (float)y0;
+    /* np.interp: slope over the interval, the other end's form on NaN */
+    const double slope = (y1 - y0) / (x1 - x0);
+    double r = slope * (t - x0) + y0;
+    if (isnan(r)) {
+        r = slope * (t - x1) + y1;
+        if (isnan(r) && y0 == y1) r = y0;
+    }
+    return (float)r;
+}
+
+double orc_external_inflow(int32_t C, const float *area, const OrcInflow *x, double time_s, double dt, float *h) {
+    float *add = (float *)calloc((size_t)C, sizeof(float));
+    if (!add) return 0.0;
+    const float dtf = (float)dt;
+    double total = 0.0;
+    for (int j = 0; j < x->receiver_count; ++j) {
+        const int c = x->receiver_cell[j];
+        const float added = orc_inflow_q(x, j, time_s) * dtf;
+        add[c] = add[c] + added / area[c];
+        total += (double)added;
+    }
+    for (int c = 0; c < C; ++c) h[c] = h[c] + add[c];
+    free(add);
+    return total;
+}
+
+void orc_recharge(const OrcRecharge *r, const float *area_all, double dt, float *h, float *storage, double *diag) {
+    const int R = r->row_count;
+    const float dtf = (float)dt;
+    float *hin = (float *)malloc(sizeof(float) * (size_t)(R > 0 ? R : 1));
+    if (!hin) return;
+    for (int k = 0; k < R; ++k) hin[k] = h[r->source_cell[k]]; /* every row sees the incoming depth */
+    diag[0] = diag[1] = 0.0;
+    for (int k = 0; k < R; ++k) {
+        const int c = r->source_cell[k];
+        const float area = fmax32(area_all[c], 1.0e-6f);
+        const float removable = fmax32(hin[k] - r->stop_depth[k], 0.0f);
+        const float available = removable * area;
+        const float request = r->capture_capacity[k] * dtf;
+        const float remaining = fmax32(r->storage_capacity[k] - storage[k], 0.0f);
+        const float capture = fmin32(fmin32(available, request), remaining);
+        h[c] = fmax32(hin[k] - capture / area, 0.0f); /* the last row of a cell sets it */
+        float st = storage[k] + capture;
+        const float loss = fmin32(st, r->recharge_capacity[k] * dtf);
+        storage[k] = st - loss;
+        diag[0] += (double)capture;
+        diag[1] += (double)loss;
+    }
+    free(hin);
+}
 
 static double hyeto_rate(const OrcRunParams *p, double t) {
     /* idx = searchsorted(end_s, t, side="right") */
@@ -446,7 +699,8 @@ int orc_run(const OrcMesh *m, const OrcDrain *d, const OrcRunParams *p, float *h
         if (p->max_steps > 0 && step >= p->max_steps) break;
         double dt;
         if (cached < 0.0 || step % p->cfl_interval == 0) {
-            dt = orc_stable_dt(C, m->char_len, h, hu, hv, (float)p->cfl, (float)p->g, p->min_depth);
+            dt = p->local_inertial ? orc_li_stable_dt(C, m->char_len, h, (float)p->cfl, (float)p->g, p->min_depth)
+                                   : orc_stable_dt(C, m->char_len, h, hu, hv, (float)p->cfl, (float)p->g, p->min_depth);
             if (dt < 0.0) { rc = 3; break; }
             cached = dt;
             out->cfl_evals++;
@@ -473,18 +727,26 @@ int orc_run(const OrcMesh *m, const OrcDrain *d, const OrcRunParams *p, float *h
             f.infil_kind = p->infil_kind; f.infil_scalar = p->infil_scalar; f.infil_cell = p->infil_cell;
         }
         double sd[6], pd[7] = {0, 0, 0, 0, 0, 0, 0};
-        orc_surface_step(m, h, hu, hv, &f, dt, p->g, p->min_depth, h2, hu2, hv2, sd);
+        if (p->local_inertial)
+            orc_li_step(m, h, hu, hv, &f, dt, p->g, p->min_depth, h2, hu2, hv2, sd);
+        else
+            orc_surface_step(m, h, hu, hv, &f, dt, p->g, p->min_depth, h2, hu2, hv2, sd);
         memcpy(h, h2, sizeof(float) * (size_t)C);
         memcpy(hu, hu2, sizeof(float) * (size_t)C);
         memcpy(hv, hv2, sizeof(float) * (size_t)C);
         orc_clamp_velocity(C, h, hu, hv, (float)p->max_speed);
+        double ext = 0.0, rd[2] = {0.0, 0.0};
+        if (p->inflow && p->inflow->receiver_count > 0)
+            ext = orc_external_inflow(C, m->area, p->inflow, t + 0.5 * dt, dt, h);
         if (p->has_drainage && d) orc_pipe_step(m, d, h, V, Q, dt, (float)p->g, pd);
+        if (p->recharge && p->recharge->row_count > 0) orc_recharge(p->recharge, m->area, dt, h, p->recharge_storage, rd);
         const float dtw = (float)dt;
 #pragma omp parallel for schedule(static)
         for (int c = 0; c < C; ++c) wt[c] = wt[c] + dtw * (float)(h[c] > p->min_depth);
         out->ledger[0] += sd[0]; out->ledger[1] += sd[1]; out->ledger[2] += sd[2];
         out->ledger[3] += pd[3]; out->ledger[4] += pd[4]; out->ledger[5] += pd[5];
         out->ledger[6] += pd[0]; out->ledger[7] += pd[1]; out->ledger[8] += pd[2];
+        out->ledger[9] += ext; out->ledger[10] += rd[0]; out->ledger[11] += rd[1];
         t += dt;
         step += 1;
         if (p->finite_interval > 0 && step % p->finite_interval == 0) {

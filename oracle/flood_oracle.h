@@ -15,10 +15,14 @@
  *   timestep       equations.py:155-178, engine.py:220-232
  *   drainage       triangular_inlet_exchange_cuda_kernels.py:52-207,255-443,
  *                  triangular_pipe_network_cuda_kernels.py:39-211,263-421,
- *                  triangular_backend.py:665-830,1758-1764
+ *                  triangular_backend.py:665-830,1399-1485,1758-1764
  *   forcing        production_infiltration_support.py:96-138,
  *                  real_gurugram_domain.py:374-388
  *   run loop       gurugram_flood/solver/engine.py:219-386
+ *   local inertial triangular_local_inertial_cuda_kernels.py:59-262,
+ *                  triangular_backend.py:531-590, equations.py:181-210
+ *   inflow         gurugram_flood/domain/production_event_support.py:169-196
+ *   recharge       gurugram_flood/domain/june5_production_drainage.py:543-572
  * Surface arithmetic is float32 in the reference's operation order (build
  * with -ffp-contract=off); drainage volumes, heads and flows are float64 as
  * in the reference's CuPy kernels.
@@ -55,6 +59,11 @@ typedef struct {
     float wave_speed;
     int32_t capture_rule; /* 0 capacity, 1 head_limited_capacity, 2 orifice, 3 weir_orifice */
     float orifice_area, orifice_coef, weir_perimeter, weir_coef;
+    /* weighted surcharge-return table (triangular_backend.py:1424-1474); sur_count 0: none */
+    int32_t sur_count;
+    const int32_t *sur_cell, *sur_node;
+    const float *sur_weight;
+    int32_t sur_normalized;
 } OrcDrain;
 
 /* Forcing for one step.  rain_kind/infil_kind: 0 scalar, 1 per-cell array. */
@@ -74,6 +83,14 @@ int orc_surface_step(const OrcMesh *m, const float *h, const float *hu, const fl
 
 void orc_clamp_velocity(int32_t n, const float *h, float *hu, float *hv, float max_speed);
 
+/* Local-inertial surface step (triangular_local_inertial_cuda_kernels.py:59-262
+ * + _apply_sources); diag as orc_surface_step. */
+int orc_li_step(const OrcMesh *m, const float *h, const float *hu, const float *hv, const OrcForcing *f,
+                double dt, double g, float min_depth, float *h_out, float *hu_out, float *hv_out, double *diag);
+
+/* stable_local_inertial_timestep_s (equations.py:181-210); < 0 if no finite cell */
+double orc_li_stable_dt(int32_t n, const float *char_len, const float *h, float cfl, float g, float min_depth);
+
 /* returns the global min of the float32 local CFL dt, as a double; <0 if none finite */
 double orc_stable_dt(int32_t n, const float *char_len, const float *h, const float *hu,
                      const float *hv, float cfl, float g, float min_depth);
@@ -81,6 +98,34 @@ double orc_stable_dt(int32_t n, const float *char_len, const float *h, const flo
 /* diag[0..6]: capture, surcharge, link_abs, outfall, overflow, unreturned, final_node_volume */
 int orc_pipe_step(const OrcMesh *m, const OrcDrain *d, float *h, double *node_volume,
                   double *link_flow, double dt, float g, double *diag);
+
+/* External boundary inflow (production_event_support.py:24-29, 169-196). */
+typedef struct {
+    int32_t receiver_count, time_count;
+    const int32_t *receiver_cell;
+    const double *times_s;   /* strictly increasing */
+    const float *q_m3ps;     /* time_count x receiver_count, row-major */
+} OrcInflow;
+
+/* Receiver j's flow at time t: the first / last value outside the table,
+ * else np.interp in float64 rounded to float32. */
+float orc_inflow_q(const OrcInflow *x, int32_t j, double t);
+
+/* apply_external_boundary_inflow_depth: h += per-cell sum (in receiver order)
+ * of float32(q_j) * float32(dt) / area; returns the added volume (float32
+ * terms summed in float64). */
+double orc_external_inflow(int32_t C, const float *area, const OrcInflow *x, double time_s, double dt, float *h);
+
+/* Surface recharge rows (june5_production_drainage.py:99-111). */
+typedef struct {
+    int32_t row_count;
+    const int32_t *source_cell;
+    const float *storage_capacity, *capture_capacity, *recharge_capacity, *stop_depth;
+} OrcRecharge;
+
+/* apply_june5_surface_recharge (:543-572), float32 throughout; storage is
+ * updated in place; diag[0] capture, diag[1] recharge loss (float64 sums). */
+void orc_recharge(const OrcRecharge *r, const float *area, double dt, float *h, float *storage, double *diag);
 
 typedef struct {
     double cfl, safety, max_dt, max_speed, duration_s, snapshot_interval_s;
@@ -97,6 +142,10 @@ typedef struct {
     int32_t has_drainage;
     int64_t max_steps;           /* <=0: unlimited */
     int32_t max_snapshots;
+    const OrcInflow *inflow;     /* nullable: applied after the clamp at t + dt/2 */
+    const OrcRecharge *recharge; /* nullable: applied after the drainage step */
+    float *recharge_storage;     /* [row_count], in/out (with recharge) */
+    int32_t local_inertial;      /* 1: surface_step_mode = local_inertial */
 } OrcRunParams;
 
 typedef struct {
@@ -104,7 +153,8 @@ typedef struct {
     int32_t snapshot_count, error; /* error: 0 ok, 1 non-finite depth, 2 snapshot overflow */
     int64_t error_step;
     double t_end;
-    double ledger[9]; /* rain, infil, bnet, outfall, overflow, unreturned, capture, surcharge, link_abs */
+    double ledger[12]; /* rain, infil, bnet, outfall, overflow, unreturned, capture, surcharge, link_abs,
+                          external inflow, recharge capture, recharge loss */
 } OrcRunResult;
 
 /* state arrays are updated in place; snapshots: max_snapshots x C (h, hu, hv) and x N (volume f32) */

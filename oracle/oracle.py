@@ -43,7 +43,10 @@ def lib():
         build()
         _lib = C.CDLL(str(LIB_PATH))
         _lib.orc_stable_dt.restype = C.c_double
+        _lib.orc_li_stable_dt.restype = C.c_double
         _lib.orc_num_threads.restype = C.c_int
+        _lib.orc_external_inflow.restype = C.c_double
+        _lib.orc_inflow_q.restype = C.c_float
     return _lib
 
 
@@ -78,6 +81,8 @@ class OrcDrain(C.Structure):
         ("capture_rule", C.c_int32),
         ("orifice_area", C.c_float), ("orifice_coef", C.c_float),
         ("weir_perimeter", C.c_float), ("weir_coef", C.c_float),
+        ("sur_count", C.c_int32), ("sur_cell", i32p), ("sur_node", i32p), ("sur_weight", f32p),
+        ("sur_normalized", C.c_int32),
     ]
 
 
@@ -85,6 +90,20 @@ class OrcForcing(C.Structure):
     _fields_ = [
         ("rain_kind", C.c_int32), ("rain_scalar", C.c_float), ("rain_cell", f32p),
         ("infil_kind", C.c_int32), ("infil_scalar", C.c_float), ("infil_cell", f32p),
+    ]
+
+
+class OrcInflow(C.Structure):
+    _fields_ = [
+        ("receiver_count", C.c_int32), ("time_count", C.c_int32),
+        ("receiver_cell", i32p), ("times_s", f64p), ("q_m3ps", f32p),
+    ]
+
+
+class OrcRecharge(C.Structure):
+    _fields_ = [
+        ("row_count", C.c_int32), ("source_cell", i32p),
+        ("storage_capacity", f32p), ("capture_capacity", f32p), ("recharge_capacity", f32p), ("stop_depth", f32p),
     ]
 
 
@@ -102,6 +121,8 @@ class OrcRunParams(C.Structure):
         ("has_drainage", C.c_int32),
         ("max_steps", C.c_int64),
         ("max_snapshots", C.c_int32),
+        ("inflow", C.POINTER(OrcInflow)), ("recharge", C.POINTER(OrcRecharge)), ("recharge_storage", f32p),
+        ("local_inertial", C.c_int32),
     ]
 
 
@@ -110,7 +131,7 @@ class OrcRunResult(C.Structure):
         ("step_count", C.c_int64), ("cfl_evals", C.c_int64), ("cfl_reused", C.c_int64),
         ("snapshot_count", C.c_int32), ("error", C.c_int32),
         ("error_step", C.c_int64), ("t_end", C.c_double),
-        ("ledger", C.c_double * 9),
+        ("ledger", C.c_double * 12),
     ]
 
 
@@ -204,6 +225,15 @@ def make_drain(coupling, pipe, capture_rule="orifice", orifice_area=0.04, orific
         capture_rule=CAPTURE_RULES[capture_rule],
         orifice_area=orifice_area, orifice_coef=orifice_coef, weir_perimeter=weir_perimeter, weir_coef=weir_coef,
     )
+    # the weighted return table is used when all three arrays are given (reference :1424-1428)
+    sc, sn, sw = (getattr(coupling, a, None) for a in ("surcharge_cell_index", "surcharge_node_index",
+                                                        "surcharge_return_weight"))
+    if sc is not None and sn is not None and sw is not None:
+        d.sur_count = int(np.asarray(sc).size)
+        d.sur_cell = _p(k.i32(sc), C.c_int32)
+        d.sur_node = _p(k.i32(sn), C.c_int32)
+        d.sur_weight = _p(k.f32(sw), C.c_float)
+        d.sur_normalized = int(bool(getattr(coupling, "surcharge_return_weight_is_normalized", False)))
     return d, k
 
 
@@ -234,6 +264,36 @@ def surface_step(topo, h, hu, hv, dt, rainfall=0.0, infiltration=0.0, stage=None
     if rc != 0:
         raise RuntimeError(f"orc_surface_step failed: {rc}")
     return ho, huo, hvo, diag
+
+
+def li_step(topo, h, hu, hv, dt, rainfall=0.0, infiltration=0.0, g=9.80665, min_depth=1e-5):
+    """One local-inertial surface step (discharge, donor scale, gather + sources)."""
+
+    m, keep = make_mesh(topo, None)
+    rk, rs, ra = _forcing(rainfall, keep)
+    ik, is_, ia = _forcing(infiltration, keep)
+    f = OrcForcing(rain_kind=rk, rain_scalar=rs, rain_cell=_p(ra, C.c_float),
+                   infil_kind=ik, infil_scalar=is_, infil_cell=_p(ia, C.c_float))
+    h, hu, hv = keep.f32(h), keep.f32(hu), keep.f32(hv)
+    n = topo.cell_count
+    ho, huo, hvo = np.empty(n, np.float32), np.empty(n, np.float32), np.empty(n, np.float32)
+    diag = np.zeros(6, np.float64)
+    rc = lib().orc_li_step(C.byref(m), _p(h, C.c_float), _p(hu, C.c_float), _p(hv, C.c_float), C.byref(f),
+                           C.c_double(dt), C.c_double(g), C.c_float(min_depth),
+                           _p(ho, C.c_float), _p(huo, C.c_float), _p(hvo, C.c_float), _p(diag, C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"orc_li_step failed: {rc}")
+    return ho, huo, hvo, diag
+
+
+def li_stable_dt(char_len, h, cfl=0.85, g=9.80665, min_depth=1e-5):
+    cl = np.ascontiguousarray(char_len, np.float32)
+    h = np.ascontiguousarray(h, np.float32)
+    v = lib().orc_li_stable_dt(C.c_int32(h.size), _p(cl, C.c_float), _p(h, C.c_float), C.c_float(cfl),
+                               C.c_float(g), C.c_float(min_depth))
+    if v < 0:
+        raise ValueError("No finite cells are available for timestep calculation.")
+    return float(v)
 
 
 def clamp_velocity(h, hu, hv, max_speed=5.0):
@@ -272,6 +332,61 @@ def pipe_step(topo, coupling, pipe, h, node_volume, link_flow, dt, g=9.80665, **
     return h, V, Q, diag
 
 
+def make_inflow(external, keep):
+    """OrcInflow of an ExternalBoundaryInflowSurface-like object (receiver_cell_index,
+    times_s, q_m3ps_by_receiver [times x receivers])."""
+
+    cells = keep.i32(external.receiver_cell_index)
+    times = keep.f64(external.times_s)
+    q = keep.f32(np.asarray(external.q_m3ps_by_receiver, np.float32).reshape(times.size, cells.size))
+    return OrcInflow(receiver_count=cells.size, time_count=times.size, receiver_cell=_p(cells, C.c_int32),
+                     times_s=_p(times, C.c_double), q_m3ps=_p(q, C.c_float))
+
+
+def make_recharge(topo, keep):
+    """OrcRecharge of a June5RechargeTopology-like object (float32 rows)."""
+
+    cells = keep.i32(topo.source_cell_index)
+    return OrcRecharge(row_count=cells.size, source_cell=_p(cells, C.c_int32),
+                       storage_capacity=_p(keep.f32(topo.storage_capacity_m3), C.c_float),
+                       capture_capacity=_p(keep.f32(topo.capture_capacity_m3ps), C.c_float),
+                       recharge_capacity=_p(keep.f32(topo.recharge_capacity_m3ps), C.c_float),
+                       stop_depth=_p(keep.f32(topo.stop_depth_m), C.c_float))
+
+
+def external_inflow(area, external, h, time_s: float, dt: float):
+    """apply_external_boundary_inflow_depth on a copy of h: (new h, added m^3)."""
+
+    keep = _Keep()
+    x = make_inflow(external, keep)
+    a = keep.f32(area)
+    out = np.array(h, np.float32)
+    added = lib().orc_external_inflow(a.size, _p(a, C.c_float), C.byref(x), C.c_double(time_s), C.c_double(dt),
+                                      _p(out, C.c_float))
+    return out, float(added)
+
+
+def inflow_q(external, time_s: float) -> np.ndarray:
+    keep = _Keep()
+    x = make_inflow(external, keep)
+    return np.array([lib().orc_inflow_q(C.byref(x), j, C.c_double(time_s)) for j in range(x.receiver_count)],
+                    np.float32)
+
+
+def recharge(area, topo, h, storage, dt: float):
+    """apply_june5_surface_recharge on copies: (new h, new storage, capture m^3, loss m^3)."""
+
+    keep = _Keep()
+    r = make_recharge(topo, keep)
+    a = keep.f32(area)
+    out = np.array(h, np.float32)
+    st = np.array(storage, np.float32)
+    diag = np.zeros(2, np.float64)
+    lib().orc_recharge(C.byref(r), _p(a, C.c_float), C.c_double(dt), _p(out, C.c_float), _p(st, C.c_float),
+                       _p(diag, C.c_double))
+    return out, st, float(diag[0]), float(diag[1])
+
+
 @dataclass
 class OracleRun:
     step_count: int
@@ -292,6 +407,7 @@ class OracleRun:
     ledger: dict
     error: int
     error_step: int
+    recharge_storage: np.ndarray | None = None
 
 
 def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None) -> OracleRun:
@@ -331,7 +447,21 @@ def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None
         infil_kind=1 if infil_cell is not None else 0, infil_scalar=0.0, infil_cell=_p(infil_cell, C.c_float),
         hyeto_n=hs.size, hyeto_start_s=_p(hs, C.c_double), hyeto_end_s=_p(he, C.c_double), hyeto_rate=_p(hr, C.c_double),
         has_drainage=1 if has_drain else 0, max_steps=int(max_steps), max_snapshots=n_snap,
+        local_inertial=1 if s.surface_step_mode == "local_inertial" else 0,
     )
+    ext = getattr(city, "external_boundary", None)
+    rch = getattr(city, "recharge_topology", None)
+    rstore = None
+    if ext is not None and np.asarray(ext.receiver_cell_index).size:
+        xin = make_inflow(ext, keep)
+        keep.items.append(xin)
+        p.inflow = C.pointer(xin)
+    if rch is not None and np.asarray(rch.source_cell_index).size:
+        xr = make_recharge(rch, keep)
+        keep.items.append(xr)
+        p.recharge = C.pointer(xr)
+        rstore = np.zeros(xr.row_count, np.float32)
+        p.recharge_storage = _p(rstore, C.c_float)
     n = st.cell_count
     nn = topo.coupling_topology.node_count
     h = np.array(topo.surface_state.h_m, np.float32)
@@ -354,13 +484,14 @@ def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None
     k = res.snapshot_count
     names = ["rainfall_input_m3", "infiltration_loss_m3", "boundary_net_flux_m3", "outfall_discharge_m3",
              "overflow_surcharge_m3", "unreturned_overflow_m3", "surface_capture_m3", "surface_surcharge_m3",
-             "link_abs_flow_m3"]
+             "link_abs_flow_m3", "external_boundary_inflow_m3", "surface_recharge_capture_m3",
+             "surface_recharge_loss_m3"]
     return OracleRun(
         step_count=res.step_count, cfl_evals=res.cfl_evals, cfl_reused=res.cfl_reused, t_end=res.t_end,
         snapshot_times_s=st_t[:k].copy(), depth=sh[:k].copy(), hu=shu[:k].copy(), hv=shv[:k].copy(),
         node_volume=sv[:k, :nn].copy(), final_h=h, final_hu=hu, final_hv=hv, final_node_volume=V,
         final_link_flow=Q, wet_time=wt, ledger=dict(zip(names, list(res.ledger))), error=res.error,
-        error_step=res.error_step,
+        error_step=res.error_step, recharge_storage=rstore,
     )
 
 

@@ -47,6 +47,11 @@ def coupling_pipe(d, p: str):
         node_storage_area_m2=d[p + "node_storage_area_m2"], node_max_depth_m=d[p + "node_max_depth_m"],
         inlet_capture_capacity_m3ps=_opt(d, p + "inlet_capture_capacity_m3ps"),
         inlet_surcharge_capacity_m3ps=_opt(d, p + "inlet_surcharge_capacity_m3ps"),
+        surcharge_cell_index=_opt(d, p + "surcharge_cell_index"),
+        surcharge_node_index=_opt(d, p + "surcharge_node_index"),
+        surcharge_return_weight=_opt(d, p + "surcharge_return_weight"),
+        surcharge_return_weight_is_normalized=bool(int(d[p + "surcharge_return_weight_is_normalized"]))
+        if p + "surcharge_return_weight_is_normalized" in d.files else False,
     )
     names = ["link_flow_capacity_m3ps", "outfall_area_m2", "outfall_coefficient", "outfall_tailwater_head_m",
              "outfall_flow_capacity_m3ps", "link_invert_elevation_m", "link_diameter_m",
@@ -81,3 +86,39 @@ def scenario(d, p: str) -> Scenario:
     rain = rainfall_event(hy[0], hy[1], hy[2])
     overrides = dict(ast.literal_eval(str(d[p + "overrides"])))
     return Scenario(p.strip("/"), city, rain, overrides)
+
+
+def inflow(d, p: str):
+    """ExternalBoundaryInflowSurface of a fixture prefix (None if absent)."""
+
+    from floodgb.domain import ExternalBoundaryInflowSurface
+
+    if p + "ext_cells" not in d.files:
+        return None
+    return ExternalBoundaryInflowSurface(receiver_cell_index=d[p + "ext_cells"], times_s=d[p + "ext_times"],
+                                         q_m3ps_by_receiver=d[p + "ext_q"])
+
+
+def recharge(d, p: str):
+    """June5RechargeTopology of a fixture prefix (None if absent)."""
+
+    from floodgb.domain import June5RechargeTopology
+
+    if p + "rch_source_cell_index" not in d.files:
+        return None
+    cells = d[p + "rch_source_cell_index"]
+    n = cells.size
+    return June5RechargeTopology(
+        source_cell_index=cells, overflow_cell_index=cells.copy(),
+        storage_capacity_m3=d[p + "rch_storage_capacity_m3"], capture_capacity_m3ps=d[p + "rch_capture_capacity_m3ps"],
+        recharge_capacity_m3ps=d[p + "rch_recharge_capacity_m3ps"], activation_depth_m=np.full(n, 0.05, np.float32),
+        stop_depth_m=d[p + "rch_stop_depth_m"])
+
+
+def forcing_scenario(d, p: str) -> Scenario:
+    """scenario() plus the prefix's external inflow and recharge rows."""
+
+    sc = scenario(d, p)
+    sc.city.external_boundary = inflow(d, p)
+    sc.city.recharge_topology = recharge(d, p)
+    return sc

@@ -9,8 +9,11 @@ The reference package ``gurugram_flood`` cannot be imported normally here
 stubs point at its source directories and only the NumPy-capable modules are
 loaded: ``kernels/triangular_backend.py`` (with ``equations.py``,
 ``network_kernels.py``, ``pipe_kernels.py``), ``solver/stabilizers.py`` and
-``domain/production_infiltration_support.py``.  The engine loop
-(``solver/engine.py:219-344``) is restated here on top of those functions.
+``domain/production_infiltration_support.py``, plus
+``domain/production_event_support.py`` (external inflow) and
+``domain/june5_production_drainage.py`` (recharge) behind an empty pandas
+stand-in.  The engine loop (``solver/engine.py:219-344``) is restated here on
+top of those functions.
 
 Dtype discipline follows the reference's CuPy production path: every scalar
 forcing is passed as ``np.float32`` and ``h`` is cast back to float32 after the
@@ -48,6 +51,18 @@ def import_reference(ref_root: Path):
     return tb, stab, pis
 
 
+def import_reference_forcing():
+    """The reference's inflow and recharge modules.  Both import pandas at
+    module level (for their CSV loaders, which are not called here); pandas is
+    absent in this container, so an empty stand-in module satisfies the import."""
+
+    sys.modules.setdefault("pandas", types.ModuleType("pandas"))
+    import gurugram_flood.domain.june5_production_drainage as j5
+    import gurugram_flood.domain.production_event_support as pes
+
+    return pes, j5
+
+
 def topo_arrays(prefix, st):
     return {
         f"{prefix}bed": st.bed_elevation_m, f"{prefix}manning": st.manning_n, f"{prefix}area": st.cell_area_m2,
@@ -64,10 +79,13 @@ def coupling_arrays(prefix, cp, pp):
     out = {}
     for name in ("inlet_cell_index", "inlet_node_index", "node_surface_cell_index", "node_invert_elevation_m",
                  "node_storage_area_m2", "node_max_depth_m", "inlet_capture_capacity_m3ps",
-                 "inlet_surcharge_capacity_m3ps"):
+                 "inlet_surcharge_capacity_m3ps", "surcharge_cell_index", "surcharge_node_index",
+                 "surcharge_return_weight"):
         v = getattr(cp, name)
         if v is not None:
             out[f"{prefix}{name}"] = np.asarray(v)
+    if cp.surcharge_cell_index is not None:
+        out[f"{prefix}surcharge_return_weight_is_normalized"] = np.int32(cp.surcharge_return_weight_is_normalized)
     for name in ("link_from_node_index", "link_to_node_index", "link_length_m", "link_area_m2",
                  "link_hydraulic_radius_m", "link_manning_n", "link_flow_capacity_m3ps", "outfall_area_m2",
                  "outfall_coefficient", "outfall_tailwater_head_m", "outfall_flow_capacity_m3ps",
@@ -170,6 +188,36 @@ def tiny_coupled(seed=5):
                              n_outfalls=3, area_km2=0.25, seed=seed, duration_min=3.0)
 
 
+def surcharge_table(tb, cp, st, rng, normalized: bool):
+    """A weighted surcharge-return table on a coupling topology: about 60 % of
+    nodes with one to three entries on random active cells (some sharing a
+    cell), a few invalid entries (node or cell -1), zero and negative weights."""
+
+    active = np.flatnonzero(np.asarray(st.active_mask) > 0.5)
+    nodes = rng.choice(cp.node_count, size=int(0.6 * cp.node_count), replace=False)
+    cells, owner, weight = [], [], []
+    for n in nodes:
+        k = int(rng.integers(1, 4))
+        cells.extend(rng.choice(active, size=k).tolist())
+        owner.extend([int(n)] * k)
+        w = rng.uniform(0.0, 2.0, k)
+        if normalized:
+            w = (w / w.sum()).astype(np.float32)
+        weight.extend(w.tolist())
+    cells, owner = np.array(cells, np.int32), np.array(owner, np.int32)
+    weight = np.array(weight, np.float32)
+    order = rng.permutation(cells.size)
+    cells, owner, weight = cells[order], owner[order], weight[order]
+    if not normalized:
+        weight[::11] = 0.0
+        weight[5::17] = -0.5
+    cells[3::23] = -1
+    owner[7::29] = -1
+    return tb.TriangularNodeCouplingTopology(**{
+        **cp.__dict__, "surcharge_cell_index": cells, "surcharge_node_index": owner,
+        "surcharge_return_weight": weight, "surcharge_return_weight_is_normalized": normalized})
+
+
 def make_pipe_cases(tb):
     rng = np.random.default_rng(77)
     sc = tiny_coupled()
@@ -192,8 +240,13 @@ def make_pipe_cases(tb):
         "link_rect_height_m": rng.uniform(0.4, 1.5, L).astype(np.float32), "link_invert_elevation_m": inv,
         "outfall_flow_capacity_m3ps": np.full(cp.node_count, 0.3, np.float32)})
     variants.append(("rect_invert_orifice", rect, "orifice"))
+    trng = np.random.default_rng(78)  # its own stream: the cases above keep their inputs
+    variants.append(("table_orifice", pp, "orifice", surcharge_table(tb, cp, st, trng, normalized=False)))
+    variants.append(("table_normalized_capacity", pp, "capacity", surcharge_table(tb, cp, st, trng, normalized=True)))
     names = []
-    for name, pipe, rule in variants:
+    base_cp = cp
+    for name, pipe, rule, *alt in variants:
+        cp = alt[0] if alt else base_cp
         h = rng.uniform(0.0, 0.4, st.cell_count).astype(np.float32)
         h[rng.random(st.cell_count) < 0.3] = 0.0
         if st.active_mask is not None:
@@ -222,8 +275,10 @@ def make_pipe_cases(tb):
     return names
 
 
-def reference_run(tb, stab, pis, sc, max_steps, snapshot_interval_s):
-    """engine.py:219-344 restated on the reference's NumPy step functions."""
+def reference_run(tb, stab, pis, sc, max_steps, snapshot_interval_s, extra=None, li=False):
+    """engine.py:219-344 restated on the reference's NumPy step functions;
+    ``extra`` = (production_event_support, june5_production_drainage) adds
+    the external inflow and recharge steps (engine.py:263-289)."""
 
     from floodgb.config import load_config
 
@@ -250,11 +305,30 @@ def reference_run(tb, stab, pis, sc, max_steps, snapshot_interval_s):
     cached = None
     next_snap = 0.0
     snaps_t, snaps_h, snaps_hu, snaps_hv, snaps_v = [], [], [], [], []
-    cum = np.zeros(6)
+    cum = np.zeros(9)
     has_drain = cp.node_count > 0
+    ext = rch = rstore = None
+    if extra is not None:
+        pes, j5 = extra
+        e = sc.city.external_boundary
+        if e is not None:
+            ext = pes.ExternalBoundaryInflowSurface(
+                receiver_cell_index=np.asarray(e.receiver_cell_index, np.int32), times_s=np.asarray(e.times_s, np.float64),
+                q_m3ps_by_receiver=np.asarray(e.q_m3ps_by_receiver, np.float32), peak_total_m3ps=0.0, report={})
+        r = sc.city.recharge_topology
+        if r is not None:
+            rch = j5.recharge_to_backend(j5.June5RechargeTopology(
+                source_cell_index=r.source_cell_index, overflow_cell_index=r.overflow_cell_index,
+                storage_capacity_m3=r.storage_capacity_m3, capture_capacity_m3ps=r.capture_capacity_m3ps,
+                recharge_capacity_m3ps=r.recharge_capacity_m3ps, activation_depth_m=r.activation_depth_m,
+                stop_depth_m=r.stop_depth_m), np)
+            rstore = np.zeros(r.source_cell_index.size, np.float32)
     while t < final_t and step < max_steps:
         if cached is None or step % s.cfl_update_interval_steps == 0:
-            dt = float(tb.stable_triangular_timestep_s(st, state, cfl=s.cfl))
+            if li:
+                dt = float(tb.stable_local_inertial_triangular_timestep_s(st, state, cfl=s.cfl))
+            else:
+                dt = float(tb.stable_triangular_timestep_s(st, state, cfl=s.cfl))
             cached = dt
         else:
             dt = cached * s.cfl_reuse_safety_factor
@@ -269,16 +343,34 @@ def reference_run(tb, stab, pis, sc, max_steps, snapshot_interval_s):
             rain = np.float32(base)
             infil = np.float32(0.0)
         forcing = tb.TriangularSurfaceForcing(rainfall_rate_mps=rain, infiltration_capacity_mps=infil)
-        state, sd = tb.step_triangular_surface(state, st, forcing, timestep_s=dt)
+        if li:
+            state, sd = tb.step_triangular_surface_local_inertial(state, st, forcing, timestep_s=dt)
+            state = tb.TriangularSurfaceState(np.asarray(state.h_m, np.float32), np.asarray(state.hu_m2ps, np.float32),
+                                              np.asarray(state.hv_m2ps, np.float32))
+        else:
+            state, sd = tb.step_triangular_surface(state, st, forcing, timestep_s=dt)
         state = stab.clamp_velocity(state, s.max_speed_mps, np)
         od = us = 0.0
         ov = 0.0
+        ea = rc = rl = 0.0
+        if ext is not None:
+            hx, added = pes.apply_external_boundary_inflow_depth(state.h_m, st.cell_area_m2, ext, timestep_s=dt,
+                                                                 time_s=t + 0.5 * dt, xp=np)
+            assert hx.dtype == np.float32
+            state = tb.TriangularSurfaceState(hx, state.hu_m2ps, state.hv_m2ps)
+            ea = float(added)
         if has_drain:
             h, pstate, pd = tb.step_triangular_dynamic_pipe_network(state.h_m, st, cp, pp, pstate, dt)
             state = tb.TriangularSurfaceState(np.asarray(h, np.float32), state.hu_m2ps, state.hv_m2ps)
             od, ov, us = float(pd.outfall_discharge_m3), float(pd.overflow_surcharge_m3), float(pd.unreturned_overflow_m3)
+        if rch is not None:
+            hr, rstore, c_m3, l_m3 = j5.apply_june5_surface_recharge(state.h_m, rch, rstore, st.cell_area_m2, dt, np)
+            assert hr.dtype == np.float32 and rstore.dtype == np.float32
+            state = tb.TriangularSurfaceState(hr, state.hu_m2ps, state.hv_m2ps)
+            rc, rl = float(c_m3), float(l_m3)
         wet = wet + pis.wet_time_increment_s(xp=np, depth_m=state.h_m, dt_s=dt, min_depth_m=1e-5)
-        cum += [float(sd.rainfall_input_m3), float(sd.infiltration_loss_m3), float(sd.boundary_net_flux_m3), od, ov, us]
+        cum += [float(sd.rainfall_input_m3), float(sd.infiltration_loss_m3), float(sd.boundary_net_flux_m3), od, ov, us,
+                ea, rc, rl]
         t += dt
         step += 1
         if t >= next_snap or t >= final_t:
@@ -291,8 +383,9 @@ def reference_run(tb, stab, pis, sc, max_steps, snapshot_interval_s):
     return dict(step_count=np.int64(step), t_end=np.float64(t), snap_t=np.array(snaps_t), snap_h=np.array(snaps_h),
                 snap_hu=np.array(snaps_hu), snap_hv=np.array(snaps_hv),
                 snap_v=np.array(snaps_v) if has_drain else np.zeros((len(snaps_t), 0), np.float32),
-                ledger=cum, final_V=np.asarray(pstate.node_volume_m3), final_Q=np.asarray(pstate.link_flow_m3ps),
-                wet_time=wet)
+                ledger=cum[:6] if extra is None else cum,
+                final_V=np.asarray(pstate.node_volume_m3), final_Q=np.asarray(pstate.link_flow_m3ps),
+                wet_time=wet, **({} if rstore is None else {"recharge_storage": np.asarray(rstore)}))
 
 
 def scenario_arrays(prefix, sc):
@@ -343,12 +436,163 @@ def make_run_cases(tb, stab, pis):
     np.savez_compressed(OUT / "run_cases.npz", **out)
 
 
+def make_li_cases(tb, stab, pis):
+    """Local-inertial steps (the reference's NumPy path, triangular_backend.py
+    :531-590 and :1181-1291) and its timestep, plus two multi-step runs of the
+    restated engine loop in local-inertial mode."""
+
+    from floodgb.synthetic import make_grid_city
+
+    rng = np.random.default_rng(20261204)
+    out = {}
+    names = []
+    st, _, _ = grid_topology(tb, rng, n=12, mode="outflow", active_frac=0.85)
+    st2, _, _ = grid_topology(tb, rng, n=10, mode="transmissive", active_frac=0.9)
+    st3, _, _ = grid_topology(tb, rng, n=10, mode="reflective", active_frac=1.0)
+    st3 = tb.TriangularSurfaceTopology(**{**st3.__dict__, "active_mask": None})
+    cases = [
+        ("outflow_scalar", st, np.float32(60.0 / 3.6e6), np.float32(5.0 / 3.6e6), 0.7),
+        ("outflow_percell", st, (rng.uniform(0, 80, st.cell_count) / 3.6e6).astype(np.float32),
+         (rng.uniform(0, 120, st.cell_count) / 3.6e6).astype(np.float32), 0.3),
+        ("transmissive_dry", st2, np.float32(0.0), np.float32(0.0), 1.0),
+        ("reflective_nomask", st3, np.float32(20.0 / 3.6e6), np.float32(0.0), 0.5),
+    ]
+    for name, topo, rain, infil, dt in cases:
+        h, hu, hv = random_state(rng, topo.cell_count, hmax=0.4)
+        if name == "transmissive_dry":
+            h[rng.random(topo.cell_count) < 0.5] = 0.0
+        state = tb.TriangularSurfaceState(h, hu, hv)
+        forcing = tb.TriangularSurfaceForcing(rainfall_rate_mps=rain, infiltration_capacity_mps=infil)
+        new, diag = tb.step_triangular_surface_local_inertial(state, topo, forcing, dt)
+        p = f"{name}/"
+        out.update(topo_arrays(p, topo))
+        out[f"{p}h"], out[f"{p}hu"], out[f"{p}hv"] = h, hu, hv
+        out[f"{p}rain"], out[f"{p}infil"], out[f"{p}dt"] = np.asarray(rain), np.asarray(infil), np.float64(dt)
+        out[f"{p}h_out"] = np.asarray(new.h_m, np.float32)
+        out[f"{p}hu_out"] = np.asarray(new.hu_m2ps, np.float32)
+        out[f"{p}hv_out"] = np.asarray(new.hv_m2ps, np.float32)
+        out[f"{p}diag"] = np.array([
+            float(diag.rainfall_input_m3), float(diag.infiltration_loss_m3), float(diag.boundary_net_flux_m3),
+            float(diag.boundary_inflow_m3), float(diag.boundary_outflow_m3), float(diag.final_surface_volume_m3)])
+        out[f"{p}dt_li"] = np.float64(tb.stable_local_inertial_triangular_timestep_s(topo, state, cfl=0.85))
+        names.append(name)
+    out["cases"] = np.array(names)
+    sc = tiny_coupled(seed=21)
+    sc.overrides["solver.snapshot_interval_min"] = 0.5
+    sc.overrides["solver.duration_min"] = 3.0
+    sc.overrides["solver.surface_step_mode"] = "local_inertial"
+    st4 = sc.city.topologies.surface_topology
+    rng2 = np.random.default_rng(14)
+    h0 = np.where(st4.active_mask > 0.5, rng2.uniform(0, 0.3, st4.cell_count), 0).astype(np.float32)
+    sc.city.topologies.surface_state = tb.TriangularSurfaceState(h0, np.zeros_like(h0), np.zeros_like(h0))
+    out.update(scenario_arrays("coupled/", sc))
+    res = reference_run(tb, stab, pis, sc, max_steps=400, snapshot_interval_s=30.0, li=True)
+    out.update({f"coupled/{k}": v for k, v in res.items()})
+    gsc = make_grid_city(n=20, size_m=200.0, seed=6, rain_mmhr=80.0, duration_min=4.0)
+    gsc.overrides["solver.snapshot_interval_min"] = 1.0
+    gsc.overrides["solver.surface_step_mode"] = "local_inertial"
+    out.update(scenario_arrays("grid/", gsc))
+    res = reference_run(tb, stab, pis, gsc, max_steps=100000, snapshot_interval_s=60.0, li=True)
+    out.update({f"grid/{k}": v for k, v in res.items()})
+    np.savez_compressed(OUT / "li_cases.npz", **out)
+    return names
+
+
+def forcing_arrays(prefix, city):
+    out = {}
+    e = city.external_boundary
+    if e is not None:
+        out[prefix + "ext_cells"] = np.asarray(e.receiver_cell_index, np.int32)
+        out[prefix + "ext_times"] = np.asarray(e.times_s, np.float64)
+        out[prefix + "ext_q"] = np.asarray(e.q_m3ps_by_receiver, np.float32)
+    r = city.recharge_topology
+    if r is not None:
+        for k in ("source_cell_index", "storage_capacity_m3", "capture_capacity_m3ps", "recharge_capacity_m3ps",
+                  "stop_depth_m"):
+            out[prefix + "rch_" + k] = np.asarray(getattr(r, k))
+    return out
+
+
+def make_forcing_cases(tb, stab, pis, pes, j5):
+    """Inflow and recharge alone (reference functions on seeded inputs) and a
+    coupled run with both."""
+
+    from floodgb.synthetic import add_boundary_forcing
+
+    out = {}
+    rng = np.random.default_rng(31)
+    sc = tiny_coupled(seed=13)
+    add_boundary_forcing(sc, n_receivers=5, n_recharge=24, seed=3, peak_m3ps=1.5, step_s=20.0)
+    st = sc.city.topologies.surface_topology
+    area = np.asarray(st.cell_area_m2, np.float32)
+    out["unit/area"] = area
+    out.update(forcing_arrays("unit/", sc.city))
+    e = sc.city.external_boundary
+    ext = pes.ExternalBoundaryInflowSurface(receiver_cell_index=e.receiver_cell_index, times_s=e.times_s,
+                                            q_m3ps_by_receiver=e.q_m3ps_by_receiver, peak_total_m3ps=0.0, report={})
+    h = np.where(st.active_mask > 0.5, rng.uniform(0, 0.2, st.cell_count), 0).astype(np.float32)
+    out["unit/h"] = h
+    times = [-5.0, 0.0, 7.3, 20.0, 33.33, 59.99, float(e.times_s[-1]), float(e.times_s[-1]) + 100.0]
+    dts = [0.5, 0.37, 1.0, 0.01, 0.85, 0.2, 0.6, 1.0]
+    ext_h, ext_v, ext_q = [], [], []
+    for t, dt in zip(times, dts):
+        hx, added = pes.apply_external_boundary_inflow_depth(h, st.cell_area_m2, ext, timestep_s=dt, time_s=t, xp=np)
+        ext_h.append(np.asarray(hx, np.float32))
+        ext_v.append(float(added))
+        ext_q.append(pes.external_boundary_inflow_q_m3ps(ext, t))
+    out["unit/ext_time"] = np.array(times)
+    out["unit/ext_dt"] = np.array(dts)
+    out["unit/ext_h_out"] = np.stack(ext_h)
+    out["unit/ext_added"] = np.array(ext_v)
+    out["unit/ext_q_at"] = np.stack(ext_q)
+    r = sc.city.recharge_topology
+    rb = j5.recharge_to_backend(j5.June5RechargeTopology(
+        source_cell_index=r.source_cell_index, overflow_cell_index=r.overflow_cell_index,
+        storage_capacity_m3=r.storage_capacity_m3, capture_capacity_m3ps=r.capture_capacity_m3ps,
+        recharge_capacity_m3ps=r.recharge_capacity_m3ps, activation_depth_m=r.activation_depth_m,
+        stop_depth_m=r.stop_depth_m), np)
+    # deep water on the recharge cells so capture, storage limits and losses all act
+    hr = h.copy()
+    hr[r.source_cell_index] = rng.uniform(0.0, 0.6, r.source_cell_index.size).astype(np.float32)
+    store = np.zeros(r.source_cell_index.size, np.float32)
+    store[::5] = np.asarray(r.storage_capacity_m3, np.float32)[::5] * np.float32(0.97)
+    out["unit/rch_h"], out["unit/rch_storage0"] = hr.copy(), store.copy()
+    rh, rs, rc, rl = [], [], [], []
+    for dt in (0.9, 30.0, 5.0, 120.0):
+        hr, store, c_m3, l_m3 = j5.apply_june5_surface_recharge(hr, rb, store, st.cell_area_m2, dt, np)
+        rh.append(np.asarray(hr, np.float32))
+        rs.append(np.asarray(store, np.float32))
+        rc.append(float(c_m3))
+        rl.append(float(l_m3))
+    out["unit/rch_dt"] = np.array([0.9, 30.0, 5.0, 120.0])
+    out["unit/rch_h_out"], out["unit/rch_storage_out"] = np.stack(rh), np.stack(rs)
+    out["unit/rch_capture"], out["unit/rch_loss"] = np.array(rc), np.array(rl)
+
+    # a coupled run with both
+    run_sc = tiny_coupled(seed=9)
+    run_sc.overrides["solver.snapshot_interval_min"] = 0.5
+    run_sc.overrides["solver.duration_min"] = 3.0
+    add_boundary_forcing(run_sc, n_receivers=4, n_recharge=20, seed=5, peak_m3ps=0.8, step_s=30.0)
+    rst = run_sc.city.topologies.surface_topology
+    rng2 = np.random.default_rng(12)
+    h0 = np.where(rst.active_mask > 0.5, rng2.uniform(0, 0.3, rst.cell_count), 0).astype(np.float32)
+    run_sc.city.topologies.surface_state = tb.TriangularSurfaceState(h0, np.zeros_like(h0), np.zeros_like(h0))
+    out.update(scenario_arrays("run/", run_sc))
+    out.update(forcing_arrays("run/", run_sc.city))
+    res = reference_run(tb, stab, pis, run_sc, max_steps=400, snapshot_interval_s=30.0, extra=(pes, j5))
+    out.update({f"run/{k}": v for k, v in res.items()})
+    np.savez_compressed(OUT / "forcing_cases.npz", **out)
+
+
 def main():
     ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
     tb, stab, pis = import_reference(ref)
+    pes, j5 = import_reference_forcing()
     print("surface:", make_surface_cases(tb, stab))
     print("pipe:", make_pipe_cases(tb))
     make_run_cases(tb, stab, pis)
+    make_forcing_cases(tb, stab, pis, pes, j5)
+    print("local inertial:", make_li_cases(tb, stab, pis))
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -148,3 +148,21 @@ def test_small_workload_shape():
     st = sc.city.topologies.surface_topology
     assert st.cell_count == 20_000 and st.edge_count == 30_200
     assert int((np.asarray(st.boundary_code) == 4).sum()) == 400
+
+
+def test_plan_accepts_surcharge_table_and_rejects_bad_entries(lib):
+    from floodgb.topology import TriangularNodeCouplingTopology
+
+    d = F.load("pipe_cases.npz")
+    st = F.surface_topology(d, "mesh/")
+    cp, pp = F.coupling_pipe(d, "table_orifice/")
+    assert cp.surcharge_cell_index is not None
+    stats, _ = native.plan_check(st, cp, pp)
+    assert stats["nodes"] == cp.node_count
+    bad = np.array(cp.surcharge_node_index, copy=True)
+    bad[0] = cp.node_count + 3
+    with pytest.raises(ValueError, match="surcharge entry"):
+        native.plan_check(st, TriangularNodeCouplingTopology(**{**cp.__dict__, "surcharge_node_index": bad}), pp)
+    short = np.asarray(cp.surcharge_return_weight)[:-1]
+    with pytest.raises(ValueError, match="differ in length"):
+        native.plan_check(st, TriangularNodeCouplingTopology(**{**cp.__dict__, "surcharge_return_weight": short}), pp)

@@ -174,6 +174,28 @@ def test_coupled_city_hour_gates_against_oracle():
         assert rmse <= 1e-3 and csi >= 0.995 and abs(verr) <= 5e-4, (k, rmse, csi, verr)
 
 
+def test_surcharge_table_run_gates_against_oracle():
+    """Weighted surcharge-return table (reference triangular_backend.py:1424-1474)
+    through the device loop against the oracle's float64 restatement."""
+
+    from floodgb.synthetic import add_surcharge_table
+
+    sc = coupled_test_city(scale=1, seed=5, duration_min=20.0)
+    add_surcharge_table(sc, seed=2)
+    cfg = load_config(None, sc.overrides)
+    ref = O.run(sc, cfg)
+    prog, (t, h, hu, hv, v), state, led = run_device(sc, cfg)
+    assert prog.error == 0 and ref.error == 0
+    assert ref.ledger["overflow_surcharge_m3"] > 100.0
+    area = np.asarray(sc.city.topologies.surface_topology.cell_area_m2, np.float64)
+    valid = np.asarray(sc.city.mesh.active_mask, bool)
+    for k in range(min(h.shape[0], ref.depth.shape[0])):
+        rmse, csi, verr = gates(h[k], ref.depth[k], area, valid)
+        assert rmse <= 1e-3 and csi >= 0.995 and abs(verr) <= 5e-4, (k, rmse, csi, verr)
+    for n in ("overflow_surcharge_m3", "outfall_discharge_m3", "unreturned_overflow_m3"):
+        np.testing.assert_allclose(led[n], ref.ledger[n], rtol=2e-3, atol=0.5)
+
+
 def test_mass_ledger_closes():
     sc = coupled_test_city(scale=1, seed=7, duration_min=20.0)
     cfg = load_config(None, sc.overrides)
