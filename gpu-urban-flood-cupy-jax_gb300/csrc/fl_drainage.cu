@@ -82,59 +82,47 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
     return fmax32(ff_val(ff_clamp0(V)), 0.0f) / fmax32(A, 1.0e-12f);
 }
 
-// One thread per node: the inlet exchange of its volume.
-__global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs a, int slot) {
-    const StepCtrl s = a.ctrl[slot];
-    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    float led[D1_TERMS] = {0.0f, 0.0f};
-    if (n < a.N) {
-        const float2 V = ff_clamp0(a.Va[n]);
-        const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
-        if (j0 == j1) {
-            a.Vb[n] = V;
-        } else {
-            float sum = 0.0f;
-            for (int j = j0; j < j1; ++j) sum += a.req[a.in_qk[j].x].y;
-            const float sf = fmin32(1.0f, fmax32(ff_val(V), 0.0f) / fmax32(sum, 1.0e-12f));
-            float dv = 0.0f;
-            for (int j = j0; j < j1; ++j) {
-                const int2 qk = a.in_qk[j];
-                const float2 r = a.req[qk.x];
-                const float cap = r.x * a.capf[qk.y];
-                const float sur = r.y * sf;
-                a.capsur[qk.x] = make_float2(cap, sur);
-                dv += cap - sur;
-                led[0] += cap;
-                led[1] += sur;
-            }
-            a.Vb[n] = ff_add(V, dv);
-        }
+// The drainage step's four passes as per-item functions; each kernel below
+// runs one pass with one thread per item.  Values one pass writes and a
+// later one reads (Vb, capsur, T, fac) are read through L2 (ld.cg).
+
+// Node n: the inlet exchange of its volume.
+__device__ __forceinline__ void node_item(const NodeArgs &a, int n, float (&led)[D1_TERMS]) {
+    const float2 V = ff_clamp0(a.Va[n]);
+    const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
+    if (j0 == j1) {
+        a.Vb[n] = V;
+        return;
     }
-    warp_add_ledger<D1_TERMS>(led, a.ledger);
+    float sum = 0.0f;
+    for (int j = j0; j < j1; ++j) sum += a.req[a.in_qk[j].x].y;
+    const float sf = fmin32(1.0f, fmax32(ff_val(V), 0.0f) / fmax32(sum, 1.0e-12f));
+    float dv = 0.0f;
+    for (int j = j0; j < j1; ++j) {
+        const int2 qk = a.in_qk[j];
+        const float2 r = a.req[qk.x];
+        const float cap = r.x * a.capf[qk.y];
+        const float sur = r.y * sf;
+        a.capsur[qk.x] = make_float2(cap, sur);
+        dv += cap - sur;
+        led[0] += cap;
+        led[1] += sur;
+    }
+    a.Vb[n] = ff_add(V, dv);
 }
 
-// One thread per link: the transfer volume from the end volumes after the
-// inlet exchange.
-__global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a, int slot) {
-    const StepCtrl s = a.ctrl[slot];
-    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= a.L) return;
+// Link l: the transfer volume from the end volumes after the inlet exchange.
+__device__ __forceinline__ void link_item(const LinkArgs &a, const StepCtrl &s, int l) {
     const int f = a.link_from[l], to = a.link_to[l];
-    const float df = node_depth(a.Vb[f], a.node_area[f]);
-    const float dtn = node_depth(a.Vb[to], a.node_area[to]);
+    const float df = node_depth(__ldcg(&a.Vb[f]), a.node_area[f]);
+    const float dtn = node_depth(__ldcg(&a.Vb[to]), a.node_area[to]);
     const float *Qin = s.parity ? a.Q1 : a.Q0;
     a.T[l] = link_transfer(a.lk0[l], a.lk1[l], a.lk2[l], df, dtn, Qin[l], a.g, a.wave_speed, s.dt_f);
 }
 
-// One thread per node: its donor factor min(1, V / sum of the transfers it
-// gives), summed in ascending link order.
-__global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs a, int slot) {
-    const StepCtrl s = a.ctrl[slot];
-    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= a.N) return;
+// Node n: its donor factor min(1, V / sum of the transfers it gives), summed
+// in ascending link order.
+__device__ __forceinline__ void donor_item(const DonorArgs &a, int n) {
     const int js = a.node_link_start[n], je = a.node_link_start[n + 1];
     float given = 0.0f;
     for (int j0 = js; j0 < je; j0 += 4) {
@@ -143,7 +131,7 @@ __global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs
         for (int u = 0; u < 4; ++u) e[u] = (j0 + u < je) ? a.nl[j0 + u] : make_int2(-1, 0);
         float t[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) t[u] = e[u].x >= 0 ? a.T[e[u].x] : 0.0f;
+        for (int u = 0; u < 4; ++u) t[u] = e[u].x >= 0 ? __ldcg(&a.T[e[u].x]) : 0.0f;
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (e[u].x < 0) continue;
@@ -151,141 +139,168 @@ __global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs
             if (t[u] >= 0.0f ? (meta & NL_FROM) : (meta & NL_TO)) given += fabsf(t[u]);
         }
     }
-    a.fac[n] = fmin32(1.0f, fmax32(ff_val(ff_clamp0(a.Vb[n])), 0.0f) / fmax32(given, 1.0e-12f));
+    a.fac[n] = fmin32(1.0f, fmax32(ff_val(ff_clamp0(__ldcg(&a.Vb[n]))), 0.0f) / fmax32(given, 1.0e-12f));
+}
+
+// Group g: limited transfers, node continuity, outfall, overflow return and
+// the group cell's final depth.
+__device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, int g, float (&led)[D2_TERMS]) {
+    float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
+    float *Qout = s.parity ? a.Q0 : a.Q1;
+    const float dt = s.dt_f;
+    const int4 gr = a.grp[g];
+    const int c = gr.x, k = gr.y;
+    float h = 0.0f, area = 1.0f;
+    uint32_t cflags = 0u;
+    if (c >= 0) {
+        h = hs[c].x;
+        const float4 ci = a.cinfo[c];
+        area = ci.x;
+        cflags = __float_as_uint(ci.z);
+        if (k >= 0) {  // the cell's inlet exchange, in its inlets' order
+            float dh = 0.0f;
+            for (int q = a.kcell_start[k]; q < a.kcell_start[k + 1]; ++q) {
+                const float2 cs = __ldcg(&a.capsur[q]);
+                dh += (cs.y - cs.x) / area;
+            }
+            h = h + dh;
+        }
+    }
+    float hd = 0.0f;
+    double hd64 = 0.0;  // table mode: the fallback return depth in float64
+    for (int n = gr.z; n < gr.w; ++n) {
+        const float2 Vp = ff_clamp0(__ldcg(&a.Vb[n]));
+        const float fn = __ldcg(&a.fac[n]);
+        const int js = a.node_link_start[n], je = a.node_link_start[n + 1];
+        float dv = 0.0f;
+        for (int j0 = js; j0 < je; j0 += 4) {
+            int2 e[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) e[u] = (j0 + u < je) ? a.nl[j0 + u] : make_int2(-1, 0);
+            float t[4], fo[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (e[u].x >= 0) {
+                    t[u] = __ldcg(&a.T[e[u].x]);
+                    fo[u] = __ldcg(&a.fac[(uint32_t)e[u].y & NL_NODE_MASK]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (e[u].x < 0) continue;
+                const uint32_t meta = (uint32_t)e[u].y;
+                const bool is_from = (meta & NL_FROM) != 0, is_to = (meta & NL_TO) != 0;
+                // donor = the from-node for t >= 0, else the to-node
+                const bool donor_is_from = t[u] >= 0.0f || (is_from && is_to);
+                const bool donor_here = donor_is_from ? is_from : is_to;
+                const float lim = fabsf(t[u]) * (donor_here ? fn : fo[u]);
+                const float sgn = donor_is_from ? lim : -lim;
+                if (is_from) {
+                    dv -= sgn;
+                    Qout[e[u].x] = sgn / fmax32(dt, 1.0e-12f);
+                    led[3] += lim;
+                }
+                if (is_to) dv += sgn;
+            }
+        }
+        float2 V = ff_clamp0(ff_add(Vp, dv));
+        // outfall (reference pipe_outfall_kernel :176-211)
+        const float4 nd = a.nd0[n];
+        const float vol = fmax32(ff_val(V), 0.0f);
+        if (nd.z > 0.0f) {
+            const float dh = nd.y + vol / fmax32(nd.x, 1.0e-12f);
+            const float sgn = (float)((dh > 0.0f) - (dh < 0.0f));
+            float qo = nd.z * sqrtf(2.0f * a.g * fabsf(dh)) * sgn;
+            qo = fmin32(qo, nd.w);
+            const float out = fmin32(vol, fmax32(qo, 0.0f) * dt);
+            V = ff_add(V, -out);
+            led[0] += out;
+        }
+        const float capv = a.nd_capv[n];
+        if (a.table) {
+            // weighted return (reference triangular_backend.py:1424-1474) in
+            // float64: a node with table entries returns overflow x weight
+            // through them (at most its overflow); the others fall back to
+            // their cell
+            const double ovf = fmax((double)V.x + (double)V.y - (double)capv, 0.0);
+            const int e0 = a.node_tstart[n], e1 = a.node_tstart[n + 1];
+            double r = 0.0;
+            if (e1 > e0) {
+                for (int e = e0; e < e1; ++e) r += ovf * (double)a.node_tw[e];
+                r = fmin(r, ovf);
+                a.ovf_node[n] = ovf;
+            } else if (c >= 0) {
+                r = ovf;
+                hd64 += r / (double)area;
+            }
+            if (r > 0.0) {
+                const float rh = (float)r;
+                V = ff_add(ff_add(V, -rh), -(float)(r - (double)rh));
+                led[1] += rh;
+            }
+        } else {
+            // overflow return (reference node_overflow_return_kernel :179-207)
+            const float ovf = fmax32(ff_val(V) - capv, 0.0f);
+            if (c >= 0 && ovf > 0.0f) {
+                V = ff_add(V, -ovf);
+                hd += ovf / area;
+                led[1] += ovf;
+            }
+        }
+        led[2] += fmax32(ff_val(V) - capv, 0.0f);
+        a.Va[n] = V;
+        if (s.snap_slot >= 0) a.snap_v[(size_t)s.snap_slot * (size_t)a.N + n] = ff_val(V);
+    }
+    if (c >= 0 && a.table && (cflags & CELL_SURCHARGE)) {
+        // k_surcharge adds the table's return first, then this fallback
+        hs[c].x = h;
+        int lo = 0, hi = a.U;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (a.tcell[mid] < c) lo = mid + 1; else hi = mid;
+        }
+        a.s2[lo] = hd64;
+    } else if (c >= 0) {
+        const float hf = a.table ? (float)((double)h + hd64) : h + hd;
+        hs[c].x = hf;
+        // a recharge cell is finished by k_recharge
+        const bool fin = !(a.has_recharge && (s.phases & FL_PHASE_RECHARGE) && (cflags & CELL_RECHARGE));
+        if (fin) {
+            if ((s.phases & FL_PHASE_SURFACE) && a.forcing_kind == 1) a.wet[c] = a.wet[c] + dt * (float)(hf > a.md);
+            if (s.snap_slot >= 0) a.snap_h[(size_t)s.snap_slot * (size_t)a.C + c] = hf;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs a, int slot) {
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    float led[D1_TERMS] = {0.0f, 0.0f};
+    if (n < a.N) node_item(a, n, led);
+    warp_add_ledger<D1_TERMS>(led, a.ledger);
+}
+
+__global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a, int slot) {
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l < a.L) link_item(a, s, l);
+}
+
+__global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs a, int slot) {
+    const StepCtrl s = a.ctrl[slot];
+    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < a.N) donor_item(a, n);
 }
 
 __global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs a, int slot) {
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
-    float *Qout = s.parity ? a.Q0 : a.Q1;
-    const float dt = s.dt_f;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     float led[D2_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (g < a.G) {
-        const int4 gr = a.grp[g];
-        const int c = gr.x, k = gr.y;
-        float h = 0.0f, area = 1.0f;
-        uint32_t cflags = 0u;
-        if (c >= 0) {
-            h = hs[c].x;
-            const float4 ci = a.cinfo[c];
-            area = ci.x;
-            cflags = __float_as_uint(ci.z);
-            if (k >= 0) {  // the cell's inlet exchange, in its inlets' order
-                float dh = 0.0f;
-                for (int q = a.kcell_start[k]; q < a.kcell_start[k + 1]; ++q) {
-                    const float2 cs = a.capsur[q];
-                    dh += (cs.y - cs.x) / area;
-                }
-                h = h + dh;
-            }
-        }
-        float hd = 0.0f;
-        double hd64 = 0.0;  // table mode: the fallback return depth in float64
-        for (int n = gr.z; n < gr.w; ++n) {
-            const float2 Vp = ff_clamp0(a.Vb[n]);
-            const float fn = a.fac[n];
-            const int js = a.node_link_start[n], je = a.node_link_start[n + 1];
-            float dv = 0.0f;
-            for (int j0 = js; j0 < je; j0 += 4) {
-                int2 e[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) e[u] = (j0 + u < je) ? a.nl[j0 + u] : make_int2(-1, 0);
-                float t[4], fo[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    if (e[u].x >= 0) {
-                        t[u] = a.T[e[u].x];
-                        fo[u] = a.fac[(uint32_t)e[u].y & NL_NODE_MASK];
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    if (e[u].x < 0) continue;
-                    const uint32_t meta = (uint32_t)e[u].y;
-                    const bool is_from = (meta & NL_FROM) != 0, is_to = (meta & NL_TO) != 0;
-                    // donor = the from-node for t >= 0, else the to-node
-                    const bool donor_is_from = t[u] >= 0.0f || (is_from && is_to);
-                    const bool donor_here = donor_is_from ? is_from : is_to;
-                    const float lim = fabsf(t[u]) * (donor_here ? fn : fo[u]);
-                    const float sgn = donor_is_from ? lim : -lim;
-                    if (is_from) {
-                        dv -= sgn;
-                        Qout[e[u].x] = sgn / fmax32(dt, 1.0e-12f);
-                        led[3] += lim;
-                    }
-                    if (is_to) dv += sgn;
-                }
-            }
-            float2 V = ff_clamp0(ff_add(Vp, dv));
-            // outfall (reference pipe_outfall_kernel :176-211)
-            const float4 nd = a.nd0[n];
-            const float vol = fmax32(ff_val(V), 0.0f);
-            if (nd.z > 0.0f) {
-                const float dh = nd.y + vol / fmax32(nd.x, 1.0e-12f);
-                const float sgn = (float)((dh > 0.0f) - (dh < 0.0f));
-                float qo = nd.z * sqrtf(2.0f * a.g * fabsf(dh)) * sgn;
-                qo = fmin32(qo, nd.w);
-                const float out = fmin32(vol, fmax32(qo, 0.0f) * dt);
-                V = ff_add(V, -out);
-                led[0] += out;
-            }
-            const float capv = a.nd_capv[n];
-            if (a.table) {
-                // weighted return (reference triangular_backend.py:1424-1474) in
-                // float64: a node with table entries returns overflow x weight
-                // through them (at most its overflow); the others fall back to
-                // their cell
-                const double ovf = fmax((double)V.x + (double)V.y - (double)capv, 0.0);
-                const int e0 = a.node_tstart[n], e1 = a.node_tstart[n + 1];
-                double r = 0.0;
-                if (e1 > e0) {
-                    for (int e = e0; e < e1; ++e) r += ovf * (double)a.node_tw[e];
-                    r = fmin(r, ovf);
-                    a.ovf_node[n] = ovf;
-                } else if (c >= 0) {
-                    r = ovf;
-                    hd64 += r / (double)area;
-                }
-                if (r > 0.0) {
-                    const float rh = (float)r;
-                    V = ff_add(ff_add(V, -rh), -(float)(r - (double)rh));
-                    led[1] += rh;
-                }
-            } else {
-                // overflow return (reference node_overflow_return_kernel :179-207)
-                const float ovf = fmax32(ff_val(V) - capv, 0.0f);
-                if (c >= 0 && ovf > 0.0f) {
-                    V = ff_add(V, -ovf);
-                    hd += ovf / area;
-                    led[1] += ovf;
-                }
-            }
-            led[2] += fmax32(ff_val(V) - capv, 0.0f);
-            a.Va[n] = V;
-            if (s.snap_slot >= 0) a.snap_v[(size_t)s.snap_slot * (size_t)a.N + n] = ff_val(V);
-        }
-        if (c >= 0 && a.table && (cflags & CELL_SURCHARGE)) {
-            // k_surcharge adds the table's return first, then this fallback
-            hs[c].x = h;
-            int lo = 0, hi = a.U;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (a.tcell[mid] < c) lo = mid + 1; else hi = mid;
-            }
-            a.s2[lo] = hd64;
-        } else if (c >= 0) {
-            const float hf = a.table ? (float)((double)h + hd64) : h + hd;
-            hs[c].x = hf;
-            // a recharge cell is finished by k_recharge
-            const bool fin = !(a.has_recharge && (s.phases & FL_PHASE_RECHARGE) && (cflags & CELL_RECHARGE));
-            if (fin) {
-                if ((s.phases & FL_PHASE_SURFACE) && a.forcing_kind == 1) a.wet[c] = a.wet[c] + dt * (float)(hf > a.md);
-                if (s.snap_slot >= 0) a.snap_h[(size_t)s.snap_slot * (size_t)a.C + c] = hf;
-            }
-        }
-    }
+    if (g < a.G) group_item(a, s, g, led);
     warp_add_ledger<D2_TERMS>(led, a.ledger);
 }
 

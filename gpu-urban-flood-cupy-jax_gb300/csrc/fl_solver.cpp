@@ -316,7 +316,8 @@ static int error_code_message(FlSolver *s) {
     if (r.error == FL_E_SNAPSHOTS) return set_error(FL_E_SNAPSHOTS, "more than %d snapshots requested", r.max_snaps);
     if (r.error == FL_E_INVALID) return set_error(FL_E_INVALID, "No finite cells are available for timestep calculation.");
     if (r.error == FL_E_TIMEOUT)
-        return set_error(FL_E_TIMEOUT, "a tile copy of the surface kernel did not complete within its time limit at step %lld",
+        return set_error(FL_E_TIMEOUT,
+                         "a tile copy of the surface kernel did not complete within its time limit at step %lld",
                          (long long)r.error_step);
     if (r.error) return set_error(r.error, "device error %d at step %lld", r.error, (long long)r.error_step);
     return FL_OK;

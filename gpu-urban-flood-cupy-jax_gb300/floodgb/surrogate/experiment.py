@@ -42,10 +42,12 @@ def _mesh(grid_n: int, seed: int):
 
 
 def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: float = 0.05, seed: int = 0,
-           plain_sample: int = 8, batch_size: int = 64, baselines: bool = False, n_layers: int = 8) -> dict:
+           plain_sample: int = 8, batch_size: int = 64, baselines: bool = False, n_layers: int = 8,
+           score_all: bool = True) -> dict:
     """Screen an ensemble: surrogate rollouts of every member, flags, a random
     audit; the solver re-runs flagged + audited members (timed) and judges
-    every member; the plain single-instance solver is timed on a sample."""
+    every member (or, with score_all False, the re-run members only); the
+    plain single-instance solver is timed on a sample."""
 
     import torch
 
@@ -71,13 +73,24 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
         audited[rng.choice(cand, size=min(int(np.ceil(audit * n)), cand.size), replace=False)] = True
     idx = np.flatnonzero(flagged | audited)
     rerun_s, rerun_h = 0.0, 0.0
+    reruns = []
     if idx.size:
-        _, rerun_s, rerun_h = solve_members(city, cfg, [storms[i] for i in idx], [durations[i] for i in idx],
-                                            batch_size)
-    truth, batched_s, _ = solve_members(city, cfg, storms, durations, batch_size)
-    scores = [score(mf, p, tr) for p, tr in zip(preds, truth)]
+        reruns, rerun_s, rerun_h = solve_members(city, cfg, [storms[i] for i in idx], [durations[i] for i in idx],
+                                                 batch_size)
+    if score_all:
+        truth, batched_s, _ = solve_members(city, cfg, storms, durations, batch_size)
+        scores = [score(mf, p, tr) for p, tr in zip(preds, truth)]
+        scored = np.ones(n, bool)
+    else:
+        truth, batched_s = None, None
+        scores = [None] * n
+        for j, i in enumerate(idx):
+            scores[i] = score(mf, preds[i], reruns[j])
+        scored = flagged | audited
+    del reruns
 
     def agg(mask):
+        mask = mask & scored
         if not mask.any():
             return None
         sel = [scores[i] for i in np.flatnonzero(mask)]
@@ -85,8 +98,9 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
             "max_rmse_hmax_m": float(np.max([s["rmse_hmax_m"] for s in sel])), "members": int(mask.sum())}
 
     res = {"members": n, "scenario_hours": hours, "flagged": int(flagged.sum()), "audited": int(audited.sum()),
+           "scored": "all members" if score_all else "flagged and audited members (solver re-runs)",
            "surrogate_accepted": agg(~flagged), "surrogate_flagged": agg(flagged), "audit_scores": agg(audited)}
-    if baselines:
+    if baselines and truth is not None:
         # what the trained network gains: an untrained network and "the depth does not change"
         p0 = rollout_batch(MPNN(n_layers=n_layers, seed=seed + 99), mf, storms, durations, copies=copies)
         zero = [(p[0], np.zeros_like(p[1]), np.zeros_like(p[2])) for p in preds]
@@ -106,7 +120,7 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
     screen_s = surr_s + rerun_s
     res["throughput_scenario_h_per_s"] = {
         "plain_single_instance": plain_rate,
-        "batched_solver": hours / batched_s,
+        "batched_solver": hours / batched_s if batched_s else (rerun_h / rerun_s if rerun_s else None),
         "surrogate_only": hours / surr_s,
         "screening": hours / screen_s,
         "screening_over_plain": (hours / screen_s) / plain_rate,
@@ -176,7 +190,8 @@ def load(path):
     return model, json.loads(str(z["limits"])), meta
 
 
-def screen_saved(path, n_eval: int = 64, plain_sample: int = 2, audit: float = 0.05, duration_cap_h=None) -> dict:
+def screen_saved(path, n_eval: int = 64, plain_sample: int = 2, audit: float = 0.05, duration_cap_h=None,
+                 score_all: bool = True) -> dict:
     """Screen the first n_eval held-out storms of the saved model's mesh and seed."""
 
     from .pipeline import MeshFeatures
@@ -186,7 +201,7 @@ def screen_saved(path, n_eval: int = 64, plain_sample: int = 2, audit: float = 0
     mf = MeshFeatures(city.topologies.surface_topology)
     storms, dur = _storms(n_eval, int(meta["seed"]) + 2, duration_cap_h)
     res = screen(model, mf, city, cfg, limits, storms, dur, audit=audit, seed=int(meta["seed"]),
-                 plain_sample=plain_sample)
+                 plain_sample=plain_sample, score_all=score_all)
     res["mesh_cells"] = mf.C
     return res
 
