@@ -86,22 +86,41 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
 // runs one pass with one thread per item.  Values one pass writes and a
 // later one reads (Vb, capsur, T, fac) are read through L2 (ld.cg).
 
-// Node n: the inlet exchange of its volume.
-__device__ __forceinline__ void node_item(const NodeArgs &a, int n, float (&led)[D1_TERMS]) {
+// Capture limit factor of inlet cell k at depth h: its volume over the summed
+// capture requests of its inlets, in their order (reference :133-177).
+__device__ __forceinline__ float cell_capture_factor(const InletReqView &v, int k, float h, float area, float dt) {
+    float sum = 0.0f;
+    for (int q = v.kcell_start[k]; q < v.kcell_start[k + 1]; ++q)
+        sum += inlet_request(v, q, h, ff_clamp0(v.Va[v.in_node[q]]), dt).x;
+    return fmin32(1.0f, (fmax32(h, 0.0f) * area) / fmax32(sum, 1.0e-12f));
+}
+
+// Node n: the requests of its inlets from the depth the surface step left in
+// their cells (reference inlet_exchange_request_kernel :52-131), captures
+// limited by each cell's volume, surcharges by the node's, and the node
+// volume after the exchange.
+__device__ __forceinline__ void node_item(const NodeArgs &a, const StepCtrl &s, int n, float (&led)[D1_TERMS]) {
     const float2 V = ff_clamp0(a.Va[n]);
     const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
     if (j0 == j1) {
         a.Vb[n] = V;
         return;
     }
+    const float4 *hs = s.parity ? a.state0 : a.state1;  // written by the surface step
+    const float dt = s.dt_f;
     float sum = 0.0f;
-    for (int j = j0; j < j1; ++j) sum += a.req[a.in_qk[j].x].y;
+    for (int j = j0; j < j1; ++j) {
+        const int2 qk = a.in_qk[j];
+        sum += inlet_request(a.inl, qk.x, hs[a.kcell_cell[qk.y]].x, V, dt).y;
+    }
     const float sf = fmin32(1.0f, fmax32(ff_val(V), 0.0f) / fmax32(sum, 1.0e-12f));
     float dv = 0.0f;
     for (int j = j0; j < j1; ++j) {
         const int2 qk = a.in_qk[j];
-        const float2 r = a.req[qk.x];
-        const float cap = r.x * a.capf[qk.y];
+        const int c = a.kcell_cell[qk.y];
+        const float h = hs[c].x;
+        const float2 r = inlet_request(a.inl, qk.x, h, V, dt);
+        const float cap = r.x * cell_capture_factor(a.inl, qk.y, h, a.cinfo[c].x, dt);
         const float sur = r.y * sf;
         a.capsur[qk.x] = make_float2(cap, sur);
         dv += cap - sur;
@@ -277,7 +296,7 @@ __global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs 
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     float led[D1_TERMS] = {0.0f, 0.0f};
-    if (n < a.N) node_item(a, n, led);
+    if (n < a.N) node_item(a, s, n, led);
     warp_add_ledger<D1_TERMS>(led, a.ledger);
 }
 

@@ -9,9 +9,8 @@
 //               (the reference adds them with atomicAdd)           [:172-189]
 //   k_li_cells  one thread per cell: the gathered volume change, momentum
 //               from the face discharges, then the same sources, clamp,
-//               external inflow, inlet requests, wet time and snapshots as
-//               the full-SWE surface kernel; its last block plans the next
-//               step                                               [:194-262]
+//               external inflow, wet time and snapshots as the full-SWE
+//               surface kernel; its last block plans the next step [:194-262]
 // Compiled with -fmad=false: the discharge arithmetic is rounded as written.
 #include <cuda_runtime.h>
 
@@ -162,18 +161,6 @@ __global__ void __launch_bounds__(256) k_li_cells(const __grid_constant__ LiArgs
         if (s.phases & FL_PHASE_CLAMP) clamp_velocity_exact(hn, hun, hvn, a.vmax);
         if ((info & CELL_RECEIVER) && (s.phases & FL_PHASE_INFLOW)) hn = __fadd_rn(hn, a.ext_add[c]);
         out[c] = make_float4(hn, hun, hvn, st.w);
-        // the inlet requests of the cell and its capture limit factor, as in k_surface
-        const uint32_t kc = __float_as_uint(ci.w);
-        if (kc && drain_finishes && a.has_inlets) {
-            const InletReqView &v = a.inl;
-            float sum = 0.0f;
-            for (int q = v.kcell_start[kc - 1]; q < v.kcell_start[kc]; ++q) {
-                const float2 r = inlet_request(v, q, hn, ff_clamp0(v.Va[v.in_node[q]]), dt);
-                v.req[q] = r;
-                sum += r.x;
-            }
-            v.capf[kc - 1] = fmin32(1.0f, (fmax32(hn, 0.0f) * ci.x) / fmax32(sum, 1.0e-12f));
-        }
         const bool final_here = !(drain_finishes && (info & CELL_COUPLED)) &&
                                 !(recharge_finishes && (info & CELL_RECHARGE));
         if (KIND == 1 && do_surface && final_here) a.wet[c] = wt + dt * (float)(hn > md);

@@ -115,8 +115,6 @@ struct InletReqView {
     const int32_t *in_node;       // [I] cell order
     const float4 *in_par;         // [I] {bed - invert, capture capacity, surcharge capacity, node storage area}
     const float2 *Va;             // node volume (float-float) at the start of the drainage step
-    float2 *req;                  // [I] cell order: requested {capture, surcharge}
-    float *capf;                  // [K] capture limit factor of each inlet cell
     int32_t rule;
     float coef_area;              // float32(Cd * A_orifice)
     float weir_coef_perim;        // float32(Cw * perimeter) for weir_orifice
@@ -163,8 +161,6 @@ struct SurfArgs {
     float infil_scalar;
     float g, half_g, md, vmax, stage;
     int32_t has_stage;
-    int32_t has_inlets;
-    InletReqView inl;
     const float *ext_add;         // [Cp] external inflow depth of receiver cells this step
 };
 
@@ -194,10 +190,8 @@ struct LiArgs {
     float2 *ledger;               // [warps * SURF_TERMS] of the cell kernel
     float *snap_h, *snap_hu, *snap_hv;
     const float *ext_add;
-    InletReqView inl;
     int32_t E, C;
     int32_t forcing_kind;
-    int32_t has_inlets;
     float infil_scalar, g, md, vmax;
 };
 
@@ -220,8 +214,10 @@ struct DtArgs {
 struct NodeArgs {
     const int32_t *node_in_start; // [N + 1] inlet range (node order)
     const int2 *in_qk;            // [I] node order: {inlet in cell order, its inlet cell}
-    const float2 *req;            // [I] cell order requested {capture, surcharge}
-    const float *capf;            // [K]
+    InletReqView inl;             // inlet parameters and the per-cell inlet ranges
+    const int32_t *kcell_cell;    // [K] the cell of each inlet cell index
+    const float4 *cinfo;
+    const float4 *state0, *state1;  // the surface step's output holds the inlet cells' depth
     float2 *capsur;               // [I] cell order: granted {capture, surcharge}
     const float2 *Va;             // node volume before the exchange
     float2 *Vb;                   // after

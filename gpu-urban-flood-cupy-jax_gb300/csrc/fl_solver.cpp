@@ -562,34 +562,32 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         s->d2_blocks = network_blocks(s->G);
         s->n_led_1 = (size_t)s->d1_blocks * 4 * D1_TERMS;
         s->n_led_2 = (size_t)s->d2_blocks * 4 * D2_TERMS;
-        float *T, *fac, *capf;
-        float2 *req, *capsur;
+        float *T, *fac;
+        float2 *capsur;
+        int32_t *kcell_cell;
         if ((rc = s->alloc(&s->led_1, s->n_led_1)) || (rc = s->alloc(&s->led_2, s->n_led_2)) ||
             (rc = s->alloc(&T, s->NL)) || (rc = s->alloc(&fac, s->N)) || (rc = s->alloc(&capsur, s->I)) ||
-            (rc = s->alloc(&req, s->I)) || (rc = s->alloc(&capf, s->K)))
+            (rc = s->upload(&kcell_cell, L.kcell_cell)))
             return rc;
-        FL_CUDA(cudaMemset(req, 0, sizeof(float2) * std::max(s->I, 1)));
         FL_CUDA(cudaMemset(capsur, 0, sizeof(float2) * std::max(s->I, 1)));
-        FL_CUDA(cudaMemset(capf, 0, sizeof(float) * std::max(s->K, 1)));
-        InletReqView &v = s->sa.inl;
+        InletReqView &v = s->nd.inl;
         v.kcell_start = kcell_start;
         v.in_node = in_node;
         v.in_par = in_par;
         v.Va = s->Va;
-        v.req = req;
-        v.capf = capf;
         v.rule = drain->inlet_capture_rule;
         v.coef_area = drain->inlet_orifice_coefficient * drain->inlet_orifice_area_m2;
         const float eq = sqrtf(4.0f * 3.14159265358979323846f * std::max(drain->inlet_orifice_area_m2, 0.0f));
         const float perim = drain->inlet_weir_perimeter_m > 0.0f ? drain->inlet_weir_perimeter_m : eq;
         v.weir_coef_perim = drain->inlet_weir_coefficient * std::max(perim, 0.0f);
         v.g2 = (float)(2.0 * (double)(float)p.gravity_mps2);
-        s->sa.has_inlets = s->I > 0;
         NodeArgs &a = s->nd;
         a.node_in_start = node_in_start;
         a.in_qk = in_qk;
-        a.req = req;
-        a.capf = capf;
+        a.kcell_cell = kcell_cell;
+        a.cinfo = cinfo;
+        a.state0 = s->state[0];
+        a.state1 = s->state[1];
         a.capsur = capsur;
         a.Va = s->Va;
         a.Vb = s->Vb;
@@ -799,11 +797,9 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         q.snap_hu = s->snap_hu;
         q.snap_hv = s->snap_hv;
         q.ext_add = nullptr;
-        q.inl = s->sa.inl;
         q.E = E;
         q.C = C;
         q.forcing_kind = s->kind;
-        q.has_inlets = s->sa.has_inlets;
         q.infil_scalar = forcing->infiltration_mps;
         q.g = (float)p.gravity_mps2;
         q.md = (float)p.min_depth_m;

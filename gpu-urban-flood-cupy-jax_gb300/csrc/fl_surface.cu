@@ -200,21 +200,6 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
             // external boundary inflow after the clamp (reference engine.py:263-273)
             if ((info & CELL_RECEIVER) && (s.phases & FL_PHASE_INFLOW)) hn = __fadd_rn(hn, a.ext_add[c]);
             out[c] = make_float4(hn, hun, hvn, st.w);
-            // requested inlet capture / surcharge of this cell's inlets, from the
-            // depth the drainage step starts with, and the cell's capture limit
-            // factor: its volume over the summed capture requests (reference
-            // :52-177)
-            const uint32_t kc = __float_as_uint(ci.w);
-            if (kc && drain_finishes && a.has_inlets) {
-                const InletReqView &v = a.inl;
-                float sum = 0.0f;
-                for (int q = v.kcell_start[kc - 1]; q < v.kcell_start[kc]; ++q) {
-                    const float2 r = inlet_request(v, q, hn, ff_clamp0(v.Va[v.in_node[q]]), dt);
-                    v.req[q] = r;
-                    sum += r.x;
-                }
-                v.capf[kc - 1] = fmin32(1.0f, (fmax32(hn, 0.0f) * ci.x) / fmax32(sum, 1.0e-12f));
-            }
             const bool final_here = !(drain_finishes && (info & CELL_COUPLED)) &&
                                     !(recharge_finishes && (info & CELL_RECHARGE));
             if (KIND == 1 && do_surface && final_here) a.wet[c] = wt + dt * (float)(hn > md);
