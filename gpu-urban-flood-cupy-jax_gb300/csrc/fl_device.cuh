@@ -375,6 +375,18 @@ __device__ __forceinline__ void warp_add_ledger(const float (&v)[NT], float2 *le
     }
 }
 
+// The same with an explicit warp index (kernels whose warps do not all add).
+template <int NT>
+__device__ __forceinline__ void warp_add_ledger_at(const float (&v)[NT], float2 *ledger, int warp) {
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        float x = v[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) ff_accumulate(&ledger[(size_t)warp * NT + j], x);
+    }
+}
+
 // --------------------------------------------------------------- async copies
 // Bulk (TMA engine) copies global -> shared completing on an mbarrier, and
 // 16-byte cp.async gathers.  Every wait on an mbarrier is bounded in time.
@@ -394,6 +406,16 @@ __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier
 
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// One arrive on the barrier when all of this thread's earlier cp.async
+// copies have landed (the barrier's expected count includes it).
+__device__ __forceinline__ void cp_async_arrive_noinc(uint32_t bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {

@@ -26,6 +26,7 @@ namespace fl {
 // {nx, ny, len, bits}:
 // ---------------------------------------------------------------------------
 constexpr int TILE = 256;
+constexpr int SURF_THREADS = TILE + 32;  // surface kernel: 8 compute warps + 1 producer warp
 constexpr uint32_t EB_IDX_MASK = 1023u;    // bits 0-9: left local index
 constexpr int EB_RIGHT_SHIFT = 10;         // bits 10-19: right local index
 constexpr int EB_LSLOT_SHIFT = 20;         // bits 20-21: the edge's slot in the left cell

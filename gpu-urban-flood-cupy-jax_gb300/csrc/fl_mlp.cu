@@ -287,14 +287,6 @@ __global__ void __launch_bounds__(MM_THREADS, 1) k_gemm_bf16(const __grid_consta
 constexpr int PG_PROD_WARPS = 2, PG_EPI_WARPS = 8, PG_THREADS = 32 * (PG_PROD_WARPS + 1 + PG_EPI_WARPS);
 constexpr int PG_MAX_STAGES = 8, PG_MAX_K = 512, PG_SMEM_LIMIT = 227 * 1024;
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_arrive_noinc(uint32_t bar) {
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
-}
-
 // Source rows of the four tile rows (lane, lane + 32, ...) a producer lane
 // copies, per segment; -1 past the end.  Loaded once per tile so the chunk
 // copies do not wait on index loads.

@@ -294,7 +294,7 @@ int surface_smem_layout(SurfArgs &a, int kind) {
     auto up = [](int x, int m) { return (x + m - 1) / m * m; };
     const int flux = TILE * 3 * 16;
     a.off_bar = flux;
-    a.off_stage = up(flux + 64, 128);
+    a.off_stage = up(flux + 128, 128);  // barriers (6 x 8 B) and the two tile records (2 x 16 B)
     int o = (TILE + a.h_cap) * 16;
     a.so_ci = o;
     o += TILE * 16;

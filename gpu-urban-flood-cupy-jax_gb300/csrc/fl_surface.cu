@@ -84,18 +84,41 @@ __device__ __forceinline__ void issue_tile(const SurfArgs &a, const float4 *in, 
     if (halo_bytes) bulk_copy_g2s(smem_addr(S.hs), a.halo_src + ti.z, halo_bytes, bar);
 }
 
-// Gather the halo states of a staged tile (all threads; after its copy landed).
-__device__ __forceinline__ void gather_halo(const float4 *in, const TileStage &S, int halo_count) {
-    for (int j = threadIdx.x; j < halo_count; j += TILE) cp_async16(smem_addr(&S.st[TILE + j]), in + S.hs[j]);
-    cp_async_commit();
+// Named barrier and barrier-reduction among the compute warps only (id 1).
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(TILE) : "memory"); }
+
+__device__ __forceinline__ bool compute_all(bool p) {
+    uint32_t r;
+    asm volatile(
+        "{\n"
+        ".reg .pred pi, po;\n"
+        "setp.ne.u32 pi, %1, 0;\n"
+        "bar.red.and.pred po, 1, %2, pi;\n"
+        "selp.u32 %0, 1, 0, po;\n"
+        "}\n"
+        : "=r"(r)
+        : "r"((uint32_t)p), "n"(TILE)
+        : "memory");
+    return r != 0;
 }
 
+// Warp-specialised persistent surface kernel: 8 compute warps (one thread
+// per cell of a 256-cell tile) and one producer warp.  The producer fills the
+// two stages: bulk copies (TMA engine) of a tile's states, cell info, Horton
+// fields, wet time, edge entries and halo list onto stage barrier full[s],
+// then, once they land, the halo state gathers (cp.async, one arrive per lane
+// on halo[s] when they land).  The compute warps wait on full[s] and halo[s],
+// run phase 2 (each edge entry once: flux into per-(cell, slot) places) and
+// phase 3 (the cell update), and release the stage on empty[s].  Loads of
+// the next tile therefore overlap both compute phases of the current one.
+// Every wait is bounded (1 s): a timeout records FL_E_TIMEOUT and the CTA
+// leaves after its copies in flight have landed (or a second bounded wait).
 template <int KIND>
-__global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
+__global__ void __launch_bounds__(SURF_THREADS, 4) k_surface(const __grid_constant__ SurfArgs a, int slot, int plan_next) {
     extern __shared__ __align__(128) unsigned char smem[];
     float4 *s_flux = (float4 *)smem;  // [TILE * 3] per (cell, slot): {mass, x-mom, y-mom} x len
-    uint64_t *s_bar = (uint64_t *)(smem + a.off_bar);
-    int4 *s_info = (int4 *)(smem + a.off_bar + 16);
+    uint64_t *s_bar = (uint64_t *)(smem + a.off_bar);  // full[2], halo[2], empty[2]
+    int4 *s_info = (int4 *)(smem + a.off_bar + 48);
     const int tid = threadIdx.x;
     const int ncta = (int)gridDim.x - 1;  // the last CTA plans
     if ((int)blockIdx.x == ncta) {
@@ -106,48 +129,80 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
     if (!s.active) return;
     const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
     float4 *__restrict__ out = s.parity ? a.state0 : a.state1;
+    // barrier addresses: full(s) = base + 8 s, halo(s) = base + 16 + 8 s, empty(s) = base + 32 + 8 s
+    const uint32_t bar_base = smem_addr(s_bar);
+    const TileStage S0 = stage_at(a, smem, 0), S1 = stage_at(a, smem, 1);
+    if (tid < TILE) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) s_flux[tid * 3 + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (tid == 0) {
+        for (int k = 0; k < 2; ++k) {
+            mbar_init(bar_base + 8u * k, 1);
+            mbar_init(bar_base + 16u + 8u * k, 32);
+            mbar_init(bar_base + 32u + 8u * k, 1);
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();  // the last block-wide barrier: the roles split here
+
+    if (tid >= TILE) {
+        // ---------------------------------------------------------- producer
+        const int lane = tid - TILE;
+        bool failed = false;
+        int i = 0;
+        for (int t = blockIdx.x; t < a.n_tiles; t += ncta, ++i) {
+            const int st = i & 1;
+            const TileStage &S = st ? S1 : S0;
+            if (i >= 2) {  // the compute warps released this stage's previous tile
+                bool ok = true;
+                if (lane == 0) ok = mbar_wait_bounded((bar_base + 32u + 8u * st), ((i >> 1) - 1) & 1u, COPY_WAIT_NS);
+                if (!__shfl_sync(0xffffffffu, ok, 0)) {
+                    failed = true;
+                    break;
+                }
+            }
+            if (lane == 0) issue_tile<KIND>(a, in, S, &s_info[st], (bar_base + 8u * st), t);
+            // every lane waits: each then reads the landed halo list itself
+            const bool ok = mbar_wait_bounded((bar_base + 8u * st), (i >> 1) & 1u, COPY_WAIT_NS);
+            if (!__all_sync(0xffffffffu, ok)) {
+                // a copy is late: one more bounded wait so none lands after the CTA leaves
+                (void)mbar_wait_bounded((bar_base + 8u * st), (i >> 1) & 1u, COPY_WAIT_NS);
+                failed = true;
+                break;
+            }
+            const int hc = s_info[st].w;
+            for (int j = lane; j < hc; j += 32) cp_async16(smem_addr(&S.st[TILE + j]), in + S.hs[j]);
+            cp_async_arrive_noinc((bar_base + 16u + 8u * st));
+        }
+        cp_async_wait_all();
+        if (failed && lane == 0) {
+            if (atomicCAS(&a.run->error, 0, FL_E_TIMEOUT) == 0) a.run->error_step = s.step;
+        }
+        return;
+    }
+
+    // ------------------------------------------------------------- compute
     const float dt = s.dt_f;
     const float md = a.md;
     const bool do_surface = (s.phases & FL_PHASE_SURFACE) != 0;
     const bool drain_finishes = (s.phases & FL_PHASE_DRAINAGE) != 0;
     const bool recharge_finishes = (s.phases & FL_PHASE_RECHARGE) != 0;
     float led[SURF_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
-
-    const uint32_t bar0 = smem_addr(&s_bar[0]), bar1 = smem_addr(&s_bar[1]);
-    const TileStage S0 = stage_at(a, smem, 0), S1 = stage_at(a, smem, 1);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) s_flux[tid * 3 + k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    uint32_t wpar = 0u;     // bit k: parity of the next wait on stage k's barrier
-    uint32_t pending = 0u;  // bit k: stage k has copies issued and not yet waited for (thread 0)
-    if (tid == 0) {
-        mbar_init(bar0, 1);
-        mbar_init(bar1, 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    int t = blockIdx.x;
-    if (tid == 0) {
-        issue_tile<KIND>(a, in, S0, &s_info[0], bar0, t);
-        pending = 1u;
-    }
-    bool timed_out = !mbar_wait_bounded(bar0, 0, COPY_WAIT_NS);
-    wpar ^= 1u;
-    if (__syncthreads_or(timed_out)) goto abort;
-    pending = 0u;
-    gather_halo(in, S0, s_info[0].w);
-
-    for (int i = 0; t < a.n_tiles; ++i, t += ncta) {
+    int i = 0;
+    for (int t = blockIdx.x; t < a.n_tiles; t += ncta, ++i) {
         const int st_i = i & 1;
         const TileStage &S = st_i ? S1 : S0;
-        const TileStage &SN = st_i ? S0 : S1;
-        const uint32_t barN = st_i ? bar0 : bar1;
-        const int tn = t + ncta;
-        if (tid == 0 && tn < a.n_tiles) {
-            issue_tile<KIND>(a, in, SN, &s_info[st_i ^ 1], barN, tn);
-            pending |= 1u << (st_i ^ 1);
+        // one thread waits for the tile's copies and gathers; the barrier
+        // reduction hands them to the other compute threads
+        bool ok = true;
+        if (tid == 0)
+            ok = mbar_wait_bounded((bar_base + 8u * st_i), (i >> 1) & 1u, COPY_WAIT_NS) &&
+                 mbar_wait_bounded((bar_base + 16u + 8u * st_i), (i >> 1) & 1u, COPY_WAIT_NS);
+        if (!compute_all(ok)) {
+            if (tid == 0 && atomicCAS(&a.run->error, 0, FL_E_TIMEOUT) == 0) a.run->error_step = s.step;
+            break;  // the producer waits out its own copies
         }
-        cp_async_wait_all();
-        __syncthreads();  // this tile's halo states are in place
 
         // phase 2: each edge entry of the tile once
         const int c0 = t * TILE;
@@ -157,16 +212,7 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
             for (int e = tid; e < n_e; e += TILE)
                 tile_entry(S.en[e], S.st, s_flux, a.g, a.half_g, md, a.stage, dt, led[2], led[3]);
         }
-        // the next tile's copies: wait for them here (they had all of phase 2)
-        // and start its halo gathers, which then overlap phase 3
-        bool bad = false;
-        if (tn < a.n_tiles) {
-            bad = !mbar_wait_bounded(barN, (wpar >> (st_i ^ 1)) & 1u, COPY_WAIT_NS);
-            wpar ^= 1u << (st_i ^ 1);
-        }
-        if (__syncthreads_or(bad)) goto abort;  // also: phase 2's slots are complete
-        pending = 0u;
-        if (tn < a.n_tiles) gather_halo(in, SN, s_info[st_i ^ 1].w);
+        compute_sync();  // phase 2's slots are complete
 
         // phase 3: the cell update
         const int c = c0 + tid;
@@ -210,22 +256,10 @@ __global__ void __launch_bounds__(TILE, 4) k_surface(const __grid_constant__ Sur
                 a.snap_hv[o] = hvn;
             }
         }
-        __syncthreads();  // this stage and the flux slots are free again
+        compute_sync();  // this stage and the flux slots are free again
+        if (tid == 0) mbar_arrive((bar_base + 32u + 8u * st_i));
     }
-    warp_add_ledger<SURF_TERMS>(led, a.ledger);
-    return;
-
-abort:
-    // a tile copy did not land in time: record it, give the copies in flight a
-    // second bounded wait so none lands after the CTA has left, and stop
-    if (tid == 0) {
-        if (atomicCAS(&a.run->error, 0, FL_E_TIMEOUT) == 0) a.run->error_step = s.step;
-        // a pending stage's wait gave up; wpar was already advanced past it
-        if (pending & 1u) (void)mbar_wait_bounded(bar0, (wpar & 1u) ^ 1u, COPY_WAIT_NS);
-        if (pending & 2u) (void)mbar_wait_bounded(bar1, ((wpar >> 1) & 1u) ^ 1u, COPY_WAIT_NS);
-    }
-    cp_async_wait_all();
-    __syncthreads();
+    warp_add_ledger_at<SURF_TERMS>(led, a.ledger, (int)blockIdx.x * (TILE / 32) + (tid >> 5));
 }
 
 template __global__ void k_surface<0>(const __grid_constant__ SurfArgs, int, int);
@@ -387,8 +421,8 @@ namespace fl {
 
 cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, int grid, int smem_bytes,
                            cudaStream_t stream) {
-    if (kind) k_surface<1><<<grid, TILE, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
-    else k_surface<0><<<grid, TILE, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
+    if (kind) k_surface<1><<<grid, SURF_THREADS, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
+    else k_surface<0><<<grid, SURF_THREADS, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
     return cudaGetLastError();
 }
 
@@ -401,7 +435,7 @@ cudaError_t plan_surface_launch(SurfArgs &a, int kind, int device, int *grid, in
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, *smem_bytes);
     if (e != cudaSuccess) return e;
     int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TILE, (size_t)*smem_bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, SURF_THREADS, (size_t)*smem_bytes);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return e;
