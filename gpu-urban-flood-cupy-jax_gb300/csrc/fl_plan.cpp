@@ -439,10 +439,6 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     }
     L.kcell_start.push_back(I);
     L.K = (int32_t)L.kcell_cell.size();
-    for (int32_t k = 0; k < L.K; ++k) {
-        const uint32_t v = (uint32_t)(k + 1);
-        memcpy(&L.cinfo[L.kcell_cell[k]].w, &v, 4);
-    }
     for (int32_t k = 0; k < L.K; ++k)
         L.max_inlets_per_cell = std::max(L.max_inlets_per_cell, L.kcell_start[k + 1] - L.kcell_start[k]);
 

@@ -428,7 +428,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     if (rc) return rc;
     const bool with_drain = drain && drain->node_count > 0;
     if (with_drain) {
-        rc = build_drain_layout(*mesh, *drain, L);  // also sets the inlet-cell words of cinfo
+        rc = build_drain_layout(*mesh, *drain, L);  // also flags the surcharge-table cells in cinfo
         if (rc) return rc;
     }
     s->C = L.C;

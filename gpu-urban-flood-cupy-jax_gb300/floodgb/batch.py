@@ -141,3 +141,75 @@ class BatchSolver:
         d = dict(zip(N.LEDGER_NAMES[:4] + [N.LEDGER_NAMES[10]], [float(out[i]) for i in (0, 1, 2, 3, 10)]))
         d["boundary_net_flux_m3"] = d["boundary_inflow_m3"] - d["boundary_outflow_m3"]
         return d
+
+
+def measure_ensemble(per_size: int = 16, duration_cap_h: float | None = None, sequential_per_size: int = 2,
+                     tune_shape: bool = True, seed: int = 2) -> dict:
+    """The ragged batched ensemble: per_size members at each of the four mesh
+    sizes (10,082 / 49,928 / 100,352 / 250,632 triangles), seeded storms with
+    peak 20-120 mm/h over 1-6 h, each member run for its storm's duration,
+    all in one persistent launch per step (launch shape from the autotuner).
+    The plain single-instance solver is timed on sequential_per_size members
+    of each size, and its scenario-hours/s is extrapolated per size to the
+    whole ensemble."""
+
+    import time
+
+    import torch
+
+    from .autotune import tune
+    from .solver import solver_for_city
+    from .synthetic import ensemble_workload
+
+    members = ensemble_workload(seed=seed, per_size=per_size, duration_cap_h=duration_cap_h)
+    hours = sum(m.duration_s for m in members) / 3600.0
+    shape = tune(members) if tune_shape else {"tile_cells": 256, "ctas_per_sm": 0}
+    with BatchSolver(members, shape=shape) as b:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        b.run()
+        torch.cuda.synchronize()
+        batched_s = time.perf_counter() - t
+        steps = [b.progress(k).step_count for k in range(b.n)]
+        cell_steps = sum(s * c for s, c in zip(steps, b.cell_counts))
+        info = b.info()
+    # plain solver: per mesh size, the mean time per simulated hour of a sample
+    per_hour = {}
+    for k0 in range(0, len(members), per_size):
+        group = members[k0:k0 + per_size]
+        secs = hrs = 0.0
+        for m in group[:sequential_per_size]:
+            s = solver_for_city(m.city, m.rainfall, m.cfg, duration_s=m.duration_s)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            s.run()
+            torch.cuda.synchronize()
+            secs += time.perf_counter() - t
+            hrs += m.duration_s / 3600.0
+            s.close()
+        per_hour[group[0].city.topologies.surface_topology.cell_count] = secs / hrs
+    seq_s = sum(per_hour[m.city.topologies.surface_topology.cell_count] * m.duration_s / 3600.0 for m in members)
+    return {
+        "members": len(members), "scenario_hours": hours, "batched_s": batched_s,
+        "batched_scenario_h_per_s": hours / batched_s, "batched_cell_steps_per_s": cell_steps / batched_s,
+        "single_instance_scenario_h_per_s": hours / seq_s, "single_instance_s_estimated": seq_s,
+        "batched_over_single": seq_s / batched_s, "shape": {k: info[k] for k in ("tile_cells", "ctas_per_sm", "grid", "tiles")},
+        "single_instance_sample": f"{sequential_per_size} members per mesh size, extrapolated per size",
+    }
+
+
+def main():
+    import argparse
+    import json
+
+    p = argparse.ArgumentParser(description="time the ragged batched ensemble against the single-instance solver")
+    p.add_argument("--per-size", type=int, default=16)
+    p.add_argument("--cap-h", type=float, default=None)
+    p.add_argument("--sequential-per-size", type=int, default=2)
+    p.add_argument("--no-tune", action="store_true")
+    a = p.parse_args()
+    print(json.dumps(measure_ensemble(a.per_size, a.cap_h, a.sequential_per_size, not a.no_tune)))
+
+
+if __name__ == "__main__":
+    main()
