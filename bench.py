@@ -54,6 +54,10 @@ def parse_args():
                    help="ncu helper: open a profiler range around 64 solver steps of a wet run (loop) or "
                         "around 2 isolated launches of each step kernel (kernels); prints nothing else")
     p.add_argument("--profile-start-s", type=float, default=900.0)
+    p.add_argument("--long", action="store_true",
+                   help="the 24 h production-shaped run with hourly ledger checks, then 8 concurrent members")
+    p.add_argument("--long-hours", type=float, default=24.0)
+    p.add_argument("--long-members", type=int, default=8)
     return p.parse_args()
 
 
@@ -480,8 +484,97 @@ def profile_arm(args):
     solver.close()
 
 
+def long_arm(args):
+    """The whole 160.09 mm / 24 h front-loaded event on the production-shaped
+    coupled city (one instance, the float64 ledger closed every simulated
+    hour), then `long_members` members with seeded variants of the event
+    (intensity x U(0.7, 1.3), peak shifted by up to +-3 h) run concurrently,
+    one host thread and CUDA stream each (replicas on one GPU)."""
+
+    import threading
+
+    import numpy as np
+    import torch
+
+    from floodgb import native
+    from floodgb.build import build_library
+    from floodgb.config import load_config
+    from floodgb.rainfall import hourly_rainfall
+    from floodgb.solver import solver_for_city
+    from floodgb.synthetic import FRONT_LOADED_24H_MMHR, production_workload
+
+    build_library()
+    native.load()
+    sc = production_workload()
+    dur_s = args.long_hours * 3600.0
+    cfg = load_config(None, dict(sc.overrides, **{"solver.duration_min": args.long_hours * 60.0}))
+    topo = sc.city.topologies
+    area = np.asarray(topo.surface_topology.cell_area_m2, np.float64)
+    C = topo.surface_topology.cell_count
+    v0 = float(np.sum(np.asarray(topo.surface_state.h_m, np.float64) * area)) + float(
+        np.sum(topo.pipe_state.node_volume_m3))
+    s = solver_for_city(sc.city, sc.rainfall, cfg, duration_s=dur_s)
+    worst = 0.0
+    solve_s = 0.0
+    hours = int(np.ceil(args.long_hours))
+    for k in range(1, hours + 1):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.run(min(k * 3600.0, dur_s))
+        torch.cuda.synchronize()
+        solve_s += time.perf_counter() - t
+        led = s.ledger()
+        lhs = v0 + led["rainfall_input_m3"]
+        rhs = (led["surface_volume_m3"] + led["node_volume_m3"] + led["infiltration_loss_m3"]
+               + led["outfall_discharge_m3"] + led["unreturned_overflow_m3"] - led["boundary_net_flux_m3"])
+        worst = max(worst, abs(lhs - rhs) / max(abs(lhs), 1.0))
+    p = s.progress()
+    n_snap = p.snapshot_count
+    s.close()
+    single = {"hours": args.long_hours, "solver_s": solve_s, "steps": p.step_count,
+              "cell_steps_per_s": C * p.step_count / solve_s, "snapshots": n_snap,
+              "worst_hourly_ledger_residual_ratio": worst,
+              "reference_24h_cupy_s": 430.467, "reference_hardware": "RTX PRO 4000 Blackwell, real 981,880-tri city"}
+    # concurrent members with seeded rainfall variants
+    rng = np.random.default_rng(24)
+    solvers, streams = [], []
+    for m in range(args.long_members):
+        hourly = np.roll(FRONT_LOADED_24H_MMHR * rng.uniform(0.7, 1.3), int(rng.integers(-3, 4)))
+        s = solver_for_city(sc.city, hourly_rainfall(hourly), cfg, duration_s=dur_s)
+        solvers.append(s)
+        streams.append(torch.cuda.Stream())
+    errors = []
+
+    def go(k):
+        try:
+            solvers[k].run(stream=streams[k])
+        except Exception as e:  # reported below
+            errors.append(repr(e))
+
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    threads = [threading.Thread(target=go, args=(k,)) for k in range(len(solvers))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    torch.cuda.synchronize()
+    ens_s = time.perf_counter() - t
+    steps = [sv.progress().step_count for sv in solvers]
+    for sv in solvers:
+        sv.close()
+    ensemble = {"members": len(solvers), "wall_s": ens_s, "scenario_hours": len(solvers) * args.long_hours,
+                "scenario_h_per_s": len(solvers) * args.long_hours / ens_s, "steps": steps,
+                "cell_steps_per_s": C * sum(steps) / ens_s, "errors": errors,
+                "single_instance_scenario_h_per_s": args.long_hours / solve_s}
+    print(json.dumps({"long_run": single, "concurrent_members": ensemble}))
+
+
 def main():
     args = parse_args()
+    if args.long:
+        long_arm(args)
+        return
     if args.profile:
         profile_arm(args)
         return
