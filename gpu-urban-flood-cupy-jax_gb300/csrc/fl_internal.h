@@ -100,9 +100,8 @@ constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer
 // ---------------------------------------------------------------------------
 // Drainage layout.  Nodes are renumbered so that the nodes overflowing into
 // one surface cell are consecutive ("groups", in cell order; nodes without a
-// surface cell last).  Inlets are in cell order (q, the order the surface
-// kernel evaluates them in); each node lists its inlets (node order j) as
-// in_qk[j] = {q, inlet cell}.  Each node lists its incident links as slots
+// surface cell last).  Inlets are in cell order (q); each node lists its
+// inlets (node order j) as in_qk[j] = {q, inlet cell index}.  Each node lists its incident links as slots
 // {link, meta}: meta = the other end node | NL_FROM if the node is the link's
 // from-node | NL_TO if it is its to-node (a self-loop has both).
 // ---------------------------------------------------------------------------
@@ -110,7 +109,7 @@ constexpr uint32_t NL_NODE_MASK = 0x3FFFFFFFu;
 constexpr uint32_t NL_FROM = 1u << 30;
 constexpr uint32_t NL_TO = 1u << 31;
 
-// What k_surface needs to evaluate the inlet requests of its cell.
+// What k_nodes needs to evaluate the inlet requests of a node's inlets.
 struct InletReqView {
     const int32_t *kcell_start;   // [K + 1] inlet range (cell order) of each inlet cell
     const int32_t *in_node;       // [I] cell order

@@ -1,11 +1,12 @@
 // Surface kernels for sm_103a.
 //
-// k_surface: a persistent kernel.  Each CTA walks its tiles (256 consecutive
-// Hilbert-ordered cells each) through a two-stage shared-memory pipeline:
-// while it computes tile i, the bulk-copy (TMA) engine brings tile i+1's
-// contiguous blocks -- states, cell info, Horton fields, wet time, the edge
-// entries and the halo cell list -- into the other stage, and cp.async
-// gathers the halo states, so DRAM latency overlaps the arithmetic.  Per tile:
+// k_surface: a persistent, warp-specialised kernel.  Each CTA walks its tiles
+// (256 consecutive Hilbert-ordered cells each) through a two-stage
+// shared-memory pipeline: a producer warp has the bulk-copy (TMA) engine
+// bring a tile's contiguous blocks -- states, cell info, Horton fields, wet
+// time, the edge entries and the halo cell list -- into a stage and then
+// gathers its halo states with cp.async, while eight compute warps work on
+// the other stage, so DRAM latency overlaps the arithmetic.  Per tile:
 //   phase 2  every edge entry of the tile once -- ghost state, hydrostatic
 //            reconstruction, HLL (reference triangular_swe_cuda_kernels.py
 //            :22-203, equations.py:20-152, triangular_backend.py:1067-1178,
@@ -14,8 +15,9 @@
 //   phase 3  each thread sums its cell's slots in the reference's order and
 //            does the cell update with Manning damping (:206-252), rainfall
 //            and infiltration (triangular_backend.py:1330-1379), the velocity
-//            clamp (solver/stabilizers.py:8-27), wet time, snapshot writes,
-//            the inlet requests of its cell and the ledger.
+//            clamp (solver/stabilizers.py:8-27), external inflow, wet time,
+//            snapshot writes and the ledger.  (The inlet requests of inlet
+//            cells are evaluated by k_nodes from this kernel's output.)
 // An edge between two tiles is evaluated in each (same code, same inputs),
 // so its two cells always apply the same mass flux: the scheme is exactly
 // conservative and bitwise reproducible.  The last CTA of the grid only plans
