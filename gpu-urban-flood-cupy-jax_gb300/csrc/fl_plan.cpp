@@ -255,6 +255,35 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
                 else ent_bits[idx] |= EB_LPRESENT | ((uint32_t)lslot[e] << EB_LSLOT_SHIFT);
             }
         }
+        // entries grouped by kind so a warp's entries take the same path:
+        // active interior with both cells in the tile, active interior with
+        // one, then boundary / inactive-neighbour entries (stable; the order
+        // does not change any cell's result: each entry writes its own
+        // (cell, slot) places and a cell sums its slots in slot order)
+        {
+            const size_t n = ent_bits.size();
+            auto kind = [&](size_t j) {
+                const uint32_t b = ent_bits[j];
+                if (!(b & EB_AI)) return 2;
+                return ((b & EB_LPRESENT) && (b & EB_RPRESENT)) ? 0 : 1;
+            };
+            std::vector<size_t> order(n);
+            std::iota(order.begin(), order.end(), (size_t)0);
+            std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return kind(x) < kind(y); });
+            std::vector<int32_t> nl(n), nr(n);
+            std::vector<uint32_t> nb(n);
+            std::vector<float4> ne(n);
+            for (size_t k = 0; k < n; ++k) {
+                nl[k] = ent_left[order[k]];
+                nr[k] = ent_right[order[k]];
+                nb[k] = ent_bits[order[k]];
+                ne[k] = L.ent[first + order[k]];
+            }
+            ent_left.swap(nl);
+            ent_right.swap(nr);
+            ent_bits.swap(nb);
+            std::copy(ne.begin(), ne.end(), L.ent.begin() + (std::ptrdiff_t)first);
+        }
         // halo: cells outside the tile that an entry reads, ascending
         halo.clear();
         for (size_t j = 0; j < ent_bits.size(); ++j) {
