@@ -54,6 +54,8 @@ def parse_args():
                    help="ncu helper: open a profiler range around 64 solver steps of a wet run (loop) or "
                         "around 2 isolated launches of each step kernel (kernels); prints nothing else")
     p.add_argument("--profile-start-s", type=float, default=900.0)
+    p.add_argument("--surface-mode", choices=["full_swe", "local_inertial"], default="full_swe",
+                   help="solver.surface_step_mode of the measured run (the headline is full_swe)")
     p.add_argument("--long", action="store_true",
                    help="the 24 h production-shaped run with hourly ledger checks, then 8 concurrent members")
     p.add_argument("--long-hours", type=float, default=24.0)
@@ -270,7 +272,7 @@ def our_arm(args):
     build_library()
     native.load()
     sc = production_workload()
-    cfg = load_config(None, sc.overrides)
+    cfg = load_config(None, dict(sc.overrides, **{"solver.surface_step_mode": args.surface_mode}))
     topo = sc.city.topologies
     st = topo.surface_topology
     C, E = st.cell_count, st.edge_count
@@ -388,6 +390,7 @@ def our_arm(args):
         "config": {
             "workload": WORKLOAD, "cells": C, "edges": E, "solver_steps_per_run": steps[-1],
             "step": "one 60-min simulated run (adaptive dt, CFL every 32 steps)",
+            "surface_step_mode": args.surface_mode,
             "l2": "flushed before every run (512 MB write); state reset outside the events",
             "parallelism": f"replicas x{world}",
             "vs_baseline_ref": "7.447e8 cell-steps/s: reference CuPy on RTX PRO 4000, real 981,880-tri city",
