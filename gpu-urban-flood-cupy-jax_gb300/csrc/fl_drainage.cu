@@ -86,12 +86,20 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
 // runs one pass with one thread per item.  Values one pass writes and a
 // later one reads (Vb, capsur, T, fac) are read through L2 (ld.cg).
 
-// Capture limit factor of inlet cell k at depth h: its volume over the summed
-// capture requests of its inlets, in their order (reference :133-177).
-__device__ __forceinline__ float cell_capture_factor(const InletReqView &v, int k, float h, float area, float dt) {
+// Capture limit factor of an inlet cell at depth h: its volume over the
+// summed capture requests of its inlets [q0, q1), in their order (reference
+// :133-177).  `own` is the capture request of the calling inlet: a cell whose
+// only inlet it is needs no other node's volume (the sum is 0 + own, as the
+// loop would form it; this file is compiled without contraction, so the
+// request is rounded identically either way).
+__device__ __forceinline__ float cell_capture_factor(const InletReqView &v, int q0, int q1, float own, float h,
+                                                     float area, float dt) {
     float sum = 0.0f;
-    for (int q = v.kcell_start[k]; q < v.kcell_start[k + 1]; ++q)
-        sum += inlet_request(v, q, h, ff_clamp0(v.Va[v.in_node[q]]), dt).x;
+    if (q1 - q0 == 1) {
+        sum = sum + own;
+    } else {
+        for (int q = q0; q < q1; ++q) sum += inlet_request(v, q, h, ff_clamp0(v.Va[v.in_node[q]]), dt).x;
+    }
     return fmin32(1.0f, (fmax32(h, 0.0f) * area) / fmax32(sum, 1.0e-12f));
 }
 
@@ -110,17 +118,17 @@ __device__ __forceinline__ void node_item(const NodeArgs &a, const StepCtrl &s, 
     const float dt = s.dt_f;
     float sum = 0.0f;
     for (int j = j0; j < j1; ++j) {
-        const int2 qk = a.in_qk[j];
-        sum += inlet_request(a.inl, qk.x, hs[a.kcell_cell[qk.y]].x, V, dt).y;
+        const int4 qk = a.in_qk[j];
+        sum += inlet_request(a.inl, qk.x, hs[qk.y].x, V, dt).y;
     }
     const float sf = fmin32(1.0f, fmax32(ff_val(V), 0.0f) / fmax32(sum, 1.0e-12f));
     float dv = 0.0f;
     for (int j = j0; j < j1; ++j) {
-        const int2 qk = a.in_qk[j];
-        const int c = a.kcell_cell[qk.y];
+        const int4 qk = a.in_qk[j];
+        const int c = qk.y;
         const float h = hs[c].x;
         const float2 r = inlet_request(a.inl, qk.x, h, V, dt);
-        const float cap = r.x * cell_capture_factor(a.inl, qk.y, h, a.cinfo[c].x, dt);
+        const float cap = r.x * cell_capture_factor(a.inl, qk.z, qk.w, r.x, h, a.cinfo[c].x, dt);
         const float sur = r.y * sf;
         a.capsur[qk.x] = make_float2(cap, sur);
         dv += cap - sur;

@@ -101,7 +101,8 @@ constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer
 // Drainage layout.  Nodes are renumbered so that the nodes overflowing into
 // one surface cell are consecutive ("groups", in cell order; nodes without a
 // surface cell last).  Inlets are in cell order (q); each node lists its
-// inlets (node order j) as in_qk[j] = {q, inlet cell index}.  Each node lists its incident links as slots
+// inlets (node order j) as in_qk[j] = {q, its cell, the cell's inlet range
+// [q0, q1) in cell order}.  Each node lists its incident links as slots
 // {link, meta}: meta = the other end node | NL_FROM if the node is the link's
 // from-node | NL_TO if it is its to-node (a self-loop has both).
 // ---------------------------------------------------------------------------
@@ -111,7 +112,6 @@ constexpr uint32_t NL_TO = 1u << 31;
 
 // What k_nodes needs to evaluate the inlet requests of a node's inlets.
 struct InletReqView {
-    const int32_t *kcell_start;   // [K + 1] inlet range (cell order) of each inlet cell
     const int32_t *in_node;       // [I] cell order
     const float4 *in_par;         // [I] {bed - invert, capture capacity, surcharge capacity, node storage area}
     const float2 *Va;             // node volume (float-float) at the start of the drainage step
@@ -213,9 +213,8 @@ struct DtArgs {
 // k_nodes: one thread per node, the inlet exchange of its volume.
 struct NodeArgs {
     const int32_t *node_in_start; // [N + 1] inlet range (node order)
-    const int2 *in_qk;            // [I] node order: {inlet in cell order, its inlet cell}
-    InletReqView inl;             // inlet parameters and the per-cell inlet ranges
-    const int32_t *kcell_cell;    // [K] the cell of each inlet cell index
+    const int4 *in_qk;            // [I] node order: {inlet in cell order, its cell, the cell's inlets [q0, q1)}
+    InletReqView inl;             // inlet parameters
     const float4 *cinfo;
     const float4 *state0, *state1;  // the surface step's output holds the inlet cells' depth
     float2 *capsur;               // [I] cell order: granted {capture, surcharge}
@@ -345,7 +344,7 @@ struct HostLayout {
     int64_t slots_used = 0;
     // drainage
     std::vector<int32_t> in_cell, in_node, in_kcell, in_order; // cell order; in_order[q] = reference inlet
-    std::vector<int2> in_qk;          // node order: {inlet in cell order, inlet cell}
+    std::vector<int4> in_qk;          // node order: {inlet in cell order, its cell, the cell's inlets [q0, q1)}
     std::vector<float4> in_par;
     std::vector<int32_t> kcell_cell, kcell_start;
     std::vector<int32_t> node_in_start;

@@ -358,7 +358,9 @@ static int validate_drain(const HostLayout &L) {
             return set_error(FL_E_INVALID, "internal: inlet %d tables", q);
     for (int32_t n = 0; n < N; ++n)
         for (int32_t j = L.node_in_start[n]; j < L.node_in_start[n + 1]; ++j)
-            if (L.in_qk[j].x < 0 || L.in_qk[j].x >= I || L.in_node[L.in_qk[j].x] != n || L.in_qk[j].y != L.in_kcell[L.in_qk[j].x])
+            if (L.in_qk[j].x < 0 || L.in_qk[j].x >= I || L.in_node[L.in_qk[j].x] != n ||
+                L.in_qk[j].y != L.kcell_cell[L.in_kcell[L.in_qk[j].x]] || L.in_qk[j].z != L.kcell_start[L.in_kcell[L.in_qk[j].x]] ||
+                L.in_qk[j].w != L.kcell_start[L.in_kcell[L.in_qk[j].x] + 1])
                 return set_error(FL_E_INVALID, "internal: node %d inlet list", n);
     for (const int2 &e : L.nl)
         if (e.x < 0 || e.x >= NL || (int32_t)((uint32_t)e.y & NL_NODE_MASK) >= N || !((uint32_t)e.y & (NL_FROM | NL_TO)))
@@ -475,10 +477,13 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     L.node_in_start.assign(N + 1, 0);
     for (int32_t q = 0; q < I; ++q) L.node_in_start[L.in_node[q] + 1]++;
     for (int32_t n = 0; n < N; ++n) L.node_in_start[n + 1] += L.node_in_start[n];
-    L.in_qk.assign(I, make_int2(0, 0));
+    L.in_qk.assign(I, make_int4(0, 0, 0, 0));
     {
         std::vector<int32_t> fill(L.node_in_start.begin(), L.node_in_start.end() - 1);
-        for (int32_t q = 0; q < I; ++q) L.in_qk[fill[L.in_node[q]]++] = make_int2(q, L.in_kcell[q]);
+        for (int32_t q = 0; q < I; ++q) {
+            const int32_t k = L.in_kcell[q];
+            L.in_qk[fill[L.in_node[q]]++] = make_int4(q, L.in_cell[q], L.kcell_start[k], L.kcell_start[k + 1]);
+        }
     }
 
     // node parameters (renumbered)

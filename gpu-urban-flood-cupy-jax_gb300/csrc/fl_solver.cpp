@@ -540,8 +540,8 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         int32_t *in_node, *kcell_start, *node_in_start, *nls, *lf, *lt;
         float4 *in_par, *nd0, *lk0, *lk1, *lk2;
         float *node_area, *nd_capv;
-        int4 *grp;
-        int2 *nl, *in_qk;
+        int4 *grp, *in_qk;
+        int2 *nl;
         if ((rc = s->upload(&in_node, L.in_node)) || (rc = s->upload(&in_qk, L.in_qk)) ||
             (rc = s->upload(&lf, L.link_from)) || (rc = s->upload(&lt, L.link_to)) ||
             (rc = s->upload(&in_par, L.in_par)) || (rc = s->upload(&kcell_start, L.kcell_start)) ||
@@ -564,14 +564,11 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         s->n_led_2 = (size_t)s->d2_blocks * 4 * D2_TERMS;
         float *T, *fac;
         float2 *capsur;
-        int32_t *kcell_cell;
         if ((rc = s->alloc(&s->led_1, s->n_led_1)) || (rc = s->alloc(&s->led_2, s->n_led_2)) ||
-            (rc = s->alloc(&T, s->NL)) || (rc = s->alloc(&fac, s->N)) || (rc = s->alloc(&capsur, s->I)) ||
-            (rc = s->upload(&kcell_cell, L.kcell_cell)))
+            (rc = s->alloc(&T, s->NL)) || (rc = s->alloc(&fac, s->N)) || (rc = s->alloc(&capsur, s->I)))
             return rc;
         FL_CUDA(cudaMemset(capsur, 0, sizeof(float2) * std::max(s->I, 1)));
         InletReqView &v = s->nd.inl;
-        v.kcell_start = kcell_start;
         v.in_node = in_node;
         v.in_par = in_par;
         v.Va = s->Va;
@@ -584,7 +581,6 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         NodeArgs &a = s->nd;
         a.node_in_start = node_in_start;
         a.in_qk = in_qk;
-        a.kcell_cell = kcell_cell;
         a.cinfo = cinfo;
         a.state0 = s->state[0];
         a.state1 = s->state[1];
