@@ -467,7 +467,7 @@ def profile_arm(args):
     build_library()
     native.load()
     sc = production_workload()
-    cfg = load_config(None, sc.overrides)
+    cfg = load_config(None, dict(sc.overrides, **{"solver.surface_step_mode": args.surface_mode}))
     solver = solver_for_city(sc.city, sc.rainfall, cfg)
     solver.run(args.profile_start_s)
     torch.cuda.synchronize()

@@ -1,16 +1,22 @@
 // Local-inertial surface step for sm_103a (solver.surface_step_mode =
 // "local_inertial"): the reference's fast routing mode
 // (gurugram_flood/kernels/triangular_local_inertial_cuda_kernels.py:59-262,
-// triangular_backend.py:531-590, local_inertial.py:20-49) as three launches:
+// triangular_backend.py:531-590, local_inertial.py:20-49) as two launches:
 //   k_li_edges  one thread per edge: the LISFLOOD-style discharge update from
-//               the water-surface slope, stored once per edge     [:59-167]
-//   k_li_scale  one thread per cell: the donor limit factor, its volume over
-//               the summed outgoing requests of its edges, in slot order
-//               (the reference adds them with atomicAdd)           [:172-189]
-//   k_li_cells  one thread per cell: the gathered volume change, momentum
-//               from the face discharges, then the same sources, clamp,
-//               external inflow, wet time and snapshots as the full-SWE
-//               surface kernel; its last block plans the next step [:194-262]
+//               the water-surface slope (face distance and Manning n are
+//               static per edge), written into the (cell, slot) place of
+//               each of its cells                                   [:59-167]
+//   k_li_cells  one thread per cell: the donor limit factors (a cell's volume
+//               over the summed outgoing requests of its edges, in slot
+//               order; the reference adds them with atomicAdd) of the cell
+//               and of each neighbour that donates to it [:172-189], the
+//               volume change, momentum from the face discharges, then the
+//               same sources, clamp, external inflow, wet time and snapshots
+//               as the full-SWE surface kernel; its last block plans the next
+//               step                                                [:194-262]
+// The cell kernel reads its cell's discharges and slot tables (flags, the
+// other cell, the face normals) contiguously and gathers a donating
+// neighbour's slots, depth and area.
 // Compiled with -fmad=false: the discharge arithmetic is rounded as written.
 #include <cuda_runtime.h>
 
@@ -38,12 +44,12 @@ __global__ void __launch_bounds__(256) k_li_edges(const __grid_constant__ LiArgs
         const float etar = ai ? br + hr : bl;
         const float bstar = ai ? fmax32(bl, br) : bl;
         const float hflow = fmax32(fmax32(etal, etar) - bstar, 0.0f);
-        const float dist = fmax32(0.5f * (a.char_len[L] + a.char_len[R]), 1.0e-6f);
-        const float slope = (etar - etal) / dist;
+        const float2 dm = a.e_dm[e];  // {max(0.5 (l_L + l_R), 1e-6), face n}, formed on the host in float32
+        const float slope = (etar - etal) / dm.x;
         const float nx = geo.x, ny = geo.y, len = geo.z;
         const float nl = hul * nx + hvl * ny, nr = hur * nx + hvr * ny;
         const float qold = (ai ? 0.5f * (nl + nr) : nl) * len;
-        const float mn = ai ? 0.5f * (a.cinfo[L].y + a.cinfo[R].y) : a.cinfo[L].y;
+        const float mn = dm.y;
         const float area = fmax32(hflow * len, 1.0e-8f);
         const float radius = fmax32(hflow, 1.0e-6f);
         const float r43 = radius * cbrtf(radius);
@@ -52,32 +58,33 @@ __global__ void __launch_bounds__(256) k_li_edges(const __grid_constant__ LiArgs
         float q = numer / fric;
         if (!(ai || bedge)) q = 0.0f;
         if (bedge) q = fmax32(q, 0.0f);
-        a.Q[e] = q;
+        float *qs = reinterpret_cast<float *>(a.Qs);
+        qs[(size_t)L * 4 + ((f >> LI_SLOTL_SHIFT) & 3u)] = q;
+        if (f & LI_INTERIOR) qs[(size_t)lr.y * 4 + ((f >> LI_SLOTR_SHIFT) & 3u)] = q;
     }
 }
 
-__global__ void __launch_bounds__(256) k_li_scale(const __grid_constant__ LiArgs a, int slot) {
-    const StepCtrl s = a.ctrl[slot];
-    if (!s.active || !(s.phases & FL_PHASE_SURFACE)) return;
-    const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
-    const float dt = s.dt_f;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.C; c += gridDim.x * blockDim.x) {
-        const int4 ce = a.c_edges[c];
-        const int es[3] = {ce.x, ce.y, ce.z};
-        float req = 0.0f;
+// Donor limit factor of a cell (reference :172-189): its volume over the
+// summed outgoing requests of its active interior edges, in slot order (the
+// reference adds them with atomicAdd).  sb, q4: the cell's slot bits and
+// discharges; h, area: its depth at the step start and its area.  The cell
+// kernel evaluates it for a cell and for each neighbour that donates to it;
+// every evaluation of one cell reads the same values, so all agree
+// bit-for-bit (this file is compiled without contraction).
+__device__ __forceinline__ float li_donor_scale(uint32_t sb, float4 q4, float h, float area, float dt) {
+    const float qk[3] = {q4.x, q4.y, q4.z};
+    float req = 0.0f;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int e = es[k];
-            if (e < 0) continue;
-            if (!(__float_as_uint(a.e_geo[e].w) & LI_AI)) continue;
-            const float q = a.Q[e];
-            if (q == 0.0f) continue;
-            const int2 lr = a.e_lr[e];
-            if ((q >= 0.0f ? lr.x : lr.y) == c) req += fabsf(q) * dt;
-        }
-        const float vol = fmax32(in[c].x, 0.0f) * a.cinfo[c].x;
-        a.scale[c] = req > 1.0e-12f ? fmin32(1.0f, vol / req) : 1.0f;
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t b = sb >> (4 * k);
+        if (!(b & LIS_PRESENT) || !(b & LIS_AI)) continue;
+        const float q = qk[k];
+        if (q == 0.0f) continue;
+        // the donor is the left cell for q >= 0, else the right one
+        if ((q >= 0.0f) == ((b & LIS_LEFT) != 0)) req += fabsf(q) * dt;
     }
+    const float vol = fmax32(h, 0.0f) * area;
+    return req > 1.0e-12f ? fmin32(1.0f, vol / req) : 1.0f;
 }
 
 template <int KIND>
@@ -113,28 +120,37 @@ __global__ void __launch_bounds__(256) k_li_cells(const __grid_constant__ LiArgs
         if (!do_surface) {
             hn = st.x; hun = st.y; hvn = st.z;
         } else if (info & CELL_ACTIVE) {
-            // gather the stored face discharges in slot order
-            const int4 ce = a.c_edges[c];
-            const int es[3] = {ce.x, ce.y, ce.z};
+            // the cell's face discharges in slot order
+            const uint32_t sb = a.c_bits[c];
+            const float4 q4 = a.Qs[c];
+            const int4 oc = a.c_other[c];
+            const float qk[3] = {q4.x, q4.y, q4.z};
+            const int ok[3] = {oc.x, oc.y, oc.z};
+            const float own_scale = li_donor_scale(sb, q4, st.x, ci.x, dt);
             float hd = 0.0f, qx = 0.0f, qy = 0.0f, bf = 0.0f;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const int e = es[k];
-                if (e < 0) continue;
-                const float q = a.Q[e];
+                const uint32_t b = sb >> (4 * k);
+                if (!(b & LIS_PRESENT)) continue;
+                const float q = qk[k];
                 if (q == 0.0f) continue;
-                const float4 geo = a.e_geo[e];
-                if (__float_as_uint(geo.w) & LI_INTERIOR) {
-                    const int2 lr = a.e_lr[e];
-                    const float lim = q * a.scale[q >= 0.0f ? lr.x : lr.y] * dt;
-                    hd += (c == lr.x) ? -lim : lim;
+                const float2 nrm = a.c_nrm[(size_t)k * (size_t)a.C + (size_t)c];
+                if (b & LIS_INTERIOR) {
+                    const bool left = (b & LIS_LEFT) != 0;
+                    float sd = own_scale;
+                    if ((q >= 0.0f) != left) {  // the neighbour donates: its factor from its own slots
+                        const int m = ok[k];
+                        sd = li_donor_scale(a.c_bits[m], a.Qs[m], in[m].x, a.cinfo[m].x, dt);
+                    }
+                    const float lim = q * sd * dt;
+                    hd += left ? -lim : lim;
                 } else {
-                    const float b = q * dt;
-                    hd -= b;
-                    bf += b;
+                    const float bq = q * dt;
+                    hd -= bq;
+                    bf += bq;
                 }
-                qx += q * geo.x;
-                qy += q * geo.y;
+                qx += q * nrm.x;
+                qy += q * nrm.y;
             }
             const float area = ci.x;
             const float h0 = fmax32(st.x + hd / area, 0.0f);
@@ -179,7 +195,6 @@ int li_cell_blocks(int32_t C) { return (C + 255) / 256 + 1; }  // + the planner 
 
 cudaError_t launch_li(const LiArgs &a, int kind, int slot, int plan_next, int sms, cudaStream_t stream) {
     k_li_edges<<<li_edge_blocks(a.E, sms), 256, 0, stream>>>(a, slot);
-    k_li_scale<<<std::max(1, std::min(sms * 8, (a.C + 255) / 256)), 256, 0, stream>>>(a, slot);
     if (kind == 1)
         k_li_cells<1><<<li_cell_blocks(a.C), 256, 0, stream>>>(a, slot, plan_next);
     else

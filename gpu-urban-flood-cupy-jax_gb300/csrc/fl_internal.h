@@ -164,25 +164,37 @@ struct SurfArgs {
     const float *ext_add;         // [Cp] external inflow depth of receiver cells this step
 };
 
-// Local-inertial surface step (three launches: edge discharge, donor scale,
-// cell update).  Edges are renumbered by their first cell (new order).
+// Local-inertial surface step (two launches: edge discharge, cell update with
+// the donor limit factors).  Edges are renumbered by their first cell (new
+// order).  The edge kernel writes each discharge into its cells' (cell, slot)
+// places, so the cell kernel reads a cell's three discharges and static slot
+// tables contiguously.
 constexpr uint32_t LI_INTERIOR = 1u;  // the edge has a right cell
 constexpr uint32_t LI_AI = 2u;        // active interior (both cells active)
 constexpr uint32_t LI_BEDGE = 4u;     // routable boundary edge (left active, outflow / transmissive)
 constexpr uint32_t LI_LACTIVE = 8u;
 constexpr uint32_t LI_RACTIVE = 16u;
+constexpr int LI_SLOTL_SHIFT = 8;     // bits 8-9: the edge's slot in its left cell
+constexpr int LI_SLOTR_SHIFT = 10;    // bits 10-11: its slot in its right cell
+// per-cell slot bits, 4 per slot k at bit 4k
+constexpr uint32_t LIS_PRESENT = 1u;  // the slot has an edge
+constexpr uint32_t LIS_LEFT = 2u;     // the cell is the edge's left cell
+constexpr uint32_t LIS_AI = 4u;       // active interior edge
+constexpr uint32_t LIS_INTERIOR = 8u; // the edge has a right cell
 
 struct LiArgs {
     const int2 *e_lr;             // [E] {left, right or -1}
-    const float4 *e_geo;          // [E] {nx, ny, length, flags (bits)}
-    const int4 *c_edges;          // [Cp] the cell's edges in slot order, -1 = none
+    const float4 *e_geo;          // [E] {nx, ny, length, flags | slots (bits)}
+    const float2 *e_dm;           // [E] {face distance, face Manning n}
+    const uint32_t *c_bits;       // [Cp] LIS_* of slot k at bit 4k
+    const int4 *c_other;          // [Cp] the other cell of each slot's interior edge, -1 = none
+    const float2 *c_nrm;          // [3 * Cp] slot-major: the normal of slot k's edge
     const float4 *cinfo;
     const float *char_len;
     const float4 *horton;         // kind 1
     float *wet;
     float4 *state0, *state1;
-    float *Q;                     // [E] discharge of the step
-    float *scale;                 // [Cp] donor limit factor
+    float4 *Qs;                   // [Cp] the discharges of the cell's slot edges this step (w unused)
     StepCtrl *ctrl;
     RunCtrl *run;
     HyetoView hy;

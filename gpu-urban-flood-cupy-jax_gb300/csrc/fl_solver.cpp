@@ -145,7 +145,7 @@ struct FlSolver {
     bool has_table() const { return sur.U > 0; }
     bool has_recharge() const { return rch.U > 0; }
     int launches_per_step() const {
-        return (li_mode ? 3 : 1) + (has_drain() ? 4 : 0) + (has_table() ? 1 : 0) + (has_inflow() ? 1 : 0) +
+        return (li_mode ? 2 : 1) + (has_drain() ? 4 : 0) + (has_table() ? 1 : 0) + (has_inflow() ? 1 : 0) +
                (has_recharge() ? 1 : 0);
     }
 
@@ -205,7 +205,7 @@ static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStr
     }
     if (s->li_mode) {
         FL_CUDA(launch_li(s->li, s->kind, slot, plan_next ? 1 : 0, s->sms, st));
-        g_launches += 3;
+        g_launches += 2;
     } else {
         FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, s->surf_grid, s->surf_smem, st));
         g_launches++;
@@ -758,32 +758,73 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
             lr[k] = make_int2(L.inv[l], interior ? L.inv[r] : -1);
             geo[k] = make_float4(mesh->edge_normal_x[e], mesh->edge_normal_y[e], mesh->edge_length_m[e], fb);
         }
-        std::vector<int4> ce(Cp, make_int4(-1, -1, -1, -1));
+        // per cell: the slot bits, the other cell and the normal of each slot's
+        // edge; per edge: its slot in each of its cells, the face distance
+        // max(0.5 (l_L + l_R), 1e-6) and the face Manning n (the mean over
+        // the two cells of an active interior edge), in float32 as the
+        // reference forms them
+        std::vector<uint32_t> cbits(Cp, 0u);
+        std::vector<int4> coth(Cp, make_int4(-1, -1, -1, -1));
+        std::vector<float2> cnrm((size_t)3 * C, make_float2(0.0f, 0.0f));
+        std::vector<uint32_t> eslot(E, 0u);
         for (int32_t i = 0; i < C; ++i) {
             const int32_t c = L.perm[i];
-            int32_t v[3];
-            for (int j = 0; j < 3; ++j) v[j] = L.inc[(size_t)c * 3 + j] >= 0 ? enew[L.inc[(size_t)c * 3 + j]] : -1;
-            ce[i] = make_int4(v[0], v[1], v[2], -1);
+            int32_t ov[3] = {-1, -1, -1};
+            for (int j = 0; j < 3; ++j) {
+                const int32_t eo = L.inc[(size_t)c * 3 + j];
+                if (eo < 0) continue;
+                const int32_t k = enew[eo];
+                uint32_t f;
+                memcpy(&f, &geo[k].w, 4);
+                const bool left = lr[k].x == i;
+                uint32_t b = LIS_PRESENT;
+                if (left) b |= LIS_LEFT;
+                if (f & LI_AI) b |= LIS_AI;
+                if (f & LI_INTERIOR) {
+                    b |= LIS_INTERIOR;
+                    ov[j] = left ? lr[k].y : lr[k].x;
+                }
+                cbits[i] |= b << (4 * j);
+                eslot[k] |= (uint32_t)j << (left ? LI_SLOTL_SHIFT : LI_SLOTR_SHIFT);
+                cnrm[(size_t)j * C + i] = make_float2(geo[k].x, geo[k].y);
+            }
+            coth[i] = make_int4(ov[0], ov[1], ov[2], -1);
+        }
+        std::vector<float2> edm(E);
+        for (int32_t k = 0; k < E; ++k) {
+            uint32_t f;
+            memcpy(&f, &geo[k].w, 4);
+            f |= eslot[k];
+            memcpy(&geo[k].w, &f, 4);
+            const int32_t l = lr[k].x, r = (f & LI_INTERIOR) ? lr[k].y : lr[k].x;
+            const float hl = 0.5f * (L.char_len[l] + L.char_len[r]);
+            const float dist = hl >= 1.0e-6f ? hl : 1.0e-6f;
+            const float mn = (f & LI_AI) ? 0.5f * (L.cinfo[l].y + L.cinfo[r].y) : L.cinfo[l].y;
+            edm[k] = make_float2(dist, mn);
         }
         int2 *d_lr;
-        float4 *d_geo;
-        int4 *d_ce;
-        float *d_q, *d_scale;
-        if ((rc = s->upload(&d_lr, lr)) || (rc = s->upload(&d_geo, geo)) || (rc = s->upload(&d_ce, ce)) ||
-            (rc = s->alloc(&d_q, (size_t)E)) || (rc = s->alloc(&d_scale, (size_t)Cp)))
+        float4 *d_geo, *d_qs;
+        float2 *d_dm, *d_nrm;
+        uint32_t *d_bits;
+        int4 *d_oth;
+        if ((rc = s->upload(&d_lr, lr)) || (rc = s->upload(&d_geo, geo)) || (rc = s->upload(&d_dm, edm)) ||
+            (rc = s->upload(&d_bits, cbits)) || (rc = s->upload(&d_oth, coth)) || (rc = s->upload(&d_nrm, cnrm)) ||
+            (rc = s->alloc(&d_qs, (size_t)Cp)))
             return rc;
         LiArgs &q = s->li;
         q.e_lr = d_lr;
         q.e_geo = d_geo;
-        q.c_edges = d_ce;
+        q.e_dm = d_dm;
+        q.c_bits = d_bits;
+        q.c_other = d_oth;
+        q.c_nrm = d_nrm;
         q.cinfo = cinfo;
         q.char_len = char_len;
         q.horton = horton;
         q.wet = s->wet;
         q.state0 = s->state[0];
         q.state1 = s->state[1];
-        q.Q = d_q;
-        q.scale = d_scale;
+        q.Qs = d_qs;
         q.ctrl = s->ctrl;
         q.run = s->run;
         q.hy = s->hy;
@@ -1051,7 +1092,7 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
     }
     if (s->li_mode) {
         FL_CUDA(launch_li(s->li, s->kind, s->slot, 0, s->sms, st));
-        g_launches += 3;
+        g_launches += 2;
     } else {
         FL_CUDA(launch_surface(s->sa, s->kind, s->slot, 0, s->surf_grid, s->surf_smem, st));
         g_launches++;
@@ -1104,40 +1145,48 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
     c.phases = FL_PHASE_ALL;
     c.step = r.step;
     FL_CUDA(cudaMemcpyAsync(&s->ctrl[0], &c, sizeof(StepCtrl), cudaMemcpyHostToDevice, st));
-    auto launch = [&]() -> int {
+    auto launch = [&](cudaStream_t ls) -> cudaError_t {
         switch (kernel) {
             case 0:
-                if (s->li_mode)
-                    FL_CUDA(launch_li(s->li, s->kind, 0, 0, s->sms, st));
-                else
-                    FL_CUDA(launch_surface(s->sa, s->kind, 0, 0, s->surf_grid, s->surf_smem, st));
-                break;
-            case 1: FL_CUDA(launch_nodes(s->nd, 0, st)); break;
-            case 2: FL_CUDA(launch_network(s->nw, 0, st)); break;
-            case 4: FL_CUDA(launch_links(s->lk, 0, st)); break;
-            case 5: FL_CUDA(launch_donor(s->dn, 0, st)); break;
+                return s->li_mode ? launch_li(s->li, s->kind, 0, 0, s->sms, ls)
+                                  : launch_surface(s->sa, s->kind, 0, 0, s->surf_grid, s->surf_smem, ls);
+            case 1: return launch_nodes(s->nd, 0, ls);
+            case 2: return launch_network(s->nw, 0, ls);
+            case 4: return launch_links(s->lk, 0, ls);
+            case 5: return launch_donor(s->dn, 0, ls);
             default: {
                 DtArgs a = s->da;
                 a.dt_out = s->dt_out;
-                FL_CUDA(launch_dt(a, s->dt_blocks, 0, 0, st));
+                return launch_dt(a, s->dt_blocks, 0, 0, ls);
             }
         }
-        g_launches++;
-        return FL_OK;
     };
-    if ((rc = launch())) return rc;  // warm-up
-    cudaEvent_t e0, e1;
-    FL_CUDA(cudaEventCreate(&e0));
-    FL_CUDA(cudaEventCreate(&e1));
-    FL_CUDA(cudaEventRecord(e0, st));
-    for (int i = 0; i < reps && rc == FL_OK; ++i) rc = launch();
-    FL_CUDA(cudaEventRecord(e1, st));
-    FL_CUDA(cudaEventSynchronize(e1));
+    const int per = (kernel == 0 && s->li_mode) ? 2 : 1;  // kernels per launch
+    // One launch captured as a graph and replayed, as in the step loop: the
+    // time is the kernels' own, not the host's launch rate.
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    FL_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t le = launch(s->cap_stream);
+    const cudaError_t ce = cudaStreamEndCapture(s->cap_stream, &g);
+    cudaError_t err = le != cudaSuccess ? le : ce;
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&ge, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
     float ms = 0.0f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (rc) return rc;
+    if (err == cudaSuccess) err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err == cudaSuccess) err = cudaGraphLaunch(ge, st);  // warm-up
+    if (err == cudaSuccess) err = cudaEventRecord(e0, st);
+    for (int i = 0; i < reps && err == cudaSuccess; ++i) err = cudaGraphLaunch(ge, st);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (ge) cudaGraphExecDestroy(ge);
+    if (err != cudaSuccess) return set_error(FL_E_CUDA, "fl_time_kernel: %s", cudaGetErrorString(err));
+    g_launches += (int64_t)per * (reps + 1);
     *ms_per_launch = (double)ms / reps;
     return FL_OK;
 }

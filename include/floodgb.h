@@ -266,7 +266,7 @@ FL_API int fl_plan_check(const FlMeshDesc *mesh, const FlDrainDesc *drain, int64
 FL_API int fl_plan_tiles(const FlMeshDesc *mesh, int64_t *tiles);
 
 /* Time `reps` back-to-back launches of one kernel of a step (0 surface (the
- * three local-inertial launches in that mode), 1 node inlet exchange, 2 pipe
+ * two local-inertial launches in that mode), 1 node inlet exchange, 2 pipe
  * network, 3 CFL reduction, 4 link update, 5 donor factors) between CUDA events on
  * `stream`, at the solver's current state and last dt; the clock is not
  * advanced but the state buffers are overwritten (reset before the next run).
