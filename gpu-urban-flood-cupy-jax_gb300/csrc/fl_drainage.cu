@@ -84,7 +84,11 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
 
 // The drainage step's four passes as per-item functions; each kernel below
 // runs one pass with one thread per item.  Values one pass writes and a
-// later one reads (Vb, capsur, T, fac) are read through L2 (ld.cg).
+// later one reads (Vb, capsur, T, fac) are read through L2 (ld.cg).  Each
+// kernel issues the loads that do not depend on the step record (the
+// item's static indices, the values earlier kernels wrote) before that
+// record arrives, so its latency overlaps theirs instead of adding to the
+// dependent-load chain.
 
 // Capture limit factor of an inlet cell at depth h: its volume over the
 // summed capture requests of its inlets [q0, q1), in their order (reference
@@ -107,9 +111,9 @@ __device__ __forceinline__ float cell_capture_factor(const InletReqView &v, int 
 // their cells (reference inlet_exchange_request_kernel :52-131), captures
 // limited by each cell's volume, surcharges by the node's, and the node
 // volume after the exchange.
-__device__ __forceinline__ void node_item(const NodeArgs &a, const StepCtrl &s, int n, float (&led)[D1_TERMS]) {
-    const float2 V = ff_clamp0(a.Va[n]);
-    const int j0 = a.node_in_start[n], j1 = a.node_in_start[n + 1];
+// V = the clamped start volume Va[n]; [j0, j1) = the node's inlets.
+__device__ __forceinline__ void node_item(const NodeArgs &a, const StepCtrl &s, int n, float2 V, int j0, int j1,
+                                          float (&led)[D1_TERMS]) {
     if (j0 == j1) {
         a.Vb[n] = V;
         return;
@@ -138,18 +142,9 @@ __device__ __forceinline__ void node_item(const NodeArgs &a, const StepCtrl &s, 
     a.Vb[n] = ff_add(V, dv);
 }
 
-// Link l: the transfer volume from the end volumes after the inlet exchange.
-__device__ __forceinline__ void link_item(const LinkArgs &a, const StepCtrl &s, int l) {
-    const int f = a.link_from[l], to = a.link_to[l];
-    const float df = node_depth(__ldcg(&a.Vb[f]), a.node_area[f]);
-    const float dtn = node_depth(__ldcg(&a.Vb[to]), a.node_area[to]);
-    const float *Qin = s.parity ? a.Q1 : a.Q0;
-    a.T[l] = link_transfer(a.lk0[l], a.lk1[l], a.lk2[l], df, dtn, Qin[l], a.g, a.wave_speed, s.dt_f);
-}
-
 // Node n: its donor factor min(1, V / sum of the transfers it gives), summed
 // in ascending link order.
-__device__ __forceinline__ void donor_item(const DonorArgs &a, int n) {
+__device__ __forceinline__ float donor_item(const DonorArgs &a, int n) {
     const int js = a.node_link_start[n], je = a.node_link_start[n + 1];
     float given = 0.0f;
     for (int j0 = js; j0 < je; j0 += 4) {
@@ -166,16 +161,16 @@ __device__ __forceinline__ void donor_item(const DonorArgs &a, int n) {
             if (t[u] >= 0.0f ? (meta & NL_FROM) : (meta & NL_TO)) given += fabsf(t[u]);
         }
     }
-    a.fac[n] = fmin32(1.0f, fmax32(ff_val(ff_clamp0(__ldcg(&a.Vb[n]))), 0.0f) / fmax32(given, 1.0e-12f));
+    return fmin32(1.0f, fmax32(ff_val(ff_clamp0(__ldcg(&a.Vb[n]))), 0.0f) / fmax32(given, 1.0e-12f));
 }
 
 // Group g: limited transfers, node continuity, outfall, overflow return and
 // the group cell's final depth.
-__device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, int g, float (&led)[D2_TERMS]) {
+// gr = the group record grp[g].
+__device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, int4 gr, float (&led)[D2_TERMS]) {
     float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
     float *Qout = s.parity ? a.Q0 : a.Q1;
     const float dt = s.dt_f;
-    const int4 gr = a.grp[g];
     const int c = gr.x, k = gr.y;
     float h = 0.0f, area = 1.0f;
     uint32_t cflags = 0u;
@@ -300,34 +295,57 @@ __device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, 
 }
 
 __global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs a, int slot) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = n < a.N;
+    const float2 V = in ? ff_clamp0(a.Va[n]) : make_float2(0.0f, 0.0f);
+    const int j0 = in ? a.node_in_start[n] : 0, j1 = in ? a.node_in_start[n + 1] : 0;
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
     float led[D1_TERMS] = {0.0f, 0.0f};
-    if (n < a.N) node_item(a, s, n, led);
+    if (in) node_item(a, s, n, V, j0, j1, led);
     warp_add_ledger<D1_TERMS>(led, a.ledger);
 }
 
+// Link l: the transfer volume from the end volumes after the inlet exchange
+// (all inputs loaded before the step record; the flow of the step's parity).
 __global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a, int slot) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = l < a.L;
+    const int f = in ? a.link_from[l] : 0, to = in ? a.link_to[l] : 0;
+    float4 k0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), k1 = k0, k2 = k0;
+    float q0 = 0.0f, q1 = 0.0f, df = 0.0f, dtn = 0.0f;
+    if (in) {
+        k0 = a.lk0[l];
+        k1 = a.lk1[l];
+        k2 = a.lk2[l];
+        q0 = a.Q0[l];
+        q1 = a.Q1[l];
+        df = node_depth(__ldcg(&a.Vb[f]), a.node_area[f]);
+        dtn = node_depth(__ldcg(&a.Vb[to]), a.node_area[to]);
+    }
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l < a.L) link_item(a, s, l);
+    if (in) a.T[l] = link_transfer(k0, k1, k2, df, dtn, s.parity ? q1 : q0, a.g, a.wave_speed, s.dt_f);
 }
 
+// The donor factor depends on nothing the step record selects: it is formed
+// while the record loads and stored only on an active step.
 __global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs a, int slot) {
-    const StepCtrl s = a.ctrl[slot];
-    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n < a.N) donor_item(a, n);
+    const StepCtrl s = a.ctrl[slot];
+    if (n >= a.N) return;
+    const float fac = donor_item(a, n);
+    if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
+    a.fac[n] = fac;
 }
 
 __global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs a, int slot) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int4 gr = g < a.G ? a.grp[g] : make_int4(-1, -1, 0, 0);
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
     float led[D2_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (g < a.G) group_item(a, s, g, led);
+    if (g < a.G) group_item(a, s, gr, led);
     warp_add_ledger<D2_TERMS>(led, a.ledger);
 }
 
