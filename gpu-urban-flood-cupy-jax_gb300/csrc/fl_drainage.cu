@@ -89,6 +89,16 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
 // item's static indices, the values earlier kernels wrote) before that
 // record arrives, so its latency overlaps theirs instead of adding to the
 // dependent-load chain.
+//
+// k_links, k_donor and k_network are launched as programmatic dependents of
+// the kernel before them: each kernel lets its dependent launch as soon as
+// its own blocks run (griddepcontrol.launch_dependents), and the dependent
+// loads its static tables, then waits for the whole previous grid to finish
+// and its writes to be visible (griddepcontrol.wait) before it reads them.
+// The launch latency and the static loads of each kernel overlap the
+// previous one.  k_nodes follows the surface kernel with an ordinary launch.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // Capture limit factor of an inlet cell at depth h: its volume over the
 // summed capture requests of its inlets [q0, q1), in their order (reference
@@ -144,8 +154,8 @@ __device__ __forceinline__ void node_item(const NodeArgs &a, const StepCtrl &s, 
 
 // Node n: its donor factor min(1, V / sum of the transfers it gives), summed
 // in ascending link order.
-__device__ __forceinline__ float donor_item(const DonorArgs &a, int n) {
-    const int js = a.node_link_start[n], je = a.node_link_start[n + 1];
+// [js, je) = the node's link slots.
+__device__ __forceinline__ float donor_item(const DonorArgs &a, int n, int js, int je) {
     float given = 0.0f;
     for (int j0 = js; j0 < je; j0 += 4) {
         int2 e[4];
@@ -166,8 +176,9 @@ __device__ __forceinline__ float donor_item(const DonorArgs &a, int n) {
 
 // Group g: limited transfers, node continuity, outfall, overflow return and
 // the group cell's final depth.
-// gr = the group record grp[g].
-__device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, int4 gr, float (&led)[D2_TERMS]) {
+// gr = the group record grp[g]; ci = the cell info of its cell (if any).
+__device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, int4 gr, float4 ci,
+                                           float (&led)[D2_TERMS]) {
     float4 *hs = s.parity ? a.state0 : a.state1;  // written by k_surface this step
     float *Qout = s.parity ? a.Q0 : a.Q1;
     const float dt = s.dt_f;
@@ -176,7 +187,6 @@ __device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, 
     uint32_t cflags = 0u;
     if (c >= 0) {
         h = hs[c].x;
-        const float4 ci = a.cinfo[c];
         area = ci.x;
         cflags = __float_as_uint(ci.z);
         if (k >= 0) {  // the cell's inlet exchange, in its inlets' order
@@ -295,6 +305,7 @@ __device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, 
 }
 
 __global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs a, int slot) {
+    pdl_launch_dependents();
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = n < a.N;
     const float2 V = in ? ff_clamp0(a.Va[n]) : make_float2(0.0f, 0.0f);
@@ -309,19 +320,26 @@ __global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs 
 // Link l: the transfer volume from the end volumes after the inlet exchange
 // (all inputs loaded before the step record; the flow of the step's parity).
 __global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a, int slot) {
+    pdl_launch_dependents();
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = l < a.L;
     const int f = in ? a.link_from[l] : 0, to = in ? a.link_to[l] : 0;
     float4 k0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), k1 = k0, k2 = k0;
-    float q0 = 0.0f, q1 = 0.0f, df = 0.0f, dtn = 0.0f;
-    if (in) {
+    float q0 = 0.0f, q1 = 0.0f, af = 1.0f, at = 1.0f;
+    if (in) {  // static tables and the previous step's flow
         k0 = a.lk0[l];
         k1 = a.lk1[l];
         k2 = a.lk2[l];
         q0 = a.Q0[l];
         q1 = a.Q1[l];
-        df = node_depth(__ldcg(&a.Vb[f]), a.node_area[f]);
-        dtn = node_depth(__ldcg(&a.Vb[to]), a.node_area[to]);
+        af = a.node_area[f];
+        at = a.node_area[to];
+    }
+    pdl_wait();  // k_nodes' volumes
+    float df = 0.0f, dtn = 0.0f;
+    if (in) {
+        df = node_depth(__ldcg(&a.Vb[f]), af);
+        dtn = node_depth(__ldcg(&a.Vb[to]), at);
     }
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
@@ -331,21 +349,27 @@ __global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs 
 // The donor factor depends on nothing the step record selects: it is formed
 // while the record loads and stored only on an active step.
 __global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs a, int slot) {
+    pdl_launch_dependents();
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const StepCtrl s = a.ctrl[slot];
+    const int js = n < a.N ? a.node_link_start[n] : 0, je = n < a.N ? a.node_link_start[n + 1] : 0;
+    pdl_wait();  // k_links' transfers
     if (n >= a.N) return;
-    const float fac = donor_item(a, n);
+    const float fac = donor_item(a, n, js, je);
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
     a.fac[n] = fac;
 }
 
 __global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs a, int slot) {
+    pdl_launch_dependents();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int4 gr = g < a.G ? a.grp[g] : make_int4(-1, -1, 0, 0);
+    const float4 ci = gr.x >= 0 ? a.cinfo[gr.x] : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
     const StepCtrl s = a.ctrl[slot];
+    pdl_wait();  // k_donor's factors (and, through it, every earlier kernel's writes)
     if (!s.active || !(s.phases & FL_PHASE_DRAINAGE)) return;
     float led[D2_TERMS] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (g < a.G) group_item(a, s, gr, led);
+    if (g < a.G) group_item(a, s, gr, ci, led);
     warp_add_ledger<D2_TERMS>(led, a.ledger);
 }
 
@@ -502,19 +526,33 @@ cudaError_t launch_nodes(const NodeArgs &a, int slot, cudaStream_t stream) {
 
 int link_blocks(int32_t L) { return (L + 127) / 128 > 0 ? (L + 127) / 128 : 1; }
 
+// Launch as a programmatic dependent of the previous kernel in the stream.
+template <class Args>
+static cudaError_t launch_dependent(void (*kernel)(Args, int), int blocks, const Args &a, int slot,
+                                    cudaStream_t stream) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, a, slot);
+}
+
 cudaError_t launch_links(const LinkArgs &a, int slot, cudaStream_t stream) {
-    k_links<<<link_blocks(a.L), 128, 0, stream>>>(a, slot);
-    return cudaGetLastError();
+    return launch_dependent(k_links, link_blocks(a.L), a, slot, stream);
 }
 
 cudaError_t launch_donor(const DonorArgs &a, int slot, cudaStream_t stream) {
-    k_donor<<<node_blocks(a.N), 128, 0, stream>>>(a, slot);
-    return cudaGetLastError();
+    return launch_dependent(k_donor, node_blocks(a.N), a, slot, stream);
 }
 
 cudaError_t launch_network(const NetArgs &a, int slot, cudaStream_t stream) {
-    k_network<<<network_blocks(a.G), 128, 0, stream>>>(a, slot);
-    return cudaGetLastError();
+    return launch_dependent(k_network, network_blocks(a.G), a, slot, stream);
 }
 
 }  // namespace fl

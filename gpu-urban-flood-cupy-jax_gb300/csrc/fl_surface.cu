@@ -127,8 +127,7 @@ __global__ void __launch_bounds__(SURF_THREADS, 4) k_surface(const __grid_consta
         if (plan_next && tid == 0) plan_step(a.run, a.snap_t, a.hy, &a.ctrl[slot ^ 1], false, 0.0f, FL_PHASE_ALL);
         return;
     }
-    const StepCtrl s = a.ctrl[slot];
-    if (!s.active) return;
+    const StepCtrl s = a.ctrl[slot];  // checked after the set-up below, which overlaps its load
     const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
     float4 *__restrict__ out = s.parity ? a.state0 : a.state1;
     // barrier addresses: full(s) = base + 8 s, halo(s) = base + 16 + 8 s, empty(s) = base + 32 + 8 s
@@ -147,6 +146,7 @@ __global__ void __launch_bounds__(SURF_THREADS, 4) k_surface(const __grid_consta
         mbar_fence_init();
     }
     __syncthreads();  // the last block-wide barrier: the roles split here
+    if (!s.active) return;  // (uniform over the grid)
 
     if (tid >= TILE) {
         // ---------------------------------------------------------- producer
