@@ -7,11 +7,12 @@
 // atomicAdd.  Here every sum is a gather over a precomputed list in a fixed
 // order, so runs are reproducible, and every exchanged quantity is computed
 // once and read by both sides, so volume is conserved exactly as in the
-// reference.  Per step, after k_surface (which evaluates the inlet requests of
-// its inlet cells and their capture limit factor, reference :52-177):
-//   k_nodes   one thread per node: captures limited by their cells, the
-//             surcharge limit by the node's volume, the node volume after
-//             the exchange                                [reference :133-177]
+// reference.  Per step, after k_surface:
+//   k_nodes   one thread per node: the capture and surcharge requests of its
+//             inlets from the depth the surface step left in their cells
+//             [reference :52-131], captures limited by their cells' volume,
+//             surcharges by the node's, the node volume after the exchange
+//                                                         [reference :133-177]
 //   k_links   one thread per link: the semi-implicit link update from the two
 //             end volumes                              [pipe network :39-139]
 //   k_donor   one thread per node: its donor limit factor, its volume over
