@@ -59,6 +59,9 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
     rng = np.random.default_rng(seed)
     n = len(storms)
     copies = max(1, min(64, 2_000_000 // mf.C))
+    # warm-up, not timed (as the solvers are warmed up): the first pass of a
+    # batch shape loads the kernels and grows the allocator's pool
+    rollout_batch(model, mf, storms[:copies], [min(float(d), 3600.0) for d in durations[:copies]], copies=copies)
     torch.cuda.synchronize()
     t = time.perf_counter()
     preds = rollout_batch(model, mf, storms, durations, copies=copies)
