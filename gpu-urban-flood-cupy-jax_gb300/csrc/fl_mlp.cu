@@ -337,18 +337,32 @@ __device__ __forceinline__ void warp_load_chunk_a(const GemmArgs &g, const TileR
     }
 }
 
+// Bias and residual are read 8 columns (two 16-byte loads) at a time: N,
+// ldr and the column offsets are multiples of 8, the tensors 16-byte aligned.
 __device__ __forceinline__ void epilogue_store(const GemmArgs &g, int r, int nb, const uint32_t (&v)[32]) {
     if (r >= g.M) return;
 #pragma unroll
     for (int q = 0; q < 32; q += 8) {
         if (nb + q >= g.N) break;
+        float bs[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, rs[8];
+        if (g.bias) {
+            const float4 b0 = *(const float4 *)(g.bias + nb + q), b1 = *(const float4 *)(g.bias + nb + q + 4);
+            bs[0] = b0.x; bs[1] = b0.y; bs[2] = b0.z; bs[3] = b0.w;
+            bs[4] = b1.x; bs[5] = b1.y; bs[6] = b1.z; bs[7] = b1.w;
+        }
+        if (g.residual) {
+            const float *rp = g.residual + (int64_t)r * g.ldr + nb + q;
+            const float4 r0 = *(const float4 *)rp, r1 = *(const float4 *)(rp + 4);
+            rs[0] = r0.x; rs[1] = r0.y; rs[2] = r0.z; rs[3] = r0.w;
+            rs[4] = r1.x; rs[5] = r1.y; rs[6] = r1.z; rs[7] = r1.w;
+        }
         float x[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             float y = __uint_as_float(v[q + u]);
-            if (g.bias) y += g.bias[nb + q + u];
+            if (g.bias) y += bs[u];
             if (g.relu) y = fmaxf(y, 0.0f);
-            if (g.residual) y += g.residual[(int64_t)r * g.ldr + nb + q + u];
+            if (g.residual) y += rs[u];
             x[u] = y;
         }
         if (g.out_f32) {
@@ -579,9 +593,12 @@ extern "C" FL_API int fl_gemm_bf16(const FlGemmDesc *d, void *stream) {
     if (d->m < 1 || d->n < 1 || d->n_seg < 1 || d->n_seg > 3 || !d->b)
         return set_error(FL_E_INVALID, "fl_gemm_bf16: bad sizes or NULL B");
     if (!d->out_f32 && !d->out_bf16) return set_error(FL_E_INVALID, "fl_gemm_bf16: no output");
-    if (d->ldb % 8 || (d->out_f32 || d->out_bf16 ? d->ldo % 8 : 0) || d->ldo < d->n || (d->residual && d->ldr < d->n))
+    if (d->ldb % 8 || (d->out_f32 || d->out_bf16 ? d->ldo % 8 : 0) || d->ldo < d->n ||
+        (d->residual && (d->ldr < d->n || d->ldr % 8)))
         return set_error(FL_E_INVALID, "fl_gemm_bf16: leading dimensions must be multiples of 8 and cover n");
     if (d->n % 8) return set_error(FL_E_INVALID, "fl_gemm_bf16: n must be a multiple of 8");
+    if (((uintptr_t)d->bias | (uintptr_t)d->residual | (uintptr_t)d->out_f32 | (uintptr_t)d->out_bf16) % 16)
+        return set_error(FL_E_INVALID, "fl_gemm_bf16: bias, residual and outputs must be 16-byte aligned");
     GemmArgs g{};
     int32_t K = 0;
     for (int s = 0; s < d->n_seg; ++s) {
