@@ -310,7 +310,10 @@ __device__ __forceinline__ TileRows tile_rows(const GemmArgs &g, int m0, int pw,
     return t;
 }
 
-// Copy one 64-wide A chunk of a tile with the 32 threads of one warp.
+// Copy one 64-wide A chunk of a tile with the 32 threads of one warp: each
+// copy instruction moves four whole 128-byte row pieces (lane l: row
+// 4 i + l / 8, 16-byte piece l % 8), so every L2 sector is fetched once and
+// whole; a row's source index comes from the lane that loaded it.
 __device__ __forceinline__ void warp_load_chunk_a(const GemmArgs &g, const TileRows &tr, int chunk, uint32_t sdst,
                                                   int pw, int lane) {
     int seg = 0, kin = chunk * MM_BK;
@@ -319,21 +322,19 @@ __device__ __forceinline__ void warp_load_chunk_a(const GemmArgs &g, const TileR
         ++seg;
     }
     const GemmSeg s = g.a[seg];
+    const int64_t own0 = seg == 0 ? tr.r[0][0] : (seg == 1 ? tr.r[1][0] : tr.r[2][0]);
+    const int64_t own1 = seg == 0 ? tr.r[0][1] : (seg == 1 ? tr.r[1][1] : tr.r[2][1]);
+    const int c = lane & 7;
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        const int R = 64 * pw + lane + 32 * j;
-        const int64_t row = seg == 0 ? tr.r[0][j] : (seg == 1 ? tr.r[1][j] : tr.r[2][j]);
-        const uint32_t row_dst = sdst + (uint32_t)(R * 128);
-        if (row >= 0) {
-            const __nv_bfloat16 *src = s.base + row * s.ld + kin;
-#pragma unroll
-            for (int c = 0; c < 8; ++c) cp_async16(row_dst + (uint32_t)((c ^ (R & 7)) << 4), src + c * 8);
-        } else {
-#pragma unroll
-            for (int c = 0; c < 8; ++c)
-                asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(row_dst + (uint32_t)(c << 4)), "r"(0u)
-                             : "memory");
-        }
+    for (int i = 0; i < 16; ++i) {
+        const int rr = 4 * i + (lane >> 3);  // row within this warp's 64 (rows rr < 32 are owned as j = 0)
+        const int64_t row = __shfl_sync(0xffffffffu, i < 8 ? own0 : own1, rr & 31);
+        const int R = 64 * pw + rr;
+        const uint32_t dst = sdst + (uint32_t)(R * 128) + (uint32_t)((c ^ (R & 7)) << 4);
+        if (row >= 0)
+            cp_async16(dst, s.base + row * s.ld + kin + c * 8);
+        else
+            asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(dst), "r"(0u) : "memory");
     }
 }
 
