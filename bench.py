@@ -70,6 +70,24 @@ def dist_info():
     return rank, world, local
 
 
+def aggregate_ranks(total_ms: float, cell_steps: float, device=None):
+    """Whole-job figures of N replicas: the slowest rank's timed milliseconds
+    and the cell-steps of all ranks (each rank solves its own copy of the
+    city; there is no data exchange).  One process without a process group
+    returns its own figures."""
+
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(total_ms), float(cell_steps)
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    cs = torch.tensor([float(cell_steps)], dtype=torch.float64, device=device)
+    dist.all_reduce(cs)
+    return float(t.item()), float(cs.item())
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
 
@@ -329,14 +347,7 @@ def our_arm(args):
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    total_ms = float(sum(ms))
-    cell_steps = float(C) * float(sum(steps))
-    if world > 1:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        cs = torch.tensor([cell_steps], device=f"cuda:{local}", dtype=torch.float64)
-        torch.distributed.all_reduce(cs)
-        total_ms, cell_steps = float(t.item()), float(cs.item())
+    total_ms, cell_steps = aggregate_ranks(float(sum(ms)), float(C) * float(sum(steps)), device=f"cuda:{local}")
     value = cell_steps / (total_ms / 1000.0)
 
     # end to end through the C ABI with host buffers (pinned H2D in, D2H of snapshots + final state)
