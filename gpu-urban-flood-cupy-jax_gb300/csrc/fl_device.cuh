@@ -387,6 +387,13 @@ __device__ __forceinline__ void warp_add_ledger_at(const float (&v)[NT], float2 
     }
 }
 
+// --------------------------------------------------------------- programmatic dependent launch
+// launch_dependents lets a grid launched as a programmatic dependent of this
+// one start; wait blocks until every prerequisite grid has completed and its
+// writes are visible (a no-op in a grid launched without the attribute).
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // --------------------------------------------------------------- async copies
 // Bulk (TMA engine) copies global -> shared completing on an mbarrier, and
 // 16-byte cp.async gathers.  Every wait on an mbarrier is bounded in time.

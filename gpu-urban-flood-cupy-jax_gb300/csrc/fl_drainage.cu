@@ -98,8 +98,7 @@ __device__ __forceinline__ float node_depth(float2 V, float A) {
 // and its writes to be visible (griddepcontrol.wait) before it reads them.
 // The launch latency and the static loads of each kernel overlap the
 // previous one.  k_nodes follows the surface kernel with an ordinary launch.
-__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 
 // Capture limit factor of an inlet cell at depth h: its volume over the
 // summed capture requests of its inlets [q0, q1), in their order (reference

@@ -124,12 +124,10 @@ __global__ void __launch_bounds__(SURF_THREADS, 4) k_surface(const __grid_consta
     const int tid = threadIdx.x;
     const int ncta = (int)gridDim.x - 1;  // the last CTA plans
     if ((int)blockIdx.x == ncta) {
+        pdl_wait();
         if (plan_next && tid == 0) plan_step(a.run, a.snap_t, a.hy, &a.ctrl[slot ^ 1], false, 0.0f, FL_PHASE_ALL);
         return;
     }
-    const StepCtrl s = a.ctrl[slot];  // checked after the set-up below, which overlaps its load
-    const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
-    float4 *__restrict__ out = s.parity ? a.state0 : a.state1;
     // barrier addresses: full(s) = base + 8 s, halo(s) = base + 16 + 8 s, empty(s) = base + 32 + 8 s
     const uint32_t bar_base = smem_addr(s_bar);
     const TileStage S0 = stage_at(a, smem, 0), S1 = stage_at(a, smem, 1);
@@ -146,7 +144,14 @@ __global__ void __launch_bounds__(SURF_THREADS, 4) k_surface(const __grid_consta
         mbar_fence_init();
     }
     __syncthreads();  // the last block-wide barrier: the roles split here
+    // launched as a programmatic dependent of the step's previous kernel: the
+    // set-up above overlaps its end; the step record, the states and the wet
+    // time it (or an earlier kernel) wrote are read after this wait
+    pdl_wait();
+    const StepCtrl s = a.ctrl[slot];
     if (!s.active) return;  // (uniform over the grid)
+    const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
+    float4 *__restrict__ out = s.parity ? a.state0 : a.state1;
 
     if (tid >= TILE) {
         // ---------------------------------------------------------- producer
@@ -421,11 +426,23 @@ __global__ void k_volumes(const float4 *state0, const float4 *state1, const floa
 // Host launch wrappers (C++ linkage, used by fl_solver.cpp).
 namespace fl {
 
+// Launched as a programmatic dependent of the previous kernel in the stream
+// (the drainage kernel before it triggers at its start), so its CTAs are
+// scheduled and set up while that kernel finishes.
 cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next, int grid, int smem_bytes,
                            cudaStream_t stream) {
-    if (kind) k_surface<1><<<grid, SURF_THREADS, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
-    else k_surface<0><<<grid, SURF_THREADS, (size_t)smem_bytes, stream>>>(a, slot, plan_next);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(SURF_THREADS);
+    cfg.dynamicSmemBytes = (size_t)smem_bytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return kind ? cudaLaunchKernelEx(&cfg, k_surface<1>, a, slot, plan_next)
+                : cudaLaunchKernelEx(&cfg, k_surface<0>, a, slot, plan_next);
 }
 
 // The persistent grid of k_surface: as many compute CTAs as fit (never more
