@@ -56,6 +56,7 @@ struct GemmArgs {
     int32_t relu;
     int32_t k_chunks_per_split;      // chunks per z slice
     int32_t stages;                  // A ring depth (persistent kernel)
+    int32_t wide;                    // bias / residual / outputs allow 32-byte accesses (persistent kernel)
     int32_t *error;                  // set to FL_E_TIMEOUT if a wait gave up
 };
 
@@ -338,10 +339,77 @@ __device__ __forceinline__ void warp_load_chunk_a(const GemmArgs &g, const TileR
     }
 }
 
-// Bias and residual are read 8 columns (two 16-byte loads) at a time: N,
+// 32-byte global accesses (8 x 32 bits; the address is 32-byte aligned).
+__device__ __forceinline__ void ld8f(const float *p, float *d) {
+    asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3]), "=f"(d[4]), "=f"(d[5]), "=f"(d[6]), "=f"(d[7])
+                 : "l"(p));
+}
+__device__ __forceinline__ void st8f(float *p, const float *s) {
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(s[0]), "f"(s[1]), "f"(s[2]),
+                 "f"(s[3]), "f"(s[4]), "f"(s[5]), "f"(s[6]), "f"(s[7])
+                 : "memory");
+}
+__device__ __forceinline__ void st8u(void *p, const uint32_t *s) {
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(s[0]), "r"(s[1]), "r"(s[2]),
+                 "r"(s[3]), "r"(s[4]), "r"(s[5]), "r"(s[6]), "r"(s[7])
+                 : "memory");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *(uint32_t *)&h;
+}
+
+// The epilogue of one row's 32 columns [nb, nb + 32).  With g.wide, 16
+// columns at a time through 32-byte loads and stores (a bf16 row piece of 16
+// columns is one 32-byte store, an fp32 piece two): half the store
+// instructions of the 16-byte path and whole 32-byte sectors.  Otherwise
+// bias and residual are read 8 columns (two 16-byte loads) at a time: N,
 // ldr and the column offsets are multiples of 8, the tensors 16-byte aligned.
 __device__ __forceinline__ void epilogue_store(const GemmArgs &g, int r, int nb, const uint32_t (&v)[32]) {
     if (r >= g.M) return;
+    if (g.wide) {
+#pragma unroll
+        for (int q = 0; q < 32; q += 16) {
+            if (nb + q >= g.N) break;
+            const bool hi = nb + q + 8 < g.N;  // the upper 8 columns exist (N is a multiple of 8)
+            float bs[16], rs[16], x[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) bs[u] = rs[u] = 0.0f;
+            if (g.bias) {
+                ld8f(g.bias + nb + q, bs);
+                if (hi) ld8f(g.bias + nb + q + 8, bs + 8);
+            }
+            if (g.residual) {
+                const float *rp = g.residual + (int64_t)r * g.ldr + nb + q;
+                ld8f(rp, rs);
+                if (hi) ld8f(rp + 8, rs + 8);
+            }
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                float y = __uint_as_float(v[q + u]);
+                if (g.bias) y += bs[u];
+                if (g.relu) y = fmaxf(y, 0.0f);
+                if (g.residual) y += rs[u];
+                x[u] = y;
+            }
+            if (g.out_f32) {
+                float *p = g.out_f32 + (int64_t)r * g.ldo + nb + q;
+                st8f(p, x);
+                if (hi) st8f(p + 8, x + 8);
+            }
+            if (g.out_bf16) {
+                uint32_t w[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) w[u] = pack_bf16x2(x[2 * u], x[2 * u + 1]);
+                __nv_bfloat16 *p = g.out_bf16 + (int64_t)r * g.ldo + nb + q;
+                if (hi) st8u(p, w);
+                else *(uint4 *)p = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        return;
+    }
 #pragma unroll
     for (int q = 0; q < 32; q += 8) {
         if (nb + q >= g.N) break;
@@ -541,6 +609,13 @@ cudaError_t launch_gemm_bf16_pers(const GemmArgs &g, cudaStream_t stream) {
     const int gx = std::max(1, std::min(tiles, std::max(1, sms / gy)));
     GemmArgs a = g;
     a.stages = pers_stages(g.K);
+    // 32-byte accesses: 32-byte aligned tensors; a bf16 row piece of 16
+    // columns must start on a 32-byte boundary (ldo a multiple of 16)
+    a.wide = ((((uintptr_t)g.bias | (uintptr_t)g.residual | (uintptr_t)g.out_f32 | (uintptr_t)g.out_bf16) % 32) == 0 &&
+              (!g.residual || g.ldr % 8 == 0) && (!(g.out_f32 || g.out_bf16) || g.ldo % 8 == 0) &&
+              (!g.out_bf16 || g.ldo % 16 == 0))
+                 ? 1
+                 : 0;
     k_gemm_bf16_pers<<<dim3(gx, gy, 1), PG_THREADS, pers_smem_bytes(g.K), stream>>>(a);
     return cudaGetLastError();
 }
