@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(256) k_segment_sum(const float *__restrict__ s
     const int p0 = start[warp], p1 = start[warp + 1];
     for (int c = lane * 4; c < width; c += 128) {
         float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        for (int p = p0; p < p1; ++p) {
+#pragma unroll 4
+        for (int p = p0; p < p1; ++p) {  // (unrolled: the loads of several rows in flight, the sum in order)
             const int64_t row = order ? (int64_t)order[p] : (int64_t)p;
             const float4 v = *(const float4 *)(src + row * lds + col0 + c);
             acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
