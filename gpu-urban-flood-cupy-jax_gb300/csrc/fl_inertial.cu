@@ -25,6 +25,8 @@
 namespace fl {
 
 __global__ void __launch_bounds__(256) k_li_edges(const __grid_constant__ LiArgs a, int slot) {
+    pdl_launch_dependents();  // the cell kernel may launch and wait meanwhile
+    pdl_wait();               // the previous step's kernels
     const StepCtrl s = a.ctrl[slot];
     if (!s.active || !(s.phases & FL_PHASE_SURFACE)) return;
     const float4 *__restrict__ in = s.parity ? a.state1 : a.state0;
@@ -89,6 +91,7 @@ __device__ __forceinline__ float li_donor_scale(uint32_t sb, float4 q4, float h,
 
 template <int KIND>
 __global__ void __launch_bounds__(256) k_li_cells(const __grid_constant__ LiArgs a, int slot, int plan_next) {
+    pdl_wait();  // the discharges of k_li_edges (and every earlier kernel's writes)
     if ((int)blockIdx.x == (int)gridDim.x - 1) {  // the last block plans the next step
         if (plan_next && threadIdx.x == 0) plan_step(a.run, a.snap_t, a.hy, &a.ctrl[slot ^ 1], false, 0.0f, FL_PHASE_ALL);
         return;
@@ -193,13 +196,24 @@ __global__ void __launch_bounds__(256) k_li_cells(const __grid_constant__ LiArgs
 int li_edge_blocks(int32_t E, int sms) { return std::max(1, std::min(sms * 8, (E + 255) / 256)); }
 int li_cell_blocks(int32_t C) { return (C + 255) / 256 + 1; }  // + the planner block
 
+// Both launched as programmatic dependents of the kernel before them, so
+// each one's launch overlaps the end of the previous one.
 cudaError_t launch_li(const LiArgs &a, int kind, int slot, int plan_next, int sms, cudaStream_t stream) {
-    k_li_edges<<<li_edge_blocks(a.E, sms), 256, 0, stream>>>(a, slot);
-    if (kind == 1)
-        k_li_cells<1><<<li_cell_blocks(a.C), 256, 0, stream>>>(a, slot, plan_next);
-    else
-        k_li_cells<0><<<li_cell_blocks(a.C), 256, 0, stream>>>(a, slot, plan_next);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3((unsigned)li_edge_blocks(a.E, sms));
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_li_edges, a, slot);
+    if (e != cudaSuccess) return e;
+    cfg.gridDim = dim3((unsigned)li_cell_blocks(a.C));
+    return kind == 1 ? cudaLaunchKernelEx(&cfg, k_li_cells<1>, a, slot, plan_next)
+                     : cudaLaunchKernelEx(&cfg, k_li_cells<0>, a, slot, plan_next);
 }
 
 }  // namespace fl
