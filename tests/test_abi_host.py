@@ -166,3 +166,33 @@ def test_plan_accepts_surcharge_table_and_rejects_bad_entries(lib):
     short = np.asarray(cp.surcharge_return_weight)[:-1]
     with pytest.raises(ValueError, match="differ in length"):
         native.plan_check(st, TriangularNodeCouplingTopology(**{**cp.__dict__, "surcharge_return_weight": short}), pp)
+
+
+def _gemm_desc(**kw):
+    """A well-formed GEMM descriptor with placeholder device addresses (the
+    checks below run before anything is dereferenced)."""
+
+    import ctypes as C
+
+    d = native.FlGemmDesc()
+    d.a[0] = native.FlGemmSegment(C.c_void_p(0x10000), None, 128, 128)
+    d.n_seg, d.m, d.n = 1, 256, 128
+    d.b, d.ldb = C.c_void_p(0x20000), 128
+    d.out_bf16, d.ldo = C.c_void_p(0x30000), 128
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+@pytest.mark.parametrize("field,value", [("out_bf16", 0x30008), ("bias", 0x40004), ("residual", 0x50008),
+                                         ("ldo", 100), ("n", 60)])
+def test_gemm_rejects_misaligned_or_ragged_arguments(lib, field, value):
+    import ctypes as C
+
+    kw = {field: C.c_void_p(value) if field in ("out_bf16", "bias", "residual") else value}
+    if field == "residual":
+        kw["ldr"] = 128
+    d = _gemm_desc(**kw)
+    rc = native.load().fl_gemm_bf16(C.byref(d), None)
+    assert rc == native.FL_E_INVALID
+    assert b"fl_gemm_bf16" in native.load().fl_last_error()

@@ -69,6 +69,32 @@ def test_gemm_gathered_segments_bias_relu_residual(tiled):
     close(outb.float(), ref, rtol=1e-2)
 
 
+@pytest.mark.parametrize("n", [128, 200])
+def test_gemm_epilogue_on_16_byte_aligned_and_padded_outputs(n):
+    """Outputs with a leading dimension that is not a multiple of 16 and a
+    bias / residual that are 16- but not 32-byte aligned take the epilogue's
+    16-byte path; n = 200 also leaves a ragged last 16-column group."""
+
+    from floodgb.surrogate import ops
+
+    m, k, ldo = 700, 128, n + 8
+    a = bf16(m, k, seed=7)
+    w = bf16(n, k, scale=0.05, seed=8)
+    g = torch.Generator(device="cuda").manual_seed(9)
+    bias_buf = torch.randn(n + 4, device="cuda", generator=g)
+    bias = bias_buf[4:]  # 16-byte offset
+    res_buf = torch.randn(m * ldo + 4, device="cuda", generator=g)
+    res = res_buf[4:].view(m, ldo)
+    outb_buf = torch.zeros(m, ldo, device="cuda", dtype=torch.bfloat16)
+    out_buf = torch.zeros(m, ldo, device="cuda", dtype=torch.float32)
+    ops.gemm([(a, None, k)], w, bias=bias, residual=res, out_f32=out_buf, out_bf16=outb_buf, relu=True)
+    ops.status()
+    ref = torch.relu(a.float() @ w.float().T + bias) + res[:, :n]
+    close(out_buf[:, :n], ref)
+    close(outb_buf[:, :n].float(), ref, rtol=1e-2)
+    assert out_buf[:, n:].abs().max().item() == 0.0  # padding columns untouched
+
+
 def test_gemm_split_k_partials_sum_to_product():
     from floodgb.surrogate import ops
 
