@@ -28,7 +28,9 @@ __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
 __device__ __forceinline__ float fsqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
 
 // Hydrostatic-reconstruction flux pair with the HLL Riemann solver on the
-// reconstructed states (reference equations.py:20-152).  Same algebra as the
+// reconstructed states (reference equations.py:20-152).  Its maxima and
+// minima are the hardware's single-instruction fmaxf / fminf (the same as
+// np.maximum / np.minimum on these finite values, up to the sign of zero).  Same algebra as the
 // reference with three rewrites that do not change the value beyond rounding:
 // a velocity is a product with one reciprocal of the depth; the HLL velocity
 // of a reconstructed state (hu* / h* with hu* = u h*) is u itself; and the
@@ -38,9 +40,9 @@ __device__ __forceinline__ float fsqrt(float x) { return x > 0.0f ? x * rsqrtf(x
 __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, float zL, float hR,
                                             float huR, float hvR, float zR, float nx, float ny,
                                             float g, float half_g, float md) {
-    const float h_l = fmax32(hL, 0.0f), h_r = fmax32(hR, 0.0f);
-    const float zs = fmax32(zL, zR);
-    const float hls = fmax32(h_l + zL - zs, 0.0f), hrs = fmax32(h_r + zR - zs, 0.0f);
+    const float h_l = fmaxf(hL, 0.0f), h_r = fmaxf(hR, 0.0f);
+    const float zs = fmaxf(zL, zR);
+    const float hls = fmaxf(h_l + zL - zs, 0.0f), hrs = fmaxf(h_r + zR - zs, 0.0f);
     const float il = h_l > md ? rcp(h_l) : 0.0f;
     const float ir = h_r > md ? rcp(h_r) : 0.0f;
     const float u_l = huL * il, v_l = hvL * il, u_r = huR * ir, v_r = hvR * ir;
@@ -52,8 +54,8 @@ __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, floa
     const float hul = u_l * hls, hvl = v_l * hls, hur = u_r * hrs, hvr = v_r * hrs;
     const float fhl = hls * un_l, fhul = hul * un_l + p_l * nx, fhvl = hvl * un_l + p_l * ny;
     const float fhr = hrs * un_r, fhur = hur * un_r + p_r * nx, fhvr = hvr * un_r + p_r * ny;
-    const float sl = fmin32(un_l - c_l, un_r - c_r);
-    const float sr = fmax32(un_l + c_l, un_r + c_r);
+    const float sl = fminf(un_l - c_l, un_r - c_r);
+    const float sr = fmaxf(un_l + c_l, un_r + c_r);
     const float d = sr - sl;
     const float inv = fabsf(d) > 1.0e-12f ? rcp(d) : 1.0f;
     const float slsr = sl * sr;
@@ -171,12 +173,12 @@ __device__ __forceinline__ CellNew cell_update(const float4 st, const float4 ci,
     }
     const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
     const float ia = rcp(ci.x);
-    float hn = fmax32(st.x + dt * d0 * ia, 0.0f);
+    float hn = fmaxf(st.x + dt * d0 * ia, 0.0f);
     float hun = st.y + dt * d1 * ia;
     float hvn = st.z + dt * d2 * ia;
     // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
     const bool wet = hn > md;
-    const float hs = fmax32(hn, md);
+    const float hs = fmaxf(hn, md);
     const float ih = rcp(hs);
     const float uu = hun * ih, vv = hvn * ih;
     const float speed = fsqrt(uu * uu + vv * vv);
@@ -187,11 +189,11 @@ __device__ __forceinline__ CellNew cell_update(const float4 st, const float4 ci,
     hun = wet ? hun * idamp : 0.0f;
     hvn = wet ? hvn * idamp : 0.0f;
     // rainfall, infiltration, momentum rescale, dry zeroing
-    const float rd = fmax32(rain, 0.0f) * dt;
+    const float rd = fmaxf(rain, 0.0f) * dt;
     const float h1 = hn + rd;
-    const float id = fmin32(h1, fmax32(infil, 0.0f) * dt);
+    const float id = fminf(h1, fmaxf(infil, 0.0f) * dt);
     const float h2 = h1 - id;
-    const float scale = (h1 > md) ? h2 * rcp(fmax32(h1, md)) : 0.0f;
+    const float scale = (h1 > md) ? h2 * rcp(fmaxf(h1, md)) : 0.0f;
     const bool wet2 = h2 > md;
     CellNew r;
     r.h = h2;
