@@ -25,7 +25,11 @@ struct EdgeFlux {
 // arithmetic is instruction-bound, and these keep it within a few ulp of the
 // correctly rounded operations the reference uses.
 __device__ __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
-__device__ __forceinline__ float fsqrt(float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; }
+__device__ __forceinline__ float fsqrt(float x) {  // x >= 0; one approximate-square-root instruction
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // Hydrostatic-reconstruction flux pair with the HLL Riemann solver on the
 // reconstructed states (reference equations.py:20-152).  Its maxima and
@@ -34,7 +38,7 @@ __device__ __forceinline__ float fsqrt(float x) { return x > 0.0f ? x * rsqrtf(x
 // reference with three rewrites that do not change the value beyond rounding:
 // a velocity is a product with one reciprocal of the depth; the HLL velocity
 // of a reconstructed state (hu* / h* with hu* = u h*) is u itself; and the
-// three HLL branches are evaluated and selected without branching.  Both
+// three HLL cases are one formula with clamped wave speeds.  Both
 // cells of an edge call this with the edge's own (left, right) order at a
 // single call site, so they get bit-identical results.
 __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, float zL, float hR,
@@ -54,18 +58,19 @@ __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, floa
     const float hul = u_l * hls, hvl = v_l * hls, hur = u_r * hrs, hvr = v_r * hrs;
     const float fhl = hls * un_l, fhul = hul * un_l + p_l * nx, fhvl = hvl * un_l + p_l * ny;
     const float fhr = hrs * un_r, fhur = hur * un_r + p_r * nx, fhvr = hvr * un_r + p_r * ny;
-    const float sl = fminf(un_l - c_l, un_r - c_r);
-    const float sr = fmaxf(un_l + c_l, un_r + c_r);
+    // HLL with the wave speeds clamped to sl <= 0 <= sr: one formula gives
+    // the left flux when sl >= 0 (sl -> 0: sr FL / sr), the right one when
+    // sr <= 0, and the star-region flux otherwise (the reference selects the
+    // three cases; here they agree to rounding, without the selects)
+    const float sl = fminf(fminf(un_l - c_l, un_r - c_r), 0.0f);
+    const float sr = fmaxf(fmaxf(un_l + c_l, un_r + c_r), 0.0f);
     const float d = sr - sl;
-    const float inv = fabsf(d) > 1.0e-12f ? rcp(d) : 1.0f;
+    const float inv = d > 1.0e-12f ? rcp(d) : 0.0f;  // both speeds ~0: still water, no flux
     const float slsr = sl * sr;
-    const float mh = (sr * fhl - sl * fhr + slsr * (hrs - hls)) * inv;
-    const float mhu = (sr * fhul - sl * fhur + slsr * (hur - hul)) * inv;
-    const float mhv = (sr * fhvl - sl * fhvr + slsr * (hvr - hvl)) * inv;
-    const bool left = sl >= 0.0f, right = sr <= 0.0f, dry = !(wl || wr);
-    float fh = left ? fhl : (right ? fhr : mh);
-    float fhu = left ? fhul : (right ? fhur : mhu);
-    float fhv = left ? fhvl : (right ? fhvr : mhv);
+    const bool dry = !(wl || wr);
+    float fh = (sr * fhl - sl * fhr + slsr * (hrs - hls)) * inv;
+    float fhu = (sr * fhul - sl * fhur + slsr * (hur - hul)) * inv;
+    float fhv = (sr * fhvl - sl * fhvr + slsr * (hvr - hvl)) * inv;
     fh = dry ? 0.0f : fh;
     fhu = dry ? 0.0f : fhu;
     fhv = dry ? 0.0f : fhv;
