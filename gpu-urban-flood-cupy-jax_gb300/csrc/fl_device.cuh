@@ -177,19 +177,18 @@ __device__ __forceinline__ CellNew cell_update(const float4 st, const float4 ci,
         }
     }
     const float d0 = L0 + R0, d1 = L1 + R1, d2 = L2 + R2;
-    const float ia = rcp(ci.x);
+    const float ia = ci.w;  // 1 / area, formed on the host
     float hn = fmaxf(st.x + dt * d0 * ia, 0.0f);
     float hun = st.y + dt * d1 * ia;
     float hvn = st.z + dt * d2 * ia;
-    // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3)
+    // semi-implicit Manning damping 1 + dt g n^2 |u| / h^(4/3), with
+    // |u| / h^(4/3) = |hu| h^(-7/3)
     const bool wet = hn > md;
     const float hs = fmaxf(hn, md);
-    const float ih = rcp(hs);
-    const float uu = hun * ih, vv = hvn * ih;
-    const float speed = fsqrt(uu * uu + vv * vv);
+    const float q = fsqrt(hun * hun + hvn * hvn);
     const float n = ci.y;
-    const float h43 = __expf(1.3333334f * __logf(hs));
-    const float damping = 1.0f + dtg * (n * n) * speed * rcp(h43);
+    const float hpow = __expf(-2.3333333f * __logf(hs));
+    const float damping = 1.0f + dtg * (n * n) * q * hpow;
     const float idamp = rcp(damping);
     hun = wet ? hun * idamp : 0.0f;
     hvn = wet ? hvn * idamp : 0.0f;
@@ -198,7 +197,7 @@ __device__ __forceinline__ CellNew cell_update(const float4 st, const float4 ci,
     const float h1 = hn + rd;
     const float id = fminf(h1, fmaxf(infil, 0.0f) * dt);
     const float h2 = h1 - id;
-    const float scale = (h1 > md) ? h2 * rcp(fmaxf(h1, md)) : 0.0f;
+    const float scale = (h1 > md) ? h2 * rcp(h1) : 0.0f;
     const bool wet2 = h2 > md;
     CellNew r;
     r.h = h2;

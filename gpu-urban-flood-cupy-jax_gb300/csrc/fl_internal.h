@@ -40,7 +40,7 @@ constexpr int EB_CODE_SHIFT = 29;          // bits 29-31: effective boundary cod
 // tile_info[t] = {first entry, entry count, first halo index (multiple of 4), halo count}
 constexpr int64_t MAX_CELLS = 0x7FFFFFFE;
 
-// cinfo[c] = {area, manning, flags (bits), 0 (reserved)}
+// cinfo[c] = {area, manning, flags (bits), 1 / area}
 constexpr uint32_t CELL_ACTIVE = 1u;
 constexpr uint32_t CELL_COUPLED = 2u;       // drainage writes this cell's final depth
 constexpr uint32_t CELL_SURCHARGE = 4u;     // a weighted surcharge-return cell (k_surcharge finishes it)
@@ -138,7 +138,7 @@ struct InflowArgs {
 };
 
 struct SurfArgs {
-    const float4 *cinfo;          // [Cp] {area, manning, flags, reserved}
+    const float4 *cinfo;          // [Cp] {area, manning, flags, 1 / area}
     const int4 *tile_info;        // [tiles]
     const float4 *ent;            // entries {nx, ny, len, bits}
     const int32_t *halo_src;      // halo cells of each tile (padded to 4 per tile)

@@ -182,11 +182,9 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
         if (coupled[c]) info |= CELL_COUPLED;
         for (int k = 0; k < count[c]; ++k)
             if (inc_right[c * 3 + k]) info |= 1u << (CELL_RIGHT_SHIFT + k);
-        uint32_t none = 0;
-        float fi, fk;
+        float fi;
         memcpy(&fi, &info, 4);
-        memcpy(&fk, &none, 4);
-        L.cinfo[i] = f4(m.cell_area_m2[c], m.manning_n[c], fi, fk);
+        L.cinfo[i] = f4(m.cell_area_m2[c], m.manning_n[c], fi, 1.0f / m.cell_area_m2[c]);
         L.char_len[i] = m.characteristic_length_m[c];
         L.bed[i] = m.bed_elevation_m[c];
     }
@@ -200,7 +198,7 @@ int build_mesh_layout(const FlMeshDesc &m, const FlDrainDesc *d, HostLayout &L) 
         uint32_t none = 0;
         float fz;
         memcpy(&fz, &none, 4);
-        L.cinfo.resize((size_t)L.Cp, f4(1.0f, 0.0f, fz, fz));  // padding cells: inactive, never referenced
+        L.cinfo.resize((size_t)L.Cp, f4(1.0f, 0.0f, fz, 1.0f));  // padding cells: inactive, never referenced
     }
     L.tile_info.assign((size_t)tiles, make_int4(0, 0, 0, 0));
     L.ent.clear();
