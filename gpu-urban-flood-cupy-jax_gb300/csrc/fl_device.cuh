@@ -41,8 +41,9 @@ __device__ __forceinline__ float fsqrt(float x) {  // x >= 0; one approximate-sq
 // three HLL cases are one formula with clamped wave speeds.  Both
 // cells of an edge call this with the edge's own (left, right) order at a
 // single call site, so they get bit-identical results.
+// The returned fluxes are per unit length times len (the face length).
 __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, float zL, float hR,
-                                            float huR, float hvR, float zR, float nx, float ny,
+                                            float huR, float hvR, float zR, float nx, float ny, float len,
                                             float g, float half_g, float md) {
     const float h_l = fmaxf(hL, 0.0f), h_r = fmaxf(hR, 0.0f);
     const float zs = fmaxf(zL, zR);
@@ -65,7 +66,7 @@ __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, floa
     const float sl = fminf(fminf(un_l - c_l, un_r - c_r), 0.0f);
     const float sr = fmaxf(fmaxf(un_l + c_l, un_r + c_r), 0.0f);
     const float d = sr - sl;
-    const float inv = d > 1.0e-12f ? rcp(d) : 0.0f;  // both speeds ~0: still water, no flux
+    const float inv = d > 1.0e-12f ? rcp(d) * len : 0.0f;  // both speeds ~0: still water, no flux
     const float slsr = sl * sr;
     const bool dry = !(wl || wr);
     float fh = (sr * fhl - sl * fhr + slsr * (hrs - hls)) * inv;
@@ -76,12 +77,13 @@ __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, floa
     fhv = dry ? 0.0f : fhv;
     const float pcl = half_g * (h_l * h_l - hls * hls);
     const float pcr = half_g * (h_r * h_r - hrs * hrs);
+    const float nxl = nx * len, nyl = ny * len;
     EdgeFlux f;
     f.h = fh;
-    f.huL = fhu + pcl * nx;
-    f.hvL = fhv + pcl * ny;
-    f.huR = fhu + pcr * nx;
-    f.hvR = fhv + pcr * ny;
+    f.huL = fhu + pcl * nxl;
+    f.hvL = fhv + pcl * nyl;
+    f.huR = fhu + pcr * nxl;
+    f.hvR = fhv + pcr * nyl;
     return f;
 }
 
@@ -137,21 +139,21 @@ __device__ __forceinline__ void tile_entry(const float4 en, const float4 *st, fl
     float4 Ls = st[li];
     if (!(f & EB_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
     const float4 Rs = ai ? st[ri] : ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, en.x, en.y, code, stage);
-    EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, en.x, en.y, g, half_g, md);
-    const float len = en.z;
+    // fluxes times the face length
+    EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, en.x, en.y, en.z, g, half_g, md);
     if (f & EB_LPRESENT) {
         if (!(f & EB_INTERIOR) && code == 4 && fl.h < 0.0f) {
             fl.h = 0.0f; fl.huL = 0.0f; fl.hvL = 0.0f;
         }
-        s_flux[li * 3 + ((f >> EB_LSLOT_SHIFT) & 3u)] = make_float4((-fl.h) * len, (-fl.huL) * len, (-fl.hvL) * len, 0.0f);
+        s_flux[li * 3 + ((f >> EB_LSLOT_SHIFT) & 3u)] = make_float4(-fl.h, -fl.huL, -fl.hvL, 0.0f);
         if (!ai) {
-            const float b = fl.h * len * dt;
+            const float b = fl.h * dt;
             led_in += fmax32(-b, 0.0f);
             led_out += fmax32(b, 0.0f);
         }
     }
     if (f & EB_RPRESENT)
-        s_flux[ri * 3 + ((f >> EB_RSLOT_SHIFT) & 3u)] = make_float4(fl.h * len, fl.huR * len, fl.hvR * len, 0.0f);
+        s_flux[ri * 3 + ((f >> EB_RSLOT_SHIFT) & 3u)] = make_float4(fl.h, fl.huR, fl.hvR, 0.0f);
 }
 
 // Phase 3 of a surface tile for one active cell: the sum of its slot
