@@ -32,16 +32,16 @@ __device__ __forceinline__ float fsqrt(float x) {  // x >= 0; one approximate-sq
 }
 
 // Hydrostatic-reconstruction flux pair with the HLL Riemann solver on the
-// reconstructed states (reference equations.py:20-152).  Its maxima and
-// minima are the hardware's single-instruction fmaxf / fminf (the same as
-// np.maximum / np.minimum on these finite values, up to the sign of zero).  Same algebra as the
-// reference with three rewrites that do not change the value beyond rounding:
-// a velocity is a product with one reciprocal of the depth; the HLL velocity
-// of a reconstructed state (hu* / h* with hu* = u h*) is u itself; and the
-// three HLL cases are one formula with clamped wave speeds.  Both
-// cells of an edge call this with the edge's own (left, right) order at a
-// single call site, so they get bit-identical results.
-// The returned fluxes are per unit length times len (the face length).
+// reconstructed states (reference equations.py:20-152), times the face
+// length len.  Same algebra as the reference with rewrites that do not
+// change the value beyond rounding: a velocity is a product with one
+// reciprocal of the depth; the HLL velocity of a reconstructed state
+// (hu* / h* with hu* = u h*) is u itself; the three HLL cases are one
+// formula with clamped wave speeds; maxima and minima are the hardware's
+// single-instruction fmaxf / fminf (np.maximum / np.minimum on these finite
+// values, up to the sign of zero).  Both cells of an edge call this with the
+// edge's own (left, right) order at a single call site, so they get
+// bit-identical results.
 __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, float zL, float hR,
                                             float huR, float hvR, float zR, float nx, float ny, float len,
                                             float g, float half_g, float md) {
