@@ -66,15 +66,13 @@ __device__ __forceinline__ EdgeFlux hr_flux(float hL, float huL, float hvL, floa
     const float sl = fminf(fminf(un_l - c_l, un_r - c_r), 0.0f);
     const float sr = fmaxf(fmaxf(un_l + c_l, un_r + c_r), 0.0f);
     const float d = sr - sl;
-    const float inv = d > 1.0e-12f ? rcp(d) * len : 0.0f;  // both speeds ~0: still water, no flux
+    // both speeds ~0 (still water) or both sides dry: no HLL flux (the
+    // products below are finite, so a zero factor zeroes them)
+    const float inv = (d > 1.0e-12f && (wl || wr)) ? rcp(d) * len : 0.0f;
     const float slsr = sl * sr;
-    const bool dry = !(wl || wr);
-    float fh = (sr * fhl - sl * fhr + slsr * (hrs - hls)) * inv;
-    float fhu = (sr * fhul - sl * fhur + slsr * (hur - hul)) * inv;
-    float fhv = (sr * fhvl - sl * fhvr + slsr * (hvr - hvl)) * inv;
-    fh = dry ? 0.0f : fh;
-    fhu = dry ? 0.0f : fhu;
-    fhv = dry ? 0.0f : fhv;
+    const float fh = (sr * fhl - sl * fhr + slsr * (hrs - hls)) * inv;
+    const float fhu = (sr * fhul - sl * fhur + slsr * (hur - hul)) * inv;
+    const float fhv = (sr * fhvl - sl * fhvr + slsr * (hvr - hvl)) * inv;
     const float pcl = half_g * (h_l * h_l - hls * hls);
     const float pcr = half_g * (h_r * h_r - hrs * hrs);
     const float nxl = nx * len, nyl = ny * len;
@@ -214,7 +212,7 @@ __device__ __forceinline__ CellNew cell_update(const float4 st, const float4 ci,
 // reference computes it.  When |q|^2 < 0.9999 (vmax max(h, 1e-8))^2 the exact
 // speed is below vmax, the exact scale is 1 and the momenta are unchanged.
 __device__ __forceinline__ void clamp_velocity_exact(float h, float &hu, float &hv, float vmax) {
-    const float hm = fmax32(h, 1.0e-8f);
+    const float hm = fmaxf(h, 1.0e-8f);  // = max(h, 1e-8) for every h, NaN included
     const float lim = vmax * hm;
     if (!(hu * hu + hv * hv < 0.9999f * (lim * lim))) {
         const float speed = xdiv(xsqrt(xadd(xmul(hu, hu), xmul(hv, hv))), hm);
