@@ -134,9 +134,13 @@ __device__ __forceinline__ void tile_entry(const float4 en, const float4 *st, fl
     const uint32_t li = f & EB_IDX_MASK, ri = (f >> EB_RIGHT_SHIFT) & EB_IDX_MASK;
     const bool ai = (f & EB_AI) != 0;
     const int code = (int)(f >> EB_CODE_SHIFT) - 1;
-    float4 Ls = st[li];
-    if (!(f & EB_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
-    const float4 Rs = ai ? st[ri] : ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, en.x, en.y, code, stage);
+    float4 Ls = st[li], Rs;
+    if (ai) {  // both cells active (entries are grouped by kind: warp-uniform)
+        Rs = st[ri];
+    } else {
+        if (!(f & EB_LACTIVE)) Ls = make_float4(0.0f, 0.0f, 0.0f, Ls.w);
+        Rs = ghost_state(Ls.x, Ls.y, Ls.z, Ls.w, en.x, en.y, code, stage);
+    }
     // fluxes times the face length
     EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, en.x, en.y, en.z, g, half_g, md);
     if (f & EB_LPRESENT) {
