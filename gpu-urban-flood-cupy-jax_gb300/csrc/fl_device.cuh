@@ -143,19 +143,20 @@ __device__ __forceinline__ void tile_entry(const float4 en, const float4 *st, fl
     }
     // fluxes times the face length
     EdgeFlux fl = hr_flux(Ls.x, Ls.y, Ls.z, Ls.w, Rs.x, Rs.y, Rs.z, Rs.w, en.x, en.y, en.z, g, half_g, md);
-    if (f & EB_LPRESENT) {
+    if (ai) {  // an interior face: no outflow-only rule, no boundary volume
+        if (f & EB_LPRESENT) s_flux[li * 3 + ((f >> EB_LSLOT_SHIFT) & 3u)] = make_float4(-fl.h, -fl.huL, -fl.hvL, 0.0f);
+        if (f & EB_RPRESENT) s_flux[ri * 3 + ((f >> EB_RSLOT_SHIFT) & 3u)] = make_float4(fl.h, fl.huR, fl.hvR, 0.0f);
+        return;
+    }
+    if (f & EB_LPRESENT) {  // (a non-active-interior face is present on its left side only)
         if (!(f & EB_INTERIOR) && code == 4 && fl.h < 0.0f) {
             fl.h = 0.0f; fl.huL = 0.0f; fl.hvL = 0.0f;
         }
         s_flux[li * 3 + ((f >> EB_LSLOT_SHIFT) & 3u)] = make_float4(-fl.h, -fl.huL, -fl.hvL, 0.0f);
-        if (!ai) {
-            const float b = fl.h * dt;
-            led_in += fmax32(-b, 0.0f);
-            led_out += fmax32(b, 0.0f);
-        }
+        const float b = fl.h * dt;
+        led_in += fmax32(-b, 0.0f);
+        led_out += fmax32(b, 0.0f);
     }
-    if (f & EB_RPRESENT)
-        s_flux[ri * 3 + ((f >> EB_RSLOT_SHIFT) & 3u)] = make_float4(fl.h, fl.huR, fl.hvR, 0.0f);
 }
 
 // Phase 3 of a surface tile for one active cell: the sum of its slot
