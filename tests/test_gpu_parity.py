@@ -161,6 +161,27 @@ def test_small_workload_hour_gates_against_oracle():
     np.testing.assert_allclose(led["rainfall_input_m3"], ref.ledger["rainfall_input_m3"], rtol=1e-4)
 
 
+@pytest.mark.parametrize("n", [1, 16, 17, 23])
+def test_tiny_and_ragged_meshes_against_oracle(n):
+    """Meshes of 2 triangles (far below one 256-cell tile), exactly two
+    tiles (512), and ragged last tiles (578, 1058 cells), each over 10
+    simulated minutes, against the oracle."""
+
+    sc = make_grid_city(n=n, size_m=10.0 * n, seed=n)
+    cfg = load_config(None, dict(sc.overrides, **{"solver.duration_min": 10.0, "solver.snapshot_interval_min": 5.0}))
+    ref = O.run(sc, cfg)
+    prog, (t, h, hu, hv, v), state, led = run_device(sc, cfg)
+    assert prog.error == 0 and ref.error == 0
+    assert abs(prog.step_count - ref.step_count) <= max(2, ref.step_count // 500)
+    assert h.shape == ref.depth.shape == (3, 2 * n * n)
+    area = np.asarray(sc.city.topologies.surface_topology.cell_area_m2, np.float64)
+    valid = np.ones(h.shape[1], bool)
+    for k in range(h.shape[0]):
+        rmse, csi, verr = gates(h[k], ref.depth[k], area, valid)
+        assert rmse <= 1e-3 and csi >= 0.995 and abs(verr) <= 5e-4, (k, rmse, csi, verr)
+    np.testing.assert_allclose(led["rainfall_input_m3"], ref.ledger["rainfall_input_m3"], rtol=1e-4)
+
+
 def test_coupled_city_hour_gates_against_oracle():
     sc = coupled_test_city(scale=2, seed=3, duration_min=60.0)
     cfg = load_config(None, sc.overrides)
