@@ -36,6 +36,9 @@ for _p in (ROOT / "gpu-urban-flood-cupy-jax_gb300", ROOT / "oracle"):
 METRIC = "cell-steps/s, 1M-tri coupled SWE on 1 GB300"
 UNIT = "cell-steps/s"
 REFERENCE_PUBLISHED = 7.447e8  # reference CuPy, RTX PRO 4000 Blackwell, real 981,880-tri city (derived)
+# the reference arm's sample: adaptive steps continued from the state half
+# way through the run (step 1,995 of 3,990), a wet mid-run state
+MID_RUN_STEP = 1995
 WORKLOAD = ("production-shaped coupled 60-min run: 981,880 triangles, 1,490,015 edges, 817,573 active, "
             "118,768 nodes, 139,798 links, 61,317 inlets, 46 outfalls, Horton infiltration, hour 1 of a "
             "160 mm/24 h front-loaded hyetograph")
@@ -49,7 +52,10 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true", help="skip the ensemble / surrogate screening measurement")
-    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--cpu-seconds", type=float, default=60.0,
+                   help="reference arm: CPU seconds spread over the timed samples")
+    p.add_argument("--mid-run-step", type=int, default=MID_RUN_STEP,
+                   help="reference arm: the step of the 60-min run its samples continue from")
     p.add_argument("--profile", choices=["loop", "kernels", "surrogate"], default=None,
                    help="ncu helper: open a profiler range around 64 solver steps of a wet run (loop) or "
                         "around 2 isolated launches of each step kernel (kernels); prints nothing else")
@@ -145,38 +151,78 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch():
-    """Per-launch DRAM bytes of k_surface from the committed ncu summary, if any."""
-
-    p = ROOT / "profiles" / "k_surface_production.txt"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+# DRAM traffic of one k_surface launch (dram__bytes_read.sum + dram__bytes_write.sum)
+# from an ncu capture, keyed by the digest of the sources the kernel is built
+# from; a kernel whose sources changed since its capture reports null.
+SURFACE_SOURCES = ("fl_surface.cu", "fl_device.cuh", "fl_internal.h")
+SURFACE_TRAFFIC_CAPTURES = {}
 
 
-def cpu_baseline(sc, cfg, seconds: float):
+def surface_source_digest() -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for name in SURFACE_SOURCES:
+        h.update((ROOT / "gpu-urban-flood-cupy-jax_gb300" / "csrc" / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def surface_traffic_per_launch():
+    return SURFACE_TRAFFIC_CAPTURES.get(surface_source_digest())
+
+
+def workload_config(world: int, surface_mode: str = "full_swe") -> dict:
+    """The workload both arms measure (identical in both JSON lines)."""
+
+    return {
+        "workload": WORKLOAD, "cells": 981_880, "edges": 1_490_015,
+        "step": "one 60-min simulated run (adaptive dt, CFL every 32 steps)",
+        "surface_step_mode": surface_mode,
+        "l2": "flushed before every run (512 MB write); state reset outside the events",
+        "parallelism": f"replicas x{world}",
+    }
+
+
+def cpu_baseline_and_parity(sc, cfg, gpu):
+    """The C oracle (all host threads) runs the whole 60-minute workload; its
+    wall time is the CPU baseline and its hourly snapshots and final drainage
+    state are this line's parity reference for the GPU run ``gpu`` (the
+    snapshots, final node volumes and link flows of the last timed run)."""
+
+    import numpy as np
+
     import oracle
+    from floodgb.parity import compare_runs
 
     oracle.build()
     c = sc.cell_count
     t0 = time.perf_counter()
-    oracle.run(sc, cfg, max_steps=2)
-    per_step = (time.perf_counter() - t0) / 2
-    steps = int(max(4, min(2000, seconds / max(per_step, 1e-6))))
-    t0 = time.perf_counter()
-    r = oracle.run(sc, cfg, max_steps=steps)
+    r = oracle.run(sc, cfg)
     wall = time.perf_counter() - t0
-    return {
+    base = {
         "value": c * r.step_count / wall, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-        "sample": f"first {r.step_count} adaptive steps of the same 60-min run from its initial state "
-                  f"({wall:.1f} s, C oracle, OpenMP)",
+        "sample": f"the whole 60-min run ({r.step_count} adaptive steps, {wall:.1f} s, C oracle, OpenMP); "
+                  f"the same run is this line's parity reference",
     }
+    topo = sc.city.topologies
+    mesh = sc.city.mesh
+    valid = np.asarray(mesh.active_mask, bool) & ~np.asarray(mesh.building_mask, bool)
+    area = np.asarray(topo.surface_topology.cell_area_m2, np.float64)
+    cmp = compare_runs(r.snapshot_times_s, r.depth, gpu["times"], gpu["depth"], valid, area,
+                       ref_node_volume=r.final_node_volume, cand_node_volume=gpu["node_volume"],
+                       ref_link_flow=r.final_link_flow, cand_link_flow=gpu["link_flow"])
+    parity = {
+        "reference": "C oracle (CPU restatement of the reference step), same seeded inputs, whole 60-min run",
+        "cells": c, "snapshot_times_s": [round(x["candidate_time_s"], 3) for x in cmp["snapshots"]],
+        "steps": {"gpu": gpu["steps"], "oracle": r.step_count},
+        "depth_rmse_m": [x["valid_depth_rmse_m"] for x in cmp["snapshots"]],
+        "csi_0_05m": [x["flood_extent_csi"] for x in cmp["snapshots"]],
+        "surface_volume_error": [x["surface_volume_error_fraction"] for x in cmp["snapshots"]],
+        "max_abs_depth_error_m": [x["max_absolute_error_m"] for x in cmp["snapshots"]],
+        "drainage_state": cmp["drainage_state"],
+        "gates": cmp["drop_in_gates"], "passed": cmp["passed"],
+    }
+    return base, parity
 
 
 def reference_arm(args):
@@ -191,21 +237,31 @@ def reference_arm(args):
     import oracle
 
     oracle.build()
+    c = sc.cell_count
+    mid = oracle.run(sc, cfg, max_steps=args.mid_run_step)  # untimed: the wet mid-run state
+    per_step = None
     per = []
-    base = None
+    n_steps = 8
     for i in range(args.warmup + args.steps):
-        secs = max(2.0, args.cpu_seconds / max(args.steps, 1)) if i >= args.warmup else 1.0
-        b = cpu_baseline(sc, cfg, secs)
+        if per_step is not None:
+            secs = max(2.0, args.cpu_seconds / max(args.steps, 1)) if i >= args.warmup else 1.0
+            n_steps = int(max(4, min(2000, secs / max(per_step, 1e-6))))
+        t0 = time.perf_counter()
+        r = oracle.run(sc, cfg, max_steps=n_steps, start=mid)
+        wall = time.perf_counter() - t0
+        per_step = wall / max(r.step_count, 1)
         if i >= args.warmup:
-            per.append(b["value"])
-            base = b
-    value = statistics.median(per)
-    base = dict(base, value=value)
+            per.append((c * r.step_count / wall, r.step_count, wall))
+    value = statistics.median(v for v, _, _ in per)
+    n, w = per[-1][1], per[-1][2]
+    sample = (f"{n} adaptive steps continued from step {mid.step_end} of the same 60-min run "
+              f"(t = {mid.t_end:.0f} s, wet mid-run state; {w:.1f} s per sample, C oracle, OpenMP)")
+    base = {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port", "sample": sample}
     print(json.dumps({
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": base["sample"]},
+        "config": workload_config(world),
         "cpu_baseline": base,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -214,53 +270,31 @@ def reference_arm(args):
 SURROGATE_WEIGHTS = ROOT / "gpu-urban-flood-cupy-jax_gb300" / "floodgb" / "surrogate" / "weights" / "mpnn_grid224.npz"
 
 
-def ensemble_measure(per_size: int = 4, cap_h: float = 1.0, screen_members: int = 512):
-    """Second metric, ensemble scenario-hours/s: a ragged 16-member ensemble
-    (4 each of 10,082 / 49,928 / 100,352 / 250,632-triangle meshes, seeded
-    storms, 1 h each) through the batched solver against the same members run
-    one by one by the single-instance solver; then, with the trained
-    surrogate, screening of held-out storms on its 100,352-triangle mesh
+def ensemble_measure(screen_members: int = 1024):
+    """Second metric, ensemble scenario-hours/s.  The ragged batched ensemble:
+    64 members, 16 each of 10,082 / 49,928 / 100,352 / 250,632-triangle
+    meshes, seeded storms of peak 20-120 mm/h over 1-6 h, each member run for
+    its storm's duration in one persistent launch per step, launch shape from
+    the autotuner; against the plain single-instance solver (two members per
+    mesh size timed, extrapolated per size).  Then, with the trained
+    surrogate, screening of the held-out storms on its 100,352-triangle mesh
     (rollouts + solver re-runs of flagged and audited members) against the
     plain single-instance solver."""
 
-    import torch
+    from floodgb.batch import measure_ensemble
 
-    from floodgb.batch import BatchSolver
-    from floodgb.solver import solver_for_city
-    from floodgb.synthetic import ensemble_workload
-
-    members = ensemble_workload(seed=2, per_size=per_size, duration_cap_h=cap_h)
-    hours = sum(m.duration_s for m in members) / 3600.0
-    shape = {"tile_cells": 256, "ctas_per_sm": 0}
-    with BatchSolver(members, shape=shape) as b:
-        b.run(max_steps=64)
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        b.run()
-        torch.cuda.synchronize()
-        batched_s = time.perf_counter() - t
-        cell_steps = sum(b.progress(k).step_count * c for k, c in enumerate(b.cell_counts))
-        info = b.info()
-    seq_s = 0.0
-    for m in members:
-        s = solver_for_city(m.city, m.rainfall, m.cfg, duration_s=m.duration_s)
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        s.run()
-        torch.cuda.synchronize()
-        seq_s += time.perf_counter() - t
-        s.close()
+    e = measure_ensemble(per_size=16, duration_cap_h=None, sequential_per_size=2, tune_shape=True)
     out = {
-        "metric": "scenario-h/s", "workload": f"{len(members)} members, 4 mesh sizes, seeded storms, {cap_h:g} h each",
-        "batched": hours / batched_s, "sequential_single_instance": hours / seq_s,
-        "batched_over_single": seq_s / batched_s, "batched_cell_steps_per_s": cell_steps / batched_s,
-        "batch_shape": {k: info[k] for k in ("tile_cells", "ctas_per_sm", "grid", "tiles")},
+        "metric": "scenario-h/s",
+        "workload": f"{e['members']} members (16 each of 10,082 / 49,928 / 100,352 / 250,632 triangles), "
+                    f"seeded storms of 1-6 h, {e['scenario_hours']:.1f} scenario-hours",
+        "batched": e["batched_scenario_h_per_s"], "sequential_single_instance": e["single_instance_scenario_h_per_s"],
+        "batched_over_single": e["batched_over_single"], "batched_cell_steps_per_s": e["batched_cell_steps_per_s"],
+        "batch_shape": dict(e["shape"], source="autotuner"), "single_instance_sample": e["single_instance_sample"],
     }
     if SURROGATE_WEIGHTS.exists():
         from floodgb.surrogate.experiment import screen_saved
 
-        # the accuracy is judged on the solver re-runs (flagged + 5 % audit);
-        # the full-ensemble scoring lives in profiles/surrogate_screening_100k.md
         r = screen_saved(SURROGATE_WEIGHTS, n_eval=screen_members, plain_sample=2, score_all=False)
         out["surrogate_screening"] = {
             "members": r["members"], "mesh_cells": r["mesh_cells"], "scenario_hours": r["scenario_hours"],
@@ -367,6 +401,9 @@ def our_arm(args):
         out_h.numpy()[:] = final[0]
         e2e_s.append(time.perf_counter() - t0)
         n_snap = len(snaps[0])
+    # the last run's hourly snapshots and final drainage state: the parity candidate
+    gpu_run = {"times": snaps[0], "depth": snaps[1], "node_volume": final[3], "link_flow": final[4],
+               "steps": solver.progress(stream=stream).step_count}
     e2e_value = float(C) * float(steps[-1]) * len(e2e_s) / sum(e2e_s)
     h2d = C * 12 + Nn * 8 + L * 8
     d2h = n_snap * (C * 12 + Nn * 4 + 8) + C * 12 + Nn * 8 + L * 8
@@ -388,9 +425,9 @@ def our_arm(args):
 
     if rank != 0:
         return
-    base = None
+    base = parity = None
     if world == 1 and not args.no_cpu_baseline:
-        base = cpu_baseline(sc, cfg, args.cpu_seconds)
+        base, parity = cpu_baseline_and_parity(sc, cfg, gpu_run)
     ensemble = None
     if world == 1 and not args.no_ensemble:
         ensemble = ensemble_measure()
@@ -398,28 +435,27 @@ def our_arm(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / len(ms), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / REFERENCE_PUBLISHED, "dtype": "f32", "data": "synthetic",
-        "config": {
-            "workload": WORKLOAD, "cells": C, "edges": E, "solver_steps_per_run": steps[-1],
-            "step": "one 60-min simulated run (adaptive dt, CFL every 32 steps)",
-            "surface_step_mode": args.surface_mode,
-            "l2": "flushed before every run (512 MB write); state reset outside the events",
-            "parallelism": f"replicas x{world}",
+        "config": workload_config(world, args.surface_mode),
+        "detail": {
+            "cells": C, "edges": E, "nodes": Nn, "links": L, "solver_steps_per_run": steps[-1],
             "vs_baseline_ref": "7.447e8 cell-steps/s: reference CuPy on RTX PRO 4000, real 981,880-tri city",
             "algorithmic_bytes_per_solver_step": alg_step,
-            "kernel_ms": {"k_surface": surf_ms, "k_nodes": inlet_ms, "k_links": link_ms, "k_donor": donor_ms, "k_network": net_ms,
-                          "k_dt": dt_ms},
+            "whole_step_hbm_frac": alg_step / (total_ms / len(ms) / steps[-1] * 1e-3) / 1e9 / peak,
+            "kernel_ms": {"k_surface": surf_ms, "k_nodes": inlet_ms, "k_links": link_ms, "k_donor": donor_ms,
+                          "k_network": net_ms, "k_dt": dt_ms},
             "solver_step_us": total_ms / len(ms) / steps[-1] * 1000.0,
             "wall_s_timed_region": wall,
         },
         "roofline": {
             "bound": "hbm", "kernel": "k_surface", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": ncu_traffic_per_launch(),
-            "algorithmic_bytes_per_launch": alg_surface,
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": surface_traffic_per_launch(),
+            "algorithmic_bytes_per_launch": alg_surface, "kernel_source_digest": surface_source_digest(),
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "clocks": clk,
         "cpu_baseline": base,
+        "parity": parity,
         "ensemble": ensemble,
     }
     print(json.dumps(line), flush=True)

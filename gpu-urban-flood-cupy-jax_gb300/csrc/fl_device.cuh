@@ -230,7 +230,10 @@ __device__ __forceinline__ void clamp_velocity_exact(float h, float &hu, float &
 // CFL local timestep of one cell (equations.py:155-178), correctly rounded
 // and uncontracted: the reference's float32 expression bit-for-bit.
 __device__ __forceinline__ float cfl_local(float h, float hu, float hv, float char_len, float cfl, float g, float md) {
-    const float hs = fmax32(h, md);
+    // NumPy's maximum passes a NaN depth through, so such a cell's local dt is
+    // NaN and the caller's isfinite test drops it (the solver's own state
+    // never holds a NaN depth: the cell update clips it to zero)
+    const float hs = isnan(h) ? h : fmax32(h, md);
     const float u = xdiv(hu, hs), w = xdiv(hv, hs);
     const float speed = xadd(xsqrt(xadd(xmul(u, u), xmul(w, w))), xsqrt(xmul(g, hs)));
     return xdiv(xmul(cfl, char_len), fmax32(speed, 1.0e-12f));

@@ -30,17 +30,15 @@ constexpr int64_t NOALLOC_MAX_CELLS = (int64_t)NOALLOC_MAX_BLOCKS * NOALLOC_CELL
 // [0]: number of blocks done; [1 + b]: bit pattern of block b's minimum.  16 KB.
 static __device__ __align__(256) unsigned int g_cfl_scratch[1 + NOALLOC_MAX_BLOCKS];
 
-// Same float32 expression as the reference's stable_timestep_s
-// (equations.py:155-178), correctly rounded and uncontracted.
+// The CFL expression of the solver's own reduction (cfl_local, the
+// reference's stable_timestep_s of equations.py:155-178 in float32, correctly
+// rounded and uncontracted); cells whose local dt is not finite are skipped.
 __global__ void __launch_bounds__(NOALLOC_THREADS) k_dt_noalloc(const float *cl, const float *h, const float *hu,
                                                                 const float *hv, int32_t n, float cfl, float g,
                                                                 float md, unsigned int *scratch, double *dt_out) {
     float best = CUDART_INF_F;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float hs = fmax32(h[i], md);
-        const float u = __fdiv_rn(hu[i], hs), w = __fdiv_rn(hv[i], hs);
-        const float speed = __fadd_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(u, u), __fmul_rn(w, w))), __fsqrt_rn(__fmul_rn(g, hs)));
-        const float local = __fdiv_rn(__fmul_rn(cfl, cl[i]), fmax32(speed, 1.0e-12f));
+        const float local = cfl_local(h[i], hu[i], hv[i], cl[i], cfl, g, md);
         if (isfinite(local) && local < best) best = local;
     }
 #pragma unroll

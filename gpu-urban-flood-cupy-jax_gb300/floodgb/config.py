@@ -1,9 +1,10 @@
 """Run configuration with the reference's section and key names.
 
-Sections and defaults follow ``gurugram_flood/config.py:84-119`` (``SolverConfig``,
-``PhysicsConfig``) and the loader follows ``load_config`` (``:180-221``): a YAML
-or JSON mapping of sections plus dotted ``section.key`` overrides, with an
-error for any unknown section or key.  PyYAML is optional: ``.json`` files and
+Sections and defaults follow ``gurugram_flood/config.py:39-165``
+(``PathsConfig``, ``TopologyConfig``, ``SolverConfig``, ``PhysicsConfig``,
+``OutputsConfig``) and the loader follows ``load_config`` (``:180-221``): a
+YAML or JSON mapping of sections plus dotted ``section.key`` overrides, with
+an error for any unknown section or key.  PyYAML is optional: ``.json`` files and
 plain dicts always work, ``.yaml`` files need PyYAML.
 """
 
@@ -11,11 +12,38 @@ from __future__ import annotations
 
 import dataclasses
 import json
+import os
 from dataclasses import dataclass, field
 from pathlib import Path
 from typing import Any, Mapping
 
 from .exceptions import ConfigError
+
+
+@dataclass
+class PathsConfig:
+    """Locations of the reference's static city datasets (``config.py:39-71``).
+
+    Kept for configuration and report compatibility: this library takes its
+    inputs from the caller (``floodgb.domain`` reads the production topology
+    NPZ given its path), so nothing here is opened by the solver."""
+
+    data_dir: str = os.environ.get("GURUGRAM_FLOOD_DATA_DIR", str(Path("data") / "production_gurugram"))
+    production_topology_npz: str = "production_topology/d_june5_exact_production_topology_and_mesh.npz"
+    horton_bcr_npz: str = "production_topology/horton_bcr_fields.npz"
+    recharge_csv: str = "drainage_june5/recharge/surface_recharge_exchange_table.csv"
+    external_boundary_inflow_csv: str = (
+        "external_boundary_inflow/gurugram_external_boundary_inflow_july2025_133mm_12h.csv")
+    mesh_npz: str = "mesh/citywide_anuga_mesh_arrays.npz"
+    dem_tif: str = "terrain/hydraulic_dtm_fabdem_5m.tif"
+    drain_capacities_geojson: str = "drainage/best_guess_drain_capacities.geojson"
+    outfall_inventory_geojson: str = "drainage/outfall_inventory.geojson"
+    tailwater_priors_csv: str = "pragmatic_priors/outfall_tailwater_priors.csv"
+
+    def resolve(self, name: str) -> Path:
+        """A configured entry resolved against ``data_dir`` (absolute paths kept)."""
+        raw = Path(getattr(self, name))
+        return raw if raw.is_absolute() else Path(self.data_dir) / raw
 
 
 @dataclass
@@ -68,13 +96,18 @@ class OutputsConfig:
     wet_threshold_m: float = 0.05
     geojson_threshold_m: float = 0.05
     write_npz: bool = True
+    # GeoJSON, basemap and PNG writers are outside this library (off by default)
     write_hourly_geojson: bool = False
     write_basemap_html: bool = False
     write_timeseries_png: bool = False
+    basemap_max_features: int = 120_000
+    basemap_color_max_m: float = 3.0
+    mesh_crs: str = "EPSG:32643"
 
 
 @dataclass
 class RunConfig:
+    paths: PathsConfig = field(default_factory=PathsConfig)
     topology: TopologyConfig = field(default_factory=TopologyConfig)
     solver: SolverConfig = field(default_factory=SolverConfig)
     physics: PhysicsConfig = field(default_factory=PhysicsConfig)
@@ -148,8 +181,6 @@ def load_config(
         raise ConfigError("Config must be a mapping of sections")
     sections = {f.name: getattr(cfg, f.name) for f in dataclasses.fields(cfg)}
     for section_name, values in loaded.items():
-        if section_name == "paths":
-            continue  # data paths are not used: inputs come from the caller
         if section_name not in sections:
             raise ConfigError(f"Unknown config section '{section_name}'")
         if values is None:

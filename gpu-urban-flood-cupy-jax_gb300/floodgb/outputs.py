@@ -91,9 +91,21 @@ def build_report(result, artifacts: dict | None = None) -> dict:
     }
 
 
-def write_report(result, out_dir, artifacts: dict | None = None) -> Path:
+def write_report(result, out_dir, artifacts: dict | None = None, topology_path=None) -> Path:
+    """Write ``run_report.json``.  With ``topology_path`` (the production
+    topology NPZ the run was built from, holding ``surface_cell_area_m2``) the
+    report also carries what the reference's parity validator reads from a
+    candidate run (parity_validation.py:84-88, 163-165): the topology path
+    under ``input_report`` and the mass residual ratio under
+    ``v1_compatible_mass_residual_ratio`` (this library's ledger is the V1
+    ledger, engine.py:364-382)."""
+
+    report = build_report(result, artifacts)
+    if topology_path is not None:
+        report["input_report"] = {"assets": {"assets": {"topology": {"path": str(Path(topology_path).resolve())}}}}
+        report["v1_compatible_mass_residual_ratio"] = float(result.mass_balance["mass_residual_ratio"])
     path = Path(out_dir) / REPORT_NAME
     tmp = path.with_suffix(".json.partial")
-    tmp.write_text(json.dumps(build_report(result, artifacts), indent=2, sort_keys=True), encoding="utf-8")
+    tmp.write_text(json.dumps(report, indent=2, sort_keys=True), encoding="utf-8")
     tmp.replace(path)
     return path

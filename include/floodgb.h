@@ -273,19 +273,24 @@ FL_API int fl_plan_tiles(const FlMeshDesc *mesh, int64_t *tiles);
  * No reference counterpart: it is the measurement hook for the roofline. */
 FL_API int fl_time_kernel(FlSolver *solver, int32_t kernel, int32_t reps, void *stream, double *ms_per_launch);
 
-/* Allocation-free CFL timestep, for callers that may not allocate device
- * memory at this point (a plugin limited to its host application's memory
- * pool, code running while another library captures the stream into a CUDA
- * graph, a service that forbids allocation after start-up).  No counterpart
- * in the reference: it is the same reduction as fl_stable_timestep (the
- * reference's stable_timestep_s, equations.py:155-178) over caller-owned
- * device arrays in any cell order, writing the minimum dt (or -1.0 when no
- * cell gives a finite dt) to the device double *dt_out, asynchronously on
- * `stream`.  It allocates nothing: its scratch is a 16 KB static device
- * array that every GPU loading the library keeps until exit; the first call
- * on a device looks up that array's address (make it before any stream
- * capture).  At most 8,388,608 cells per call (FL_E_INVALID beyond).  All
- * calls share the one array, so calls that overlap on the GPU race. */
+/* Allocation-free CFL timestep.  It has no counterpart in the reference.  It
+ * is for callers that may not allocate device memory at this point: a plugin
+ * limited to its host application's memory pool, code running while another
+ * library captures the stream into a CUDA graph, a service that forbids
+ * allocation after start-up.  Over caller-owned device arrays in any cell
+ * order it computes the minimum over cells of
+ *   cfl * char_len / max(|(hu, hv)| / max(h, min_depth) + sqrt(g * max(h, min_depth)), 1e-12)
+ * in float32 with correctly rounded operations (the same reduction as
+ * fl_stable_timestep; cells whose value is not finite, e.g. a NaN depth, are
+ * skipped), writing it to the device double *dt_out (-1.0 when no cell gives
+ * a finite value), asynchronously on `stream`.  It allocates nothing: its
+ * scratch is a 16 KB static device array that every GPU loading the library
+ * keeps until exit.  The first call on a device looks up that array's
+ * address and caches it (make that call before any stream capture; a
+ * cudaDeviceReset after it is not supported, as the cached address would then
+ * be stale).  At most 8,388,608 cells per call (FL_E_INVALID beyond).  All
+ * calls share the one array, so calls that overlap on the GPU race; calls
+ * ordered on one stream are safe. */
 FL_API int fl_stable_timestep_noalloc(const float *char_len, const float *h, const float *hu, const float *hv,
                                       int32_t n, double cfl, double gravity_mps2, double min_depth_m,
                                       double *dt_out, void *stream);

@@ -691,8 +691,9 @@ int orc_run(const OrcMesh *m, const OrcDrain *d, const OrcRunParams *p, float *h
     float *infil = (float *)malloc(sizeof(float) * (size_t)C);
     if (!h2 || !hu2 || !hv2 || !rain || !infil) return -1;
     memset(out, 0, sizeof(*out));
-    double t = 0.0, cached = -1.0, next_snap = 0.0;
-    int64_t step = 0;
+    double t = p->t_start_s, cached = p->step_start > 0 ? p->cached_dt_s : -1.0;
+    double next_snap = p->next_snapshot_s;
+    int64_t step = p->step_start;
     const double T = p->duration_s;
     int rc = 0;
     while (t < T) {
@@ -766,8 +767,10 @@ int orc_run(const OrcMesh *m, const OrcDrain *d, const OrcRunParams *p, float *h
             next_snap += p->snapshot_interval_s;
         }
     }
-    out->step_count = step;
+    out->step_count = step - p->step_start;
     out->t_end = t;
+    out->cached_dt_s = cached;
+    out->next_snapshot_s = next_snap;
     free(h2); free(hu2); free(hv2); free(rain); free(infil);
     return rc;
 }

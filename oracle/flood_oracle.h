@@ -146,6 +146,14 @@ typedef struct {
     const OrcRecharge *recharge; /* nullable: applied after the drainage step */
     float *recharge_storage;     /* [row_count], in/out (with recharge) */
     int32_t local_inertial;      /* 1: surface_step_mode = local_inertial */
+    /* resume point (all zero for a run from t = 0): simulated time and step
+     * count reached, the cached CFL dt of that point (< 0: none) and the
+     * time of the next snapshot.  A run resumed from the values an earlier
+     * run returned continues it step for step. */
+    double t_start_s;
+    int64_t step_start;
+    double cached_dt_s;
+    double next_snapshot_s;
 } OrcRunParams;
 
 typedef struct {
@@ -155,6 +163,8 @@ typedef struct {
     double t_end;
     double ledger[12]; /* rain, infil, bnet, outfall, overflow, unreturned, capture, surcharge, link_abs,
                           external inflow, recharge capture, recharge loss */
+    double cached_dt_s;     /* the CFL dt the next reuse step scales (< 0: none) */
+    double next_snapshot_s; /* the snapshot time the loop waits for next */
 } OrcRunResult;
 
 /* state arrays are updated in place; snapshots: max_snapshots x C (h, hu, hv) and x N (volume f32) */

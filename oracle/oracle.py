@@ -123,6 +123,8 @@ class OrcRunParams(C.Structure):
         ("max_snapshots", C.c_int32),
         ("inflow", C.POINTER(OrcInflow)), ("recharge", C.POINTER(OrcRecharge)), ("recharge_storage", f32p),
         ("local_inertial", C.c_int32),
+        ("t_start_s", C.c_double), ("step_start", C.c_int64), ("cached_dt_s", C.c_double),
+        ("next_snapshot_s", C.c_double),
     ]
 
 
@@ -132,6 +134,7 @@ class OrcRunResult(C.Structure):
         ("snapshot_count", C.c_int32), ("error", C.c_int32),
         ("error_step", C.c_int64), ("t_end", C.c_double),
         ("ledger", C.c_double * 12),
+        ("cached_dt_s", C.c_double), ("next_snapshot_s", C.c_double),
     ]
 
 
@@ -408,10 +411,21 @@ class OracleRun:
     error: int
     error_step: int
     recharge_storage: np.ndarray | None = None
+    # where the run stopped, for run(..., start=this): absolute step count,
+    # the cached CFL dt and the next snapshot time
+    step_end: int = 0
+    cached_dt_s: float = -1.0
+    next_snapshot_s: float = 0.0
 
 
-def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None) -> OracleRun:
-    """Restated engine loop (engine.py:219-344) on the oracle step functions."""
+def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None,
+        start: OracleRun | None = None) -> OracleRun:
+    """Restated engine loop (engine.py:219-344) on the oracle step functions.
+
+    With ``start`` (the result of an earlier run of the same scenario and
+    config, stopped by ``max_steps``) the loop continues from that run's final
+    state, simulated time, step count, cached CFL dt and snapshot schedule;
+    ``step_count``, snapshots and ledger then cover the resumed part only."""
 
     from floodgb.config import load_config
     from floodgb.rainfall import hyetograph_arrays
@@ -449,6 +463,11 @@ def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None
         has_drainage=1 if has_drain else 0, max_steps=int(max_steps), max_snapshots=n_snap,
         local_inertial=1 if s.surface_step_mode == "local_inertial" else 0,
     )
+    if start is not None:
+        p.t_start_s = start.t_end
+        p.step_start = start.step_end
+        p.cached_dt_s = start.cached_dt_s
+        p.next_snapshot_s = start.next_snapshot_s
     ext = getattr(city, "external_boundary", None)
     rch = getattr(city, "recharge_topology", None)
     rstore = None
@@ -464,12 +483,20 @@ def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None
         p.recharge_storage = _p(rstore, C.c_float)
     n = st.cell_count
     nn = topo.coupling_topology.node_count
-    h = np.array(topo.surface_state.h_m, np.float32)
-    hu = np.array(topo.surface_state.hu_m2ps, np.float32)
-    hv = np.array(topo.surface_state.hv_m2ps, np.float32)
-    V = np.array(topo.pipe_state.node_volume_m3, np.float64)
-    Q = np.array(topo.pipe_state.link_flow_m3ps, np.float64)
-    wt = np.zeros(n, np.float32)
+    if start is None:
+        h = np.array(topo.surface_state.h_m, np.float32)
+        hu = np.array(topo.surface_state.hu_m2ps, np.float32)
+        hv = np.array(topo.surface_state.hv_m2ps, np.float32)
+        V = np.array(topo.pipe_state.node_volume_m3, np.float64)
+        Q = np.array(topo.pipe_state.link_flow_m3ps, np.float64)
+        wt = np.zeros(n, np.float32)
+    else:
+        h, hu, hv = (np.array(a, np.float32) for a in (start.final_h, start.final_hu, start.final_hv))
+        V = np.array(start.final_node_volume, np.float64)
+        Q = np.array(start.final_link_flow, np.float64)
+        wt = np.array(start.wet_time, np.float32)
+        if rstore is not None and start.recharge_storage is not None:
+            rstore[:] = start.recharge_storage
     st_t = np.zeros(n_snap, np.float64)
     sh = np.zeros((n_snap, n), np.float32)
     shu = np.zeros((n_snap, n), np.float32)
@@ -492,6 +519,8 @@ def run(scenario, cfg=None, max_steps: int = 0, max_snapshots: int | None = None
         node_volume=sv[:k, :nn].copy(), final_h=h, final_hu=hu, final_hv=hv, final_node_volume=V,
         final_link_flow=Q, wet_time=wt, ledger=dict(zip(names, list(res.ledger))), error=res.error,
         error_step=res.error_step, recharge_storage=rstore,
+        step_end=(start.step_end if start is not None else 0) + res.step_count,
+        cached_dt_s=res.cached_dt_s, next_snapshot_s=res.next_snapshot_s,
     )
 
 

@@ -2,7 +2,9 @@
 
 Run from the repository root in a container that has the reference checkout:
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py <reference checkout> [--only=surface,pipe,run,forcing,li,topology,outputs]
+
+(or with the checkout in $FLOODGB_REFERENCE).
 
 The reference package ``gurugram_flood`` cannot be imported normally here
 (its ``__init__`` needs PyYAML and its engine needs pandas), so bare package
@@ -584,15 +586,293 @@ def make_forcing_cases(tb, stab, pis, pes, j5):
     np.savez_compressed(OUT / "forcing_cases.npz", **out)
 
 
+def make_topology_cases(tb):
+    """Reference topology builds (build_triangular_surface_topology,
+    triangular_backend.py:244-326, with _orient_triangles_ccw / _build_edges
+    :1815-1869) on irregular meshes: seeded Delaunay triangulations with about
+    half of the triangles listed clockwise, jittered grids, every boundary
+    mode and some of its aliases (boundary_mode_code, :1050-1064), per-cell /
+    scalar / default Manning n, with and without an active mask; and the
+    ValueError text of each invalid input the builder rejects."""
+
+    from scipy.spatial import Delaunay
+
+    from floodgb.synthetic import grid_mesh
+
+    rng = np.random.default_rng(20261204)
+    out = {}
+
+    def delaunay(npts, size):
+        pts = np.vstack([rng.uniform(0.0, size, (npts, 2)), [[0, 0], [size, 0], [0, size], [size, size]]])
+        tri = Delaunay(pts).simplices.astype(np.int64)
+        flip = rng.random(len(tri)) < 0.5
+        tri[flip] = tri[flip][:, [0, 2, 1]]
+        return pts, tri
+
+    def grid(n, size):
+        pts, tri = grid_mesh(n, size, 0.2, rng)
+        tri = np.asarray(tri, np.int64).copy()
+        flip = rng.random(len(tri)) < 0.3
+        tri[flip] = tri[flip][:, [1, 0, 2]]
+        return pts, tri
+
+    cases = [
+        ("delaunay_outflow", delaunay(300, 400.0), "outflow", "cell", True),
+        ("delaunay_closed_default_n", delaunay(200, 150.0), "closed", "none", True),
+        ("delaunay_stage_scalar_n", delaunay(250, 900.0), "Dirichlet-Stage", "scalar", False),
+        ("grid_reflective", grid(11, 110.0), "reflective", "cell", True),
+        ("grid_open_alias", grid(9, 45.0), "open", "cell", True),
+        ("grid_wall_alias", grid(7, 700.0), "wall", "scalar", False),
+        ("grid_outflow_only_alias", grid(8, 80.0), "outflow_only", "cell", True),
+    ]
+    names = []
+    for name, (pts, tri), mode, mkind, with_active in cases:
+        c = len(tri)
+        bed = (rng.normal(10.0, 2.0, c)).astype(np.float32)
+        manning = {"cell": rng.choice([0.015, 0.035, 0.06, 0.1], c).astype(np.float32), "none": None,
+                   "scalar": 0.021}[mkind]
+        active = (rng.random(c) < 0.8).astype(np.float32) if with_active else None
+        st = tb.build_triangular_surface_topology(pts, tri, bed, manning, active, mode)
+        p = f"{name}/"
+        out[p + "nodes"], out[p + "triangles"], out[p + "in_bed"] = pts, tri, bed
+        out[p + "mode"] = np.array(mode)
+        out[p + "manning_kind"] = np.array(mkind)
+        out[p + "in_manning"] = np.asarray(manning if manning is not None else np.nan, np.float64 if mkind != "cell"
+                                           else np.float32)
+        out[p + "in_active"] = active if active is not None else np.zeros(0, np.float32)
+        out.update(topo_arrays(p + "out/", st))
+        names.append(name)
+    out["cases"] = np.array(names)
+
+    # invalid inputs and the reference's error text
+    pts, tri = delaunay(30, 10.0)
+    bed = np.zeros(len(tri), np.float32)
+    degenerate_pts = np.vstack([pts, [[20.0, 20.0], [21.0, 21.0], [22.0, 22.0]]])
+    k = len(pts)
+    nonmanifold_pts = np.vstack([pts, [[50.0, 0.0], [51.0, 0.0], [50.5, 1.0], [50.5, -1.0], [50.5, 2.0]]])
+    bad = {
+        "nodes_shape": (pts[:, :1], tri, bed, None, None, "closed"),
+        "triangles_shape": (pts, tri[:, :2], bed, None, None, "closed"),
+        "bed_length": (pts, tri, bed[:-1], None, None, "closed"),
+        "node_index_range": (pts, np.vstack([tri, [[0, 1, k + 5]]]), np.zeros(len(tri) + 1, np.float32), None, None,
+                             "closed"),
+        "degenerate": (degenerate_pts, np.vstack([tri, [[k, k + 1, k + 2]]]), np.zeros(len(tri) + 1, np.float32),
+                       None, None, "closed"),
+        "nonmanifold": (nonmanifold_pts, np.vstack([tri, [[k, k + 1, k + 2], [k, k + 1, k + 3], [k, k + 1, k + 4]]]),
+                        np.zeros(len(tri) + 3, np.float32), None, None, "closed"),
+        "manning_length": (pts, tri, bed, np.full(len(tri) - 1, 0.03, np.float32), None, "closed"),
+        "active_length": (pts, tri, bed, None, np.ones(len(tri) + 2, np.float32), "closed"),
+        "unsupported_mode": (pts, tri, bed, None, None, "sticky"),
+    }
+    err_names = []
+    for name, args in bad.items():
+        try:
+            tb.build_triangular_surface_topology(*args)
+        except ValueError as e:
+            msg = str(e)
+        else:
+            raise AssertionError(f"reference accepted invalid input {name}")
+        p = f"err/{name}/"
+        nodes, tris, b, man, act, mode = args
+        out[p + "nodes"], out[p + "triangles"], out[p + "bed"] = nodes, tris, b
+        out[p + "manning"] = man if man is not None else np.zeros(0, np.float32)
+        out[p + "active"] = act if act is not None else np.zeros(0, np.float32)
+        out[p + "mode"] = np.array(mode)
+        out[p + "message"] = np.array(msg)
+        err_names.append(name)
+    out["errors"] = np.array(err_names)
+    np.savez_compressed(OUT / "topology_cases.npz", **out)
+    return names + err_names
+
+
+def import_reference_outputs():
+    """The reference's output writer (postprocessing/outputs.py), its engine's
+    SimulationResult (solver/engine.py:68-105) and RunConfig (config.py), and
+    its parity validator (hybrid_flood/operational/parity_validation.py).
+    Their package ``__init__``s are bypassed like the kernels'; PyYAML (read by
+    config.load_config only) and pandas (CSV loaders only) get empty
+    stand-ins."""
+
+    src = sys.modules["gurugram_flood"].__path__[0]
+    hf = str(Path(src).parent / "hybrid_flood")
+    for name, path in (("gurugram_flood.postprocessing", str(Path(src) / "postprocessing")),
+                       ("hybrid_flood", hf), ("hybrid_flood.operational", str(Path(hf) / "operational"))):
+        mod = types.ModuleType(name)
+        mod.__path__ = [path]
+        sys.modules[name] = mod
+    sys.modules.setdefault("pandas", types.ModuleType("pandas"))
+    sys.modules.setdefault("yaml", types.ModuleType("yaml"))
+    import gurugram_flood.config as rcfg
+    import gurugram_flood.postprocessing.outputs as routs
+    import gurugram_flood.solver.engine as reng
+    import hybrid_flood.operational.parity_validation as rpv
+
+    return rcfg, reng, routs, rpv
+
+
+def output_result_arrays(tb, stab, pis, rng):
+    """A short coupled reference run (the restated engine loop) as the arrays
+    of a SimulationResult; the candidate is the same run with seeded depth
+    perturbations (some cells cross the 0.05 m threshold)."""
+
+    import json as _json
+
+    sc = tiny_coupled(seed=13)
+    st = sc.city.topologies.surface_topology
+    h0 = np.where(np.asarray(st.active_mask) > 0.5, rng.uniform(0.0, 0.12, st.cell_count), 0).astype(np.float32)
+    sc.city.topologies.surface_state = tb.TriangularSurfaceState(h0, np.zeros_like(h0), np.zeros_like(h0))
+    sc.overrides["solver.duration_min"] = 2.0
+    res = reference_run(tb, stab, pis, sc, max_steps=10_000, snapshot_interval_s=30.0)
+    mesh = sc.city.mesh
+    topo = sc.city.topologies
+    cp, pp = topo.coupling_topology, topo.pipe_topology
+    n_nodes = cp.node_count
+
+    def result_of(snap_h, snap_hu, snap_hv):
+        speed = np.zeros_like(snap_h)
+        wet = snap_h > 1.0e-4
+        speed[wet] = np.sqrt(snap_hu[wet] ** 2 + snap_hv[wet] ** 2) / snap_h[wet]
+        area = np.asarray(st.cell_area_m2, np.float64)
+        return {
+            "snapshot_times_min": np.asarray(res["snap_t"] / 60.0, np.float32),
+            "depth_snapshots_m": snap_h, "speed_snapshots_mps": speed,
+            "node_volume_snapshots_m3": np.asarray(res["snap_v"], np.float32),
+            "final_depth_m": snap_h[-1], "final_hu_m2ps": snap_hu[-1], "final_hv_m2ps": snap_hv[-1],
+            "final_node_volume_m3": np.asarray(res["final_V"], np.float32),
+            "final_link_flow_m3ps": np.asarray(res["final_Q"], np.float32),
+            "max_depth_m": np.max(snap_h, axis=0).astype(np.float32),
+            "max_speed_mps": np.max(speed, axis=0).astype(np.float32),
+            "mass_balance": {"rainfall_input_m3": float(res["ledger"][0]), "infiltration_loss_m3": float(res["ledger"][1]),
+                             "final_surface_volume_m3": float(np.sum(snap_h[-1].astype(np.float64) * area)),
+                             "mass_residual_m3": 0.25, "mass_residual_ratio": 1.5e-6},
+        }
+
+    ref = result_of(res["snap_h"], res["snap_hu"], res["snap_hv"])
+    pert = rng.normal(0.0, 2.0e-3, res["snap_h"].shape).astype(np.float32)
+    cand_h = np.maximum(res["snap_h"] + pert * (res["snap_h"] > 0), 0).astype(np.float32)
+    cand = result_of(cand_h, res["snap_hu"], res["snap_hv"])
+    cand["mass_balance"]["mass_residual_ratio"] = 2.0e-6
+    static = {
+        "mesh/nodes_xy": np.asarray(mesh.nodes_xy, np.float64), "mesh/triangles": np.asarray(mesh.triangles, np.int64),
+        "mesh/centroids_xy": np.asarray(mesh.centroids_xy, np.float64),
+        "mesh/terrain_elevation_m": np.asarray(mesh.terrain_elevation_m, np.float64),
+        "mesh/active_mask": np.asarray(mesh.active_mask, bool),
+        "mesh/building_mask": (rng.random(st.cell_count) < 0.05),
+        "mesh/road_mask": (rng.random(st.cell_count) < 0.2),
+        "cp/node_x_m": rng.uniform(0, 100, n_nodes), "cp/node_y_m": rng.uniform(0, 100, n_nodes),
+        "cp/node_count": np.int64(n_nodes), "cp/inlet_count": np.int64(cp.inlet_count),
+        "pp/link_from_node_index": np.asarray(pp.link_from_node_index, np.int64),
+        "pp/link_to_node_index": np.asarray(pp.link_to_node_index, np.int64), "pp/link_count": np.int64(pp.link_count),
+        "cell_area_m2": np.asarray(st.cell_area_m2, np.float64),
+    }
+    meta = {"step_count": int(res["step_count"]), "runtime_s": 1.25, "cfl_eval_count": 3, "cfl_reused_count": 90,
+            "backend_name": "numpy", "is_gpu": False, "duration_min": 2.0, "topology_mode": "exact_production",
+            "source_csv": "synthetic_storm.csv", "total_depth_mm": 42.5}
+    return ref, cand, static, _json.dumps(meta)
+
+
+def make_output_cases(tb, stab, pis):
+    """The reference writer's NPZ (save_run_npz, outputs.py:25-58) and report
+    (build_report, :61-99) for a short coupled run; and the reference's
+    validate_v1_parity_run (parity_validation.py:43-253) applied to that run
+    as the reference directory and, as the candidate directory, a
+    perturbed copy written by this library's floodgb.outputs."""
+
+    import json as _json
+    import tempfile
+    from types import SimpleNamespace
+
+    from floodgb import outputs as fout
+    from floodgb.config import load_config
+
+    rcfg, reng, routs, rpv = import_reference_outputs()
+    rng = np.random.default_rng(20261205)
+    ref, cand, static, meta_json = output_result_arrays(tb, stab, pis, rng)
+    meta = _json.loads(meta_json)
+
+    def city_of():
+        mesh = SimpleNamespace(**{k.split("/", 1)[1]: v for k, v in static.items() if k.startswith("mesh/")})
+        cp = SimpleNamespace(node_x_m=static["cp/node_x_m"], node_y_m=static["cp/node_y_m"],
+                             node_count=int(static["cp/node_count"]), inlet_count=int(static["cp/inlet_count"]))
+        pp = SimpleNamespace(link_from_node_index=static["pp/link_from_node_index"],
+                             link_to_node_index=static["pp/link_to_node_index"], link_count=int(static["pp/link_count"]))
+        return SimpleNamespace(mesh=mesh, topologies=SimpleNamespace(coupling_topology=cp, pipe_topology=pp),
+                               topology_mode=meta["topology_mode"])
+
+    rain = SimpleNamespace(source_csv=meta["source_csv"], total_depth_mm=meta["total_depth_mm"])
+    keys = ("step_count", "runtime_s", "cfl_eval_count", "cfl_reused_count", "backend_name", "is_gpu", "duration_min")
+    cfg = rcfg.RunConfig()
+    cfg.solver.duration_min = 2.0
+    rres = reng.SimulationResult(**ref, **{k: meta[k] for k in keys}, city=city_of(), rainfall=rain, config=cfg)
+    out = {"meta": np.array(meta_json)}
+    out.update({f"ref/{k}": v for k, v in ref.items() if k != "mass_balance"})
+    out.update({f"cand/{k}": v for k, v in cand.items() if k != "mass_balance"})
+    out["ref/mass_balance"] = np.array(_json.dumps(ref["mass_balance"]))
+    out["cand/mass_balance"] = np.array(_json.dumps(cand["mass_balance"]))
+    out.update({f"static/{k}": v for k, v in static.items()})
+    with tempfile.TemporaryDirectory() as tmp:
+        rdir, cdir = Path(tmp) / "reference", Path(tmp) / "candidate"
+        rdir.mkdir()
+        cdir.mkdir()
+        path = routs.save_run_npz(rres, rdir)
+        with np.load(path, allow_pickle=False) as z:
+            out["npz_names"] = np.array(sorted(z.files))
+            for name in z.files:
+                out[f"npz/{name}"] = z[name]
+        report = routs.build_report(rres, {"npz": str(path)})
+        out["report_json"] = np.array(_json.dumps(report, sort_keys=True))
+        routs.save_report(report, rdir)
+        # candidate: this library's writer (the reference validator reads it)
+        topo_npz = Path(tmp) / "topology.npz"
+        np.savez(topo_npz, surface_cell_area_m2=static["cell_area_m2"])
+        fcfg = load_config(None, {"solver.duration_min": 2.0})
+        cres = SimpleNamespace(**cand, **{k: meta[k] for k in keys}, city=city_of(), rainfall=rain, config=fcfg)
+        fout.save_run_npz(cres, cdir)
+        fout.write_report(cres, cdir, {"npz": "flood_simulation_outputs.npz"}, topology_path=topo_npz)
+        payload = rpv.validate_v1_parity_run(reference_dir=rdir, candidate_dir=cdir)
+        for k in ("reference_dir", "candidate_dir"):
+            payload.pop(k, None)
+        out["validation_json"] = np.array(_json.dumps(payload, sort_keys=True))
+    np.savez_compressed(OUT / "output_cases.npz", **out)
+    return sorted(payload["summary"])
+
+
+def reference_root() -> Path:
+    """The reference checkout: the first argument, else $FLOODGB_REFERENCE."""
+
+    import os
+
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else os.environ.get("FLOODGB_REFERENCE")
+    if not root:
+        raise SystemExit("usage: make_golden.py <reference checkout> [--only name,...] "
+                         "(or set FLOODGB_REFERENCE)")
+    return Path(root)
+
+
 def main():
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    ref = reference_root()
+    only = None
+    for a in sys.argv[1:]:
+        if a.startswith("--only="):
+            only = set(a.split("=", 1)[1].split(","))
+    want = lambda name: only is None or name in only  # noqa: E731
     tb, stab, pis = import_reference(ref)
-    pes, j5 = import_reference_forcing()
-    print("surface:", make_surface_cases(tb, stab))
-    print("pipe:", make_pipe_cases(tb))
-    make_run_cases(tb, stab, pis)
-    make_forcing_cases(tb, stab, pis, pes, j5)
-    print("local inertial:", make_li_cases(tb, stab, pis))
+    if want("surface"):
+        print("surface:", make_surface_cases(tb, stab))
+    if want("pipe"):
+        print("pipe:", make_pipe_cases(tb))
+    if want("run"):
+        make_run_cases(tb, stab, pis)
+    if want("forcing"):
+        pes, j5 = import_reference_forcing()
+        make_forcing_cases(tb, stab, pis, pes, j5)
+    if want("li"):
+        print("local inertial:", make_li_cases(tb, stab, pis))
+    if want("topology"):
+        print("topology:", make_topology_cases(tb))
+    if want("outputs"):
+        print("outputs:", make_output_cases(tb, stab, pis))
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

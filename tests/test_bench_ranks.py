@@ -78,7 +78,8 @@ def test_reference_arm_json_line():
 
     env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
-                        "--cpu-seconds", "1"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+                        "--cpu-seconds", "1", "--mid-run-step", "3"], cwd=ROOT, env=env, capture_output=True,
+                       text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "cell-steps/s" and line["value"] > 0
@@ -87,3 +88,9 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    # the same workload object as the GPU arm's line; the sample continues a run
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert line["config"] == bench.workload_config(1)
+    assert "continued from step 3 " in cb["sample"]

@@ -320,3 +320,29 @@ def test_bounded_device_wait_gives_up_and_reports():
     assert 0.19 <= el.value < 2.0
     native.check(native.load().fl_wait_selftest(0.05, C.byref(st), C.byref(el)), "fl_wait_selftest")
     assert st.value == native.FL_E_TIMEOUT
+
+
+def test_engine_outputs_have_reference_names_and_dtypes(tmp_path):
+    """run_simulation's result through floodgb.outputs: the NPZ array names,
+    dtypes and ranks and the report keys of the reference writer
+    (postprocessing/outputs.py:25-99, fixture written by it)."""
+
+    import json
+
+    from floodgb import outputs as fout
+    from floodgb.engine import run_simulation
+
+    ref = F.load("output_cases.npz")
+    sc = coupled_test_city(scale=1, seed=21, duration_min=3.0)
+    cfg = load_config(None, dict(sc.overrides, **{"solver.snapshot_interval_min": 1.0}))
+    res = run_simulation(sc.city, sc.rainfall, cfg)
+    path = fout.save_run_npz(res, tmp_path)
+    with np.load(path, allow_pickle=False) as z:
+        assert sorted(z.files) == [str(n) for n in ref["npz_names"]]
+        for name in z.files:
+            want = ref[f"npz/{name}"]
+            assert z[name].dtype == want.dtype and z[name].ndim == want.ndim, (name, z[name].dtype, want.dtype)
+        assert z["depth_snapshots_m"].shape == (len(z["snapshot_times_s"]), sc.cell_count)
+    rep = fout.build_report(res, {"npz": path.name})
+    assert set(rep) == set(json.loads(str(ref["report_json"])))
+    assert abs(rep["mass_residual_ratio"]) <= 1e-5
