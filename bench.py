@@ -216,7 +216,9 @@ def cpu_baseline_and_parity(sc, cfg, gpu):
         "cells": c, "snapshot_times_s": [round(x["candidate_time_s"], 3) for x in cmp["snapshots"]],
         "steps": {"gpu": gpu["steps"], "oracle": r.step_count},
         "depth_rmse_m": [x["valid_depth_rmse_m"] for x in cmp["snapshots"]],
-        "csi_0_05m": [x["flood_extent_csi"] for x in cmp["snapshots"]],
+        "csi_0_05m": [x["extent_agreement_csi"] for x in cmp["snapshots"]],
+        "wet_cells_0_05m": {"gpu": [x["candidate_wet_triangle_count"] for x in cmp["snapshots"]],
+                            "oracle": [x["reference_wet_triangle_count"] for x in cmp["snapshots"]]},
         "surface_volume_error": [x["surface_volume_error_fraction"] for x in cmp["snapshots"]],
         "max_abs_depth_error_m": [x["max_absolute_error_m"] for x in cmp["snapshots"]],
         "drainage_state": cmp["drainage_state"],

@@ -14,6 +14,12 @@ same scenario) as well as two written output directories.
 The gates are two sets: the reference's own V1-parity gates (:179-192, RMSE
 <= 0.05 m, CSI >= 0.95, volume <= 2 %) and the tighter drop-in gates this
 library is held to (RMSE <= 1e-3 m, CSI >= 0.995, volume <= 0.05 %).
+
+The reference scores a snapshot where neither run has a wet cell (an early
+snapshot of a dry start) as CSI 0 (intersection / max(union, 1)); the rows
+keep that figure, and the drop-in CSI gate reads ``extent_agreement_csi``,
+which counts two empty extents as agreeing (1.0) and equals the reference's
+CSI whenever anything is wet.
 """
 
 from __future__ import annotations
@@ -25,7 +31,7 @@ DEPTH_THRESHOLD_M = 0.05
 #: drop-in gates: (summary key, bound, "max" | "min")
 DROP_IN_GATES = {
     "depth_rmse_le_1mm": ("maximum_snapshot_valid_depth_rmse_m", 1.0e-3, "max"),
-    "csi_ge_0_995": ("minimum_snapshot_flood_extent_csi", 0.995, "min"),
+    "csi_ge_0_995": ("minimum_snapshot_extent_agreement_csi", 0.995, "min"),
     "volume_error_le_0_05pct": ("maximum_snapshot_surface_volume_error_fraction", 5.0e-4, "max"),
 }
 
@@ -55,6 +61,7 @@ def snapshot_row(ref_depth, cand_depth, valid, area, threshold_m: float = DEPTH_
         "depth_absolute_error_p99_m": float(np.percentile(np.abs(diff), 99)) if diff.size else 0.0,
         "max_absolute_error_m": float(np.max(np.abs(diff))) if diff.size else 0.0,
         "flood_extent_csi": float(inter.sum() / max(int(union.sum()), 1)),
+        "extent_agreement_csi": float(inter.sum() / union.sum()) if union.any() else 1.0,
         "reference_wet_triangle_count": int(ref_wet.sum()),
         "candidate_wet_triangle_count": int(cand_wet.sum()),
         "reference_surface_volume_m3": vr,
@@ -111,6 +118,7 @@ def compare_runs(ref_times, ref_depth, cand_times, cand_depth, valid, area, *, t
         "maximum_snapshot_time_delta_s": max((abs(r["time_delta_s"]) for r in rows), default=0.0),
         "maximum_snapshot_valid_depth_rmse_m": max((r["valid_depth_rmse_m"] for r in rows), default=0.0),
         "minimum_snapshot_flood_extent_csi": min((r["flood_extent_csi"] for r in rows), default=1.0),
+        "minimum_snapshot_extent_agreement_csi": min((r["extent_agreement_csi"] for r in rows), default=1.0),
         "maximum_snapshot_surface_volume_error_fraction": max(
             (abs(r["surface_volume_error_fraction"]) for r in rows), default=0.0),
         "maximum_snapshot_max_absolute_error_m": max((r["max_absolute_error_m"] for r in rows), default=0.0),
@@ -128,6 +136,8 @@ def compare_runs(ref_times, ref_depth, cand_times, cand_depth, valid, area, *, t
     for name, (key, bound, kind) in DROP_IN_GATES.items():
         drop_in[name] = summary[key] <= bound if kind == "max" else summary[key] >= bound
     drop_in["finite_non_negative_depth"] = finite
+    # passed: every drop-in gate and every reference gate but its CSI one, which
+    # the tighter drop-in CSI gate replaces (it differs only on all-dry snapshots)
+    passed = all(drop_in.values()) and all(v for k, v in reference_gates.items() if k != "all_snapshot_csi_ge_0_95")
     return {"threshold_m": threshold_m, "snapshots": rows, "drainage_state": drainage, "ledger_comparison": ledger,
-            "summary": summary, "reference_gates": reference_gates, "drop_in_gates": drop_in,
-            "passed": all(drop_in.values()) and all(reference_gates.values())}
+            "summary": summary, "reference_gates": reference_gates, "drop_in_gates": drop_in, "passed": passed}

@@ -742,16 +742,30 @@ def output_result_arrays(tb, stab, pis, rng):
             "final_link_flow_m3ps": np.asarray(res["final_Q"], np.float32),
             "max_depth_m": np.max(snap_h, axis=0).astype(np.float32),
             "max_speed_mps": np.max(speed, axis=0).astype(np.float32),
-            "mass_balance": {"rainfall_input_m3": float(res["ledger"][0]), "infiltration_loss_m3": float(res["ledger"][1]),
-                             "final_surface_volume_m3": float(np.sum(snap_h[-1].astype(np.float64) * area)),
-                             "mass_residual_m3": 0.25, "mass_residual_ratio": 1.5e-6},
+            "mass_balance": mass_balance(snap_h[-1], area),
         }
+
+    def mass_balance(final_h, area):
+        # the keys and formula of the reference engine's mass balance (engine.py:203-214, 364-382)
+        led = [float(x) for x in res["ledger"]]
+        cum = dict(zip(("rainfall_input_m3", "infiltration_loss_m3", "boundary_net_flux_m3", "outfall_discharge_m3",
+                        "overflow_surcharge_m3", "unreturned_overflow_m3"), led[:6]))
+        cum.update(external_boundary_inflow_m3=0.0, surface_recharge_capture_m3=0.0, surface_recharge_loss_m3=0.0)
+        vs0 = float(np.sum(h0.astype(np.float64) * area))
+        vn0 = float(np.sum(np.asarray(topo.pipe_state.node_volume_m3, np.float64)))
+        vs = float(np.sum(final_h.astype(np.float64) * area))
+        vn = float(np.asarray(res["final_V"], np.float32).sum())
+        lhs = vs0 + vn0 + cum["rainfall_input_m3"]
+        rhs = (vs + vn + cum["infiltration_loss_m3"] + cum["outfall_discharge_m3"] + cum["unreturned_overflow_m3"]
+               - cum["boundary_net_flux_m3"])
+        return {**cum, "initial_surface_volume_m3": vs0, "initial_node_volume_m3": vn0,
+                "final_surface_volume_m3": vs, "final_node_volume_m3": vn, "mass_residual_m3": lhs - rhs,
+                "mass_residual_ratio": (lhs - rhs) / max(abs(lhs), 1.0)}
 
     ref = result_of(res["snap_h"], res["snap_hu"], res["snap_hv"])
     pert = rng.normal(0.0, 2.0e-3, res["snap_h"].shape).astype(np.float32)
     cand_h = np.maximum(res["snap_h"] + pert * (res["snap_h"] > 0), 0).astype(np.float32)
     cand = result_of(cand_h, res["snap_hu"], res["snap_hv"])
-    cand["mass_balance"]["mass_residual_ratio"] = 2.0e-6
     static = {
         "mesh/nodes_xy": np.asarray(mesh.nodes_xy, np.float64), "mesh/triangles": np.asarray(mesh.triangles, np.int64),
         "mesh/centroids_xy": np.asarray(mesh.centroids_xy, np.float64),
