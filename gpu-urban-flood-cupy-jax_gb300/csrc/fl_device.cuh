@@ -229,21 +229,25 @@ __device__ __forceinline__ void clamp_velocity_exact(float h, float &hu, float &
 
 // CFL local timestep of one cell (equations.py:155-178), correctly rounded
 // and uncontracted: the reference's float32 expression bit-for-bit.
+// NumPy's maximum passes a NaN through (fmax32 would return its second
+// argument); the CFL expressions use this one, so a NaN depth or momentum
+// gives a NaN local dt that the caller's isfinite test drops, as in the
+// reference.  (The solver's own state never holds a NaN depth: the cell
+// update clips it to zero.)
+__device__ __forceinline__ float nanmax32(float a, float b) { return isnan(a) ? a : fmax32(a, b); }
+
 __device__ __forceinline__ float cfl_local(float h, float hu, float hv, float char_len, float cfl, float g, float md) {
-    // NumPy's maximum passes a NaN depth through, so such a cell's local dt is
-    // NaN and the caller's isfinite test drops it (the solver's own state
-    // never holds a NaN depth: the cell update clips it to zero)
-    const float hs = isnan(h) ? h : fmax32(h, md);
+    const float hs = nanmax32(h, md);
     const float u = xdiv(hu, hs), w = xdiv(hv, hs);
     const float speed = xadd(xsqrt(xadd(xmul(u, u), xmul(w, w))), xsqrt(xmul(g, hs)));
-    return xdiv(xmul(cfl, char_len), fmax32(speed, 1.0e-12f));
+    return xdiv(xmul(cfl, char_len), nanmax32(speed, 1.0e-12f));
 }
 
 // Local-inertial CFL of one cell (reference equations.py:181-210): gravity-
 // wave speed only, correctly rounded as the reference's float32 arrays.
 __device__ __forceinline__ float cfl_local_li(float h, float char_len, float cfl, float g, float md) {
-    const float c = xsqrt(xmul(g, fmax32(h, md)));
-    return xdiv(xmul(cfl, char_len), fmax32(c, 1.0e-12f));
+    const float c = xsqrt(xmul(g, nanmax32(h, md)));
+    return xdiv(xmul(cfl, char_len), nanmax32(c, 1.0e-12f));
 }
 
 // --------------------------------------------------------------- inlets

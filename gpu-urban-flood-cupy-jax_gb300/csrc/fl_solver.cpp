@@ -1162,12 +1162,16 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
         }
     };
     const int per = (kernel == 0 && s->li_mode) ? 2 : 1;  // kernels per launch
-    // One launch captured as a graph and replayed, as in the step loop: the
-    // time is the kernels' own, not the host's launch rate.
+    // A chain of launches captured as one graph and replayed, as in the step
+    // loop: the time is the kernels' own, not the host's launch rate or a
+    // graph launch's.
+    const int chain = std::min(reps, 32);
+    const int replays = (reps + chain - 1) / chain;
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
     FL_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
-    const cudaError_t le = launch(s->cap_stream);
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < chain && le == cudaSuccess; ++i) le = launch(s->cap_stream);
     const cudaError_t ce = cudaStreamEndCapture(s->cap_stream, &g);
     cudaError_t err = le != cudaSuccess ? le : ce;
     if (err == cudaSuccess) err = cudaGraphInstantiate(&ge, g, 0);
@@ -1178,7 +1182,7 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
     if (err == cudaSuccess) err = cudaEventCreate(&e1);
     if (err == cudaSuccess) err = cudaGraphLaunch(ge, st);  // warm-up
     if (err == cudaSuccess) err = cudaEventRecord(e0, st);
-    for (int i = 0; i < reps && err == cudaSuccess; ++i) err = cudaGraphLaunch(ge, st);
+    for (int i = 0; i < replays && err == cudaSuccess; ++i) err = cudaGraphLaunch(ge, st);
     if (err == cudaSuccess) err = cudaEventRecord(e1, st);
     if (err == cudaSuccess) err = cudaEventSynchronize(e1);
     if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
@@ -1186,8 +1190,8 @@ FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *strea
     if (e1) cudaEventDestroy(e1);
     if (ge) cudaGraphExecDestroy(ge);
     if (err != cudaSuccess) return set_error(FL_E_CUDA, "fl_time_kernel: %s", cudaGetErrorString(err));
-    g_launches += (int64_t)per * (reps + 1);
-    *ms_per_launch = (double)ms / reps;
+    g_launches += (int64_t)per * chain * (replays + 1);
+    *ms_per_launch = (double)ms / ((double)replays * chain);
     return FL_OK;
 }
 

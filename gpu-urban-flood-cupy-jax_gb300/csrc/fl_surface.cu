@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(SURF_THREADS, 4) k_surface(const __grid_consta
         for (int k = 0; k < 2; ++k) {
             mbar_init(bar_base + 8u * k, 1);
             mbar_init(bar_base + 16u + 8u * k, 32);
-            mbar_init(bar_base + 32u + 8u * k, 1);
+            mbar_init(bar_base + 32u + 8u * k, TILE / 32);  // one arrival per compute warp
         }
         mbar_fence_init();
     }
@@ -263,8 +263,12 @@ __global__ void __launch_bounds__(SURF_THREADS, 4) k_surface(const __grid_consta
                 a.snap_hv[o] = hvn;
             }
         }
-        compute_sync();  // this stage and the flux slots are free again
-        if (tid == 0) mbar_arrive((bar_base + 32u + 8u * st_i));
+        // each compute warp releases the stage once its lanes are done with it;
+        // the flux slots need no barrier here: the next tile's phase 2 writes
+        // them only after its opening barrier reduction, which every compute
+        // thread reaches after this phase 3
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive((bar_base + 32u + 8u * st_i));
     }
     warp_add_ledger_at<SURF_TERMS>(led, a.ledger, (int)blockIdx.x * (TILE / 32) + (tid >> 5));
 }

@@ -316,7 +316,7 @@ class FloodSolver:
 
     def time_kernel(self, kernel: int, reps: int = 50, stream=None) -> float:
         """Mean ms per launch of one step kernel (0 surface, 1 inlets, 2 network, 3 CFL, 4 links, 5 donor
-        factors)."""
+        factors), launched in chains as in the step loop."""
 
         v = C.c_double(0.0)
         N.check(self._lib.fl_time_kernel(self._h, int(kernel), int(reps), _stream_handle(stream), C.byref(v)),

@@ -267,8 +267,12 @@ FL_API int fl_plan_tiles(const FlMeshDesc *mesh, int64_t *tiles);
 
 /* Time `reps` back-to-back launches of one kernel of a step (0 surface (the
  * two local-inertial launches in that mode), 1 node inlet exchange, 2 pipe
- * network, 3 CFL reduction, 4 link update, 5 donor factors) between CUDA events on
- * `stream`, at the solver's current state and last dt; the clock is not
+ * network, 3 CFL reduction, 4 link update, 5 donor factors) between CUDA
+ * events on `stream`, at the solver's current state and last dt.  The
+ * launches are captured in chains of up to 32 per CUDA graph, each launched
+ * as in the step loop (the surface, link, donor and network kernels as
+ * programmatic dependents of the launch before them), so the time per launch
+ * is the kernel's own in-loop cost, not a graph launch's.  The clock is not
  * advanced but the state buffers are overwritten (reset before the next run).
  * No reference counterpart: it is the measurement hook for the roofline. */
 FL_API int fl_time_kernel(FlSolver *solver, int32_t kernel, int32_t reps, void *stream, double *ms_per_launch);
