@@ -52,6 +52,7 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true", help="skip the ensemble / surrogate screening measurement")
+    p.add_argument("--no-long-run", action="store_true", help="skip the 24 h single-instance run")
     p.add_argument("--cpu-seconds", type=float, default=60.0,
                    help="reference arm: CPU seconds spread over the timed samples")
     p.add_argument("--mid-run-step", type=int, default=MID_RUN_STEP,
@@ -433,6 +434,9 @@ def our_arm(args):
     ensemble = None
     if world == 1 and not args.no_ensemble:
         ensemble = ensemble_measure()
+    long_run = None
+    if world == 1 and not args.no_long_run:
+        long_run = long_single(24.0)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / len(ms), "higher_is_better": True, "scaling": "weak",
@@ -461,6 +465,7 @@ def our_arm(args):
         "cpu_baseline": base,
         "parity": parity,
         "ensemble": ensemble,
+        "long_run_24h": long_run,
     }
     print(json.dumps(line), flush=True)
 
@@ -538,12 +543,56 @@ def profile_arm(args):
     solver.close()
 
 
-def long_arm(args):
+def long_single(hours: float = 24.0) -> dict:
     """The whole 160.09 mm / 24 h front-loaded event on the production-shaped
-    coupled city (one instance, the float64 ledger closed every simulated
-    hour), then `long_members` members with seeded variants of the event
-    (intensity x U(0.7, 1.3), peak shifted by up to +-3 h) run concurrently,
-    one host thread and CUDA stream each (replicas on one GPU)."""
+    coupled city, one instance, the float64 ledger closed after every
+    simulated hour (its residual against the inflow)."""
+
+    import numpy as np
+    import torch
+
+    from floodgb.config import load_config
+    from floodgb.solver import solver_for_city
+    from floodgb.synthetic import production_workload
+
+    sc = production_workload()
+    dur_s = hours * 3600.0
+    cfg = load_config(None, dict(sc.overrides, **{"solver.duration_min": hours * 60.0}))
+    topo = sc.city.topologies
+    area = np.asarray(topo.surface_topology.cell_area_m2, np.float64)
+    C = topo.surface_topology.cell_count
+    v0 = float(np.sum(np.asarray(topo.surface_state.h_m, np.float64) * area)) + float(
+        np.sum(topo.pipe_state.node_volume_m3))
+    s = solver_for_city(sc.city, sc.rainfall, cfg, duration_s=dur_s)
+    worst = 0.0
+    solve_s = 0.0
+    for k in range(1, int(np.ceil(hours)) + 1):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.run(min(k * 3600.0, dur_s))
+        torch.cuda.synchronize()
+        solve_s += time.perf_counter() - t
+        led = s.ledger()
+        lhs = v0 + led["rainfall_input_m3"]
+        rhs = (led["surface_volume_m3"] + led["node_volume_m3"] + led["infiltration_loss_m3"]
+               + led["outfall_discharge_m3"] + led["unreturned_overflow_m3"] - led["boundary_net_flux_m3"])
+        worst = max(worst, abs(lhs - rhs) / max(abs(lhs), 1.0))
+    p = s.progress()
+    led = s.ledger()
+    s.close()
+    return {"hours": hours, "solver_s": solve_s, "steps": p.step_count, "cell_steps_per_s": C * p.step_count / solve_s,
+            "snapshots": p.snapshot_count, "worst_hourly_ledger_residual_ratio": worst,
+            "rainfall_input_m3": led["rainfall_input_m3"], "outfall_discharge_m3": led["outfall_discharge_m3"],
+            "timing": "wall clock around each simulated hour's fl_run (device loop), synchronised",
+            "reference_24h_cupy_s": 430.467,
+            "reference_hardware": "RTX PRO 4000 Blackwell, real 981,880-tri city, 321,645 steps"}
+
+
+def long_arm(args):
+    """The 24 h single instance (long_single), then `long_members` members
+    with seeded variants of the event (intensity x U(0.7, 1.3), peak shifted
+    by up to +-3 h) run concurrently, one host thread and CUDA stream each
+    (replicas on one GPU)."""
 
     import threading
 
@@ -559,37 +608,12 @@ def long_arm(args):
 
     build_library()
     native.load()
+    single = long_single(args.long_hours)
     sc = production_workload()
     dur_s = args.long_hours * 3600.0
     cfg = load_config(None, dict(sc.overrides, **{"solver.duration_min": args.long_hours * 60.0}))
-    topo = sc.city.topologies
-    area = np.asarray(topo.surface_topology.cell_area_m2, np.float64)
-    C = topo.surface_topology.cell_count
-    v0 = float(np.sum(np.asarray(topo.surface_state.h_m, np.float64) * area)) + float(
-        np.sum(topo.pipe_state.node_volume_m3))
-    s = solver_for_city(sc.city, sc.rainfall, cfg, duration_s=dur_s)
-    worst = 0.0
-    solve_s = 0.0
-    hours = int(np.ceil(args.long_hours))
-    for k in range(1, hours + 1):
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        s.run(min(k * 3600.0, dur_s))
-        torch.cuda.synchronize()
-        solve_s += time.perf_counter() - t
-        led = s.ledger()
-        lhs = v0 + led["rainfall_input_m3"]
-        rhs = (led["surface_volume_m3"] + led["node_volume_m3"] + led["infiltration_loss_m3"]
-               + led["outfall_discharge_m3"] + led["unreturned_overflow_m3"] - led["boundary_net_flux_m3"])
-        worst = max(worst, abs(lhs - rhs) / max(abs(lhs), 1.0))
-    p = s.progress()
-    n_snap = p.snapshot_count
-    s.close()
-    single = {"hours": args.long_hours, "solver_s": solve_s, "steps": p.step_count,
-              "cell_steps_per_s": C * p.step_count / solve_s, "snapshots": n_snap,
-              "worst_hourly_ledger_residual_ratio": worst,
-              "reference_24h_cupy_s": 430.467, "reference_hardware": "RTX PRO 4000 Blackwell, real 981,880-tri city"}
-    # concurrent members with seeded rainfall variants
+    C = sc.city.topologies.surface_topology.cell_count
+    solve_s = single["solver_s"]
     rng = np.random.default_rng(24)
     solvers, streams = [], []
     for m in range(args.long_members):
