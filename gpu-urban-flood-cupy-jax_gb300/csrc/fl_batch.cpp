@@ -258,10 +258,11 @@ static int batch_create_impl(int32_t n, const FlMeshDesc *meshes, const FlForcin
         b->snap_base_h[s] = snap_total;
         snap_total += (int64_t)params[s].max_snapshots * b->cells_s[s];
     }
-    float *snap_h, *snap_hmax;
+    float *snap_h, *snap_hmax, *snap_hu, *snap_hv;
     double *snap_t;
     int64_t *d_snap_base;
     if ((rc = b->alloc(&snap_h, (size_t)snap_total)) || (rc = b->alloc(&snap_hmax, (size_t)snap_total)) ||
+        (rc = b->alloc(&snap_hu, (size_t)snap_total)) || (rc = b->alloc(&snap_hv, (size_t)snap_total)) ||
         (rc = b->alloc(&snap_t, (size_t)n * b->max_snaps)) || (rc = b->upload(&d_snap_base, b->snap_base_h)))
         return rc;
     // hyetographs
@@ -303,6 +304,8 @@ static int batch_create_impl(int32_t n, const FlMeshDesc *meshes, const FlForcin
     a.tile_led = tile_led;
     a.snap_h = snap_h;
     a.snap_hmax = snap_hmax;
+    a.snap_hu = snap_hu;
+    a.snap_hv = snap_hv;
     a.snap_base = d_snap_base;
     a.run = b->run;
     a.n_tiles = b->tiles;
@@ -568,6 +571,26 @@ FL_API int fl_batch_get_snapshots(FlBatch *b, int32_t scen, int32_t first, int32
         if (hmax && (rc = scen_to_reference(b, scen, b->ba.snap_hmax + o, hmax + (size_t)i * C, mem, st))) return rc;
     }
     add_launches((int64_t)count * ((h ? 1 : 0) + (hmax ? 1 : 0)));
+    return FL_OK;
+}
+
+FL_API int fl_batch_get_snapshot_momentum(FlBatch *b, int32_t scen, int32_t first, int32_t count, float *hu,
+                                          float *hv, int32_t mem, void *stream) {
+    if (!b || scen < 0 || scen >= b->S) return set_error(FL_E_INVALID, "bad batch or scenario");
+    cudaStream_t st = (cudaStream_t)stream;
+    FB_CUDA(cudaSetDevice(b->device));
+    RunCtrl r;
+    FB_CUDA(cudaMemcpy(&r, b->run + scen, sizeof(RunCtrl), cudaMemcpyDeviceToHost));
+    if (first < 0 || count < 0 || first + count > r.snap_count)
+        return set_error(FL_E_INVALID, "snapshots [%d, %d) requested, %d available", first, first + count, r.snap_count);
+    const size_t C = (size_t)b->cells_s[scen];
+    for (int32_t i = 0; i < count; ++i) {
+        const size_t o = (size_t)b->snap_base_h[scen] + (size_t)(first + i) * C;
+        int rc;
+        if (hu && (rc = scen_to_reference(b, scen, b->ba.snap_hu + o, hu + (size_t)i * C, mem, st))) return rc;
+        if (hv && (rc = scen_to_reference(b, scen, b->ba.snap_hv + o, hv + (size_t)i * C, mem, st))) return rc;
+    }
+    add_launches((int64_t)count * ((hu ? 1 : 0) + (hv ? 1 : 0)));
     return FL_OK;
 }
 

@@ -45,6 +45,7 @@ struct BatchArgs {
     float *tile_min;              // [tiles] CFL minimum of the tile's output (flagged steps)
     float *tile_led;              // [tiles * SURF_TERMS] the tile's ledger terms of the step
     float *snap_h, *snap_hmax;
+    float *snap_hu, *snap_hv;     // momentum at each snapshot (same layout)
     const int64_t *snap_base;     // [n] first snapshot element of each scenario
     RunCtrl *run;                 // [n]
     int32_t n_tiles, tile, e_cap, h_cap;

@@ -210,6 +210,8 @@ __global__ void __launch_bounds__(T, 1024 / T) k_surface_batch(const __grid_cons
                 const size_t o = (size_t)a.snap_base[E.scen] + (size_t)snap * (size_t)E.cells + (size_t)c_local;
                 a.snap_h[o] = hn;
                 a.snap_hmax[o] = hm;
+                a.snap_hu[o] = hun;
+                a.snap_hv[o] = hvn;
                 a.hmax[c] = 0.0f;
             } else {
                 a.hmax[c] = hm;

@@ -119,9 +119,10 @@ class BatchSolver:
                                              _stream_handle(stream)), "fl_batch_get_state")
         return h, hu, hv
 
-    def snapshots(self, scen: int, stream=None):
+    def snapshots(self, scen: int, stream=None, momentum: bool = False):
         """(times_s, h, hmax) of every snapshot of a scenario; hmax = maximum
-        depth since the previous snapshot."""
+        depth since the previous snapshot.  With momentum, (times_s, h, hmax,
+        hu, hv)."""
 
         n = self.progress(scen, stream).snapshot_count
         c = self.cell_counts[scen]
@@ -132,7 +133,15 @@ class BatchSolver:
             N.check(self._lib.fl_batch_get_snapshots(self._h, int(scen), 0, int(n), C.c_void_p(t.ctypes.data),
                                                      C.c_void_p(h.ctypes.data), C.c_void_p(hm.ctypes.data),
                                                      N.FL_MEM_HOST, _stream_handle(stream)), "fl_batch_get_snapshots")
-        return t, h, hm
+        if not momentum:
+            return t, h, hm
+        hu = np.empty((n, c), np.float32)
+        hv = np.empty((n, c), np.float32)
+        if n:
+            N.check(self._lib.fl_batch_get_snapshot_momentum(self._h, int(scen), 0, int(n), C.c_void_p(hu.ctypes.data),
+                                                             C.c_void_p(hv.ctypes.data), N.FL_MEM_HOST,
+                                                             _stream_handle(stream)), "fl_batch_get_snapshot_momentum")
+        return t, h, hm, hu, hv
 
     def ledger(self, scen: int, stream=None) -> dict:
         out = (C.c_double * len(N.LEDGER_NAMES))()

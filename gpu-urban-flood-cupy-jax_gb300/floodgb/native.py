@@ -183,6 +183,8 @@ _SIGNATURES = {
                                      C.c_void_p]),
     "fl_batch_get_snapshots": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_int32, C.c_void_p]),
+    "fl_batch_get_snapshot_momentum": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                                 C.c_void_p, C.c_int32, C.c_void_p]),
     "fl_batch_read_ledger": (C.c_int, [C.c_void_p, C.c_int32, f64p, C.c_int32, C.c_void_p]),
     "fl_batch_info": (C.c_int, [C.c_void_p, C.POINTER(FlBatchShape), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                 i32p]),

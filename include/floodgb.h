@@ -337,6 +337,11 @@ FL_API int fl_batch_get_state(FlBatch *batch, int32_t scen, float *h, float *hu,
  * previous snapshot (count x cells each, reference order); times in s. */
 FL_API int fl_batch_get_snapshots(FlBatch *batch, int32_t scen, int32_t first, int32_t count, double *times_s,
                                   float *h, float *hmax, int32_t mem, void *stream);
+/* The momentum (hu, hv) at the same snapshots (count x cells each, reference
+ * order; either pointer may be NULL).  No counterpart in the reference: the
+ * surrogate's training data. */
+FL_API int fl_batch_get_snapshot_momentum(FlBatch *batch, int32_t scen, int32_t first, int32_t count, float *hu,
+                                          float *hv, int32_t mem, void *stream);
 /* Cumulative ledger of one scenario (FL_LEDGER_RAINFALL..BOUNDARY_OUT and
  * FL_LEDGER_SURFACE_VOLUME are filled). */
 FL_API int fl_batch_read_ledger(FlBatch *batch, int32_t scen, double *out, int32_t n, void *stream);

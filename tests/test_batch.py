@@ -89,9 +89,10 @@ def test_batch_matches_single_instance_bitwise(tile):
             assert p.step_count == prog.step_count and p.t_s == prog.t_s and p.last_dt_s == prog.last_dt_s
             h, hu, hv = b.state(k)
             assert np.array_equal(h, state[0]) and np.array_equal(hu, state[1]) and np.array_equal(hv, state[2])
-            t, sh, smax = b.snapshots(k)
+            t, sh, smax, shu, shv = b.snapshots(k, momentum=True)
             assert np.array_equal(t, snaps[0])
             assert np.array_equal(sh, snaps[1])
+            assert np.array_equal(shu, snaps[2]) and np.array_equal(shv, snaps[3])
             assert np.all(smax >= sh)
             led = b.ledger(k)
             assert led["rainfall_input_m3"] > 0.0
