@@ -301,8 +301,10 @@ def ensemble_measure(screen_members: int = 1024):
         r = screen_saved(SURROGATE_WEIGHTS, n_eval=screen_members, plain_sample=2, score_all=False)
         out["surrogate_screening"] = {
             "members": r["members"], "mesh_cells": r["mesh_cells"], "scenario_hours": r["scenario_hours"],
-            "flagged": r["flagged"], "audited": r["audited"], "scored": r["scored"],
-            "audit_scores": r["audit_scores"], "throughput_scenario_h_per_s": r["throughput_scenario_h_per_s"],
+            "ensemble_networks": r["ensemble_networks"], "flag_threshold_m": r["flag_threshold_m"],
+            "flagged": r["flagged"], "audited": r["audited"], "re_solved": r["re_solved"], "scored": r["scored"],
+            "flagged_scores": r["surrogate_flagged"], "audit_scores": r["audit_scores"],
+            "calibration": r["calibration"], "throughput_scenario_h_per_s": r["throughput_scenario_h_per_s"],
         }
     return out
 
@@ -484,7 +486,8 @@ def profile_surrogate():
 
     build_library()
     native.load()
-    model, _, meta = load(SURROGATE_WEIGHTS)
+    models, _, meta = load(SURROGATE_WEIGHTS)
+    model = models[0]
     city, _ = _mesh(int(meta["grid_n"]), int(meta["seed"]))
     mf = MeshFeatures(city.topologies.surface_topology)
     g = mf.graph.replicate(19)

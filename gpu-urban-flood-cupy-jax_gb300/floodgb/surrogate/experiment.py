@@ -2,10 +2,13 @@
 
 One mesh (a jittered grid with a seeded random-field bed), seeded storms
 (peak 20-120 mm/h, duration 1-6 h): the batched solver generates training
-trajectories, the network is trained on the GPU, then a held-out ensemble is
-screened -- surrogate rollouts for every member, flags for members outside
-the training range, a random audit -- and the solver re-runs the flagged and
-audited members and scores the surrogate on every member.  Throughput is
+trajectories, an ensemble of networks is trained on the GPU (a few training
+storms held out), the flag threshold on the networks' disagreement is
+calibrated on the held-out storms, then a held-out ensemble is screened --
+ensemble rollouts for every member, flags where the networks disagree, a
+random audit -- and the solver re-runs the flagged and audited members and
+scores the surrogate on them (or on every member).  The audit is drawn before
+the rollouts, so its re-runs overlap them on a second stream.  Throughput is
 scenario-hours per second of the whole screening (surrogate + re-runs)
 against the plain single-instance solver (one FloodSolver run per member,
 sequentially) and the batched solver.
@@ -41,45 +44,70 @@ def _mesh(grid_n: int, seed: int):
     return sc.city, cfg
 
 
-def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: float = 0.05, seed: int = 0,
+def screen(models, mf, city, cfg, threshold: float, storms, durations, *, audit: float = 0.05, seed: int = 0,
            plain_sample: int = 8, batch_size: int = 64, baselines: bool = False, n_layers: int = 8,
-           score_all: bool = True) -> dict:
-    """Screen an ensemble: surrogate rollouts of every member, flags, a random
-    audit; the solver re-runs flagged + audited members (timed) and judges
-    every member (or, with score_all False, the re-run members only); the
-    plain single-instance solver is timed on a sample."""
+           score_all: bool = True, overlap: bool = True) -> dict:
+    """Screen an ensemble: a random audit, ensemble rollouts of every member
+    (the audit re-runs overlapping them on a second stream), flags where the
+    networks disagree, solver re-runs of the flagged members; the solver
+    judges the re-run members (or, with score_all, every member); the plain
+    single-instance solver is timed on a sample."""
+
+    import threading
 
     import torch
 
     from ..solver import solver_for_city
     from . import ops
     from .model import MPNN
-    from .pipeline import flags, rollout_batch, score, solve_members
+    from .pipeline import ensemble_rollouts, flags, rollout_batch, score, solve_members
 
     rng = np.random.default_rng(seed)
     n = len(storms)
     copies = max(1, min(64, 2_000_000 // mf.C))
+    audited = np.zeros(n, bool)
+    audited[rng.choice(n, size=min(int(np.ceil(audit * n)), n), replace=False)] = True
+    a_idx = np.flatnonzero(audited)
     # warm-up, not timed (as the solvers are warmed up): the first pass of a
     # batch shape loads the kernels and grows the allocator's pool
-    rollout_batch(model, mf, storms[:copies], [min(float(d), 3600.0) for d in durations[:copies]], copies=copies)
+    ensemble_rollouts(models, mf, storms[:copies], [min(float(d), 3600.0) for d in durations[:copies]], copies=copies)
     torch.cuda.synchronize()
+    audit_out = {}
+
+    def run_audit():
+        side = torch.cuda.Stream()
+        audit_out["r"] = solve_members(city, cfg, [storms[i] for i in a_idx], [durations[i] for i in a_idx],
+                                       batch_size, stream=side)
+
     t = time.perf_counter()
-    preds = rollout_batch(model, mf, storms, durations, copies=copies)
-    torch.cuda.synchronize()
+    worker = threading.Thread(target=run_audit) if overlap else None
+    if worker is not None:
+        worker.start()
+    else:
+        run_audit()
+    main = torch.cuda.Stream()
+    with torch.cuda.stream(main):
+        preds, spread = ensemble_rollouts(models, mf, storms, durations, copies=copies)
+    main.synchronize()
     surr_s = time.perf_counter() - t
+    if worker is not None:
+        worker.join()
+    audit_trajs, audit_solver_s, audit_h = audit_out["r"]
+    overlap_s = time.perf_counter() - t
     ops.status()
     hours = float(sum(durations)) / 3600.0
-    flagged = np.array([flags(mf, s, p, limits) for s, p in zip(storms, preds)])
-    audited = np.zeros(n, bool)
-    cand = np.flatnonzero(~flagged)
-    if cand.size:
-        audited[rng.choice(cand, size=min(int(np.ceil(audit * n)), cand.size), replace=False)] = True
-    idx = np.flatnonzero(flagged | audited)
-    rerun_s, rerun_h = 0.0, 0.0
-    reruns = []
-    if idx.size:
-        reruns, rerun_s, rerun_h = solve_members(city, cfg, [storms[i] for i in idx], [durations[i] for i in idx],
-                                                 batch_size)
+    flagged = flags(spread, threshold)
+    f_idx = np.flatnonzero(flagged & ~audited)
+    t = time.perf_counter()
+    flag_trajs = []
+    if f_idx.size:
+        flag_trajs, _, _ = solve_members(city, cfg, [storms[i] for i in f_idx], [durations[i] for i in f_idx],
+                                         batch_size)
+    torch.cuda.synchronize()
+    flag_s = time.perf_counter() - t
+    rerun = {int(i): tr for i, tr in zip(a_idx, audit_trajs)}
+    rerun.update({int(i): tr for i, tr in zip(f_idx, flag_trajs)})
+    rerun_h = float(sum(durations[i] for i in rerun)) / 3600.0
     if score_all:
         truth, batched_s, _ = solve_members(city, cfg, storms, durations, batch_size)
         scores = [score(mf, p, tr) for p, tr in zip(preds, truth)]
@@ -87,10 +115,10 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
     else:
         truth, batched_s = None, None
         scores = [None] * n
-        for j, i in enumerate(idx):
-            scores[i] = score(mf, preds[i], reruns[j])
+        for i, tr in rerun.items():
+            scores[i] = score(mf, preds[i], tr)
         scored = flagged | audited
-    del reruns
+    del rerun, audit_trajs, flag_trajs
 
     def agg(mask):
         mask = mask & scored
@@ -100,11 +128,14 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
         return {k: float(np.mean([s[k] for s in sel])) for k in sel[0]} | {
             "max_rmse_hmax_m": float(np.max([s["rmse_hmax_m"] for s in sel])), "members": int(mask.sum())}
 
-    res = {"members": n, "scenario_hours": hours, "flagged": int(flagged.sum()), "audited": int(audited.sum()),
+    res = {"members": n, "scenario_hours": hours, "ensemble_networks": len(models),
+           "flag_threshold_m": float(threshold), "flagged": int(flagged.sum()), "audited": int(audited.sum()),
+           "re_solved": int(flagged.sum() + audited.sum() - (flagged & audited).sum()),
            "scored": "all members" if score_all else "flagged and audited members (solver re-runs)",
-           "surrogate_accepted": agg(~flagged), "surrogate_flagged": agg(flagged), "audit_scores": agg(audited)}
+           "surrogate_accepted": agg(~flagged), "surrogate_flagged": agg(flagged), "audit_scores": agg(audited),
+           "spread_m": {"mean": float(np.mean(spread)), "max": float(np.max(spread))}}
     if baselines and truth is not None:
-        # what the trained network gains: an untrained network and "the depth does not change"
+        # what the trained networks gain: an untrained network and "the depth does not change"
         p0 = rollout_batch(MPNN(n_layers=n_layers, seed=seed + 99), mf, storms, durations, copies=copies)
         zero = [(p[0], np.zeros_like(p[1]), np.zeros_like(p[2])) for p in preds]
         res["untrained"] = float(np.mean([score(mf, p, tr)["rmse_hmax_m"] for p, tr in zip(p0, truth)]))
@@ -120,14 +151,16 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
         plain_h += durations[i] / 3600.0
         s.close()
     plain_rate = plain_h / plain_s
-    screen_s = surr_s + rerun_s
+    screen_s = overlap_s + flag_s
     res["throughput_scenario_h_per_s"] = {
         "plain_single_instance": plain_rate,
-        "batched_solver": hours / batched_s if batched_s else (rerun_h / rerun_s if rerun_s else None),
+        "batched_solver": hours / batched_s if batched_s else (audit_h / audit_solver_s if audit_solver_s else None),
         "surrogate_only": hours / surr_s,
         "screening": hours / screen_s,
         "screening_over_plain": (hours / screen_s) / plain_rate,
-        "surrogate_s": surr_s, "rerun_s": rerun_s, "rerun_scenario_h": rerun_h,
+        "surrogate_s": surr_s, "audit_rerun_solver_s": audit_solver_s, "surrogate_and_audit_wall_s": overlap_s,
+        "flag_rerun_s": flag_s, "rerun_scenario_h": rerun_h,
+        "audit_overlapped_with_rollouts": bool(overlap),
     }
     return res
 
@@ -135,77 +168,99 @@ def screen(model, mf, city, cfg, limits: dict, storms, durations, *, audit: floa
 def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 11, epochs: int = 8,
         lr: float = 1e-3, audit: float = 0.05, n_layers: int = 8, plain_sample: int = 8, batch_size: int = 64,
         duration_cap_h: float | None = None, train_seconds: float | None = None, log=print, weights_out=None,
-        baselines: bool = False):
-    """Train on n_train solver trajectories, then screen n_eval held-out storms."""
+        baselines: bool = False, n_models: int = 2, n_val: int = 32, flag_fraction: float = 0.04,
+        extent_weight: float = 3.0, pushforward: float = 0.5):
+    """Train an ensemble of n_models networks on n_train - n_val solver
+    trajectories, calibrate the flag threshold on the other n_val, then screen
+    n_eval held-out storms."""
 
     import torch
 
     from .model import MPNN
-    from .pipeline import MeshFeatures, solve_members, train
+    from .pipeline import MeshFeatures, calibrate_flags, ensemble_rollouts, score, solve_members, train
 
     city, cfg = _mesh(grid_n, seed)
     mf = MeshFeatures(city.topologies.surface_topology)
     tr_storms, tr_dur = _storms(n_train, seed + 1, duration_cap_h)
     ev_storms, ev_dur = _storms(n_eval, seed + 2, duration_cap_h)
-    res = {"mesh_cells": mf.C, "dual_edges": mf.graph.E, "train_members": n_train, "eval_members": n_eval,
-           "layers": n_layers, "hidden": 128}
+    res = {"mesh_cells": mf.C, "dual_edges": mf.graph.E, "train_members": n_train - n_val, "validation_members": n_val,
+           "eval_members": n_eval, "layers": n_layers, "hidden": 128, "ensemble_networks": n_models,
+           "extent_weight": extent_weight, "pushforward": pushforward}
     t = time.perf_counter()
     trajs, solve_s, tr_hours = solve_members(city, cfg, tr_storms, tr_dur, batch_size)
     res["train_data"] = {"solver_s": solve_s, "scenario_hours": tr_hours, "wall_s": time.perf_counter() - t}
     log(f"training trajectories: {tr_hours:.1f} scenario-h in {solve_s:.1f} s")
-    model = MPNN(n_layers=n_layers, seed=seed)
+    fit, val = trajs[:n_train - n_val], trajs[n_train - n_val:]
+    models, hists = [], []
     torch.cuda.synchronize()
     t = time.perf_counter()
-    hist = train(model, mf, trajs, epochs=epochs, lr=lr, seed=seed, log=log, max_seconds=train_seconds)
+    for k in range(n_models):
+        m = MPNN(n_layers=n_layers, seed=seed + 1000 * k)
+        hists.append(train(m, mf, fit, epochs=epochs, lr=lr, seed=seed + k, log=log, max_seconds=train_seconds,
+                           extent_weight=extent_weight, pushforward=pushforward))
+        models.append(m)
     torch.cuda.synchronize()
-    res["train"] = {"seconds": time.perf_counter() - t, "epochs": len(hist), "loss": hist,
-                    "windows": sum(len(tr.times_s) - 1 for tr in trajs)}
+    res["train"] = {"seconds": time.perf_counter() - t, "epochs": [len(h) for h in hists], "loss": hists,
+                    "windows": sum(len(tr.times_s) - 1 for tr in fit)}
+    # flag threshold: the networks' disagreement on the held-out training storms
+    preds, spread = ensemble_rollouts(models, mf, tr_storms[n_train - n_val:], tr_dur[n_train - n_val:])
+    errors = [score(mf, p, tr)["rmse_hmax_m"] for p, tr in zip(preds, val)]
+    cal = calibrate_flags(spread, np.asarray(errors), flag_fraction)
+    res["calibration"] = cal
+    log(f"calibration: {cal}")
     depth = lambda e: float(np.sum(e.intensity_mmhr * (e.end_min - e.start_min)) / 60.0)  # noqa: E731
     limits = {"peak_mmhr": max(float(e.intensity_mmhr.max()) for e in tr_storms),
-              "depth_mm": max(depth(e) for e in tr_storms),
-              "max_depth_m": 1.2 * max(float(tr.hmax.max().item()) for tr in trajs)}
+              "depth_mm": max(depth(e) for e in tr_storms)}
     res["limits"] = limits
-    del trajs
-    res.update(screen(model, mf, city, cfg, limits, ev_storms, ev_dur, audit=audit, seed=seed,
+    del trajs, fit, val
+    res.update(screen(models, mf, city, cfg, cal["threshold_m"], ev_storms, ev_dur, audit=audit, seed=seed,
                       plain_sample=plain_sample, batch_size=batch_size, baselines=baselines, n_layers=n_layers))
     if weights_out:
-        save(weights_out, model, limits, {"grid_n": grid_n, "seed": seed, "n_layers": n_layers})
+        save(weights_out, models, cal, limits, {"grid_n": grid_n, "seed": seed, "n_layers": n_layers})
     log(json.dumps(res["throughput_scenario_h_per_s"]))
     return res
 
 
-def save(path, model, limits: dict, meta: dict):
-    st = model.state()
-    np.savez_compressed(path, **{f"w{k}": d["w"] for k, d in enumerate(st)}, **{f"b{k}": d["b"] for k, d in enumerate(st)},
-                        limits=json.dumps(limits), meta=json.dumps(meta))
+def save(path, models, calibration: dict, limits: dict, meta: dict):
+    arrays = {}
+    for j, model in enumerate(models):
+        for k, d in enumerate(model.state()):
+            arrays[f"m{j}_w{k}"] = d["w"]
+            arrays[f"m{j}_b{k}"] = d["b"]
+    np.savez_compressed(path, **arrays, calibration=json.dumps(calibration), limits=json.dumps(limits),
+                        meta=json.dumps(dict(meta, networks=len(models))))
 
 
 def load(path):
-    """(model, limits, meta) from a file written by save()."""
+    """(networks, calibration, meta) from a file written by save()."""
 
     from .model import MPNN
 
     z = np.load(path)
     meta = json.loads(str(z["meta"]))
-    model = MPNN(n_layers=int(meta["n_layers"]), seed=0)
-    n = len(model.layers())
-    model.load([{"w": z[f"w{k}"], "b": z[f"b{k}"]} for k in range(n)])
-    return model, json.loads(str(z["limits"])), meta
+    models = []
+    for j in range(int(meta["networks"])):
+        model = MPNN(n_layers=int(meta["n_layers"]), seed=0)
+        n = len(model.layers())
+        model.load([{"w": z[f"m{j}_w{k}"], "b": z[f"m{j}_b{k}"]} for k in range(n)])
+        models.append(model)
+    return models, json.loads(str(z["calibration"])), meta
 
 
 def screen_saved(path, n_eval: int = 64, plain_sample: int = 2, audit: float = 0.05, duration_cap_h=None,
                  score_all: bool = True) -> dict:
-    """Screen the first n_eval held-out storms of the saved model's mesh and seed."""
+    """Screen the first n_eval held-out storms of the saved ensemble's mesh and seed."""
 
     from .pipeline import MeshFeatures
 
-    model, limits, meta = load(path)
+    models, cal, meta = load(path)
     city, cfg = _mesh(int(meta["grid_n"]), int(meta["seed"]))
     mf = MeshFeatures(city.topologies.surface_topology)
     storms, dur = _storms(n_eval, int(meta["seed"]) + 2, duration_cap_h)
-    res = screen(model, mf, city, cfg, limits, storms, dur, audit=audit, seed=int(meta["seed"]),
+    res = screen(models, mf, city, cfg, float(cal["threshold_m"]), storms, dur, audit=audit, seed=int(meta["seed"]),
                  plain_sample=plain_sample, score_all=score_all)
     res["mesh_cells"] = mf.C
+    res["calibration"] = cal
     return res
 
 
@@ -221,6 +276,8 @@ def main():
     p.add_argument("--train-seconds", type=float, default=None)
     p.add_argument("--out", default=None)
     p.add_argument("--weights", default=None)
+    p.add_argument("--networks", type=int, default=2)
+    p.add_argument("--flag-fraction", type=float, default=0.04)
     p.add_argument("--screen-only", default=None, help="screen with saved weights (no training)")
     a = p.parse_args()
     if a.screen_only:
@@ -232,7 +289,8 @@ def main():
         print(text)
         return
     res = run(a.grid_n, a.train, a.eval, a.seed, a.epochs, n_layers=a.layers, duration_cap_h=a.duration_cap_h,
-              train_seconds=a.train_seconds, weights_out=a.weights)
+              train_seconds=a.train_seconds, weights_out=a.weights, n_models=a.networks,
+              flag_fraction=a.flag_fraction)
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:

@@ -1,20 +1,22 @@
 """Training data, training, hourly rollout and ensemble screening.
 
 The surrogate maps the state at one hourly snapshot and the coming hour's
-rainfall to the next snapshot's depth and the maximum depth reached in
+rainfall to the next snapshot's state and the maximum depth reached in
 between.  Training pairs come from the solver's own trajectories (batched
-runs of seeded storms on one mesh); screening rolls the network out hour by
-hour from a dry start, flags members it should not be trusted on, and the
+runs of seeded storms on one mesh); screening rolls an ensemble of networks
+out hour by hour from a dry start, flags the members on which the networks
+disagree beyond a threshold calibrated on held-out training storms, and the
 plain solver re-runs the flagged members plus a random audit and scores the
 surrogate on them.
 
-Node inputs (12 features, padded to 64): depth, previous-snapshot depth and
-window maximum (x10, m -> dm), bed relative to the mesh mean, Manning n
-(x10), log cell area relative to its mean, characteristic length relative to
-its mean, exterior-boundary flag, rain depth of the coming window and of the
-last window (mm / 100), peak intensity of the coming window (mm/h / 100), and
-the window length in hours.  Targets: 10 x (depth change) and 10 x (window
-maximum above the new depth).
+Node inputs (12 features, padded to 64): depth h, momenta hu and hv, the
+window maximum depth (all x10: m -> dm, m^2/s -> 0.1 m^2/s), bed relative to
+the mesh mean, Manning n (x10), infiltration state (the fraction of the
+Horton capacity above its floor, 1 - wet-time decay; 0 without
+infiltration), exterior-boundary flag, rain depth of the coming and of the
+last window (mm / 100), peak intensity of the coming window (mm/h / 100),
+and the window length in hours.  Outputs: 10 x (depth change), 10 x (window
+maximum above the new depth), 10 x the new hu and hv.
 """
 
 from __future__ import annotations
@@ -29,13 +31,17 @@ from . import ops
 from .model import FIN, FOUT, MPNN, DualGraph
 
 SCALE = 10.0
+N_OUT = 4
+THRESHOLD_M = 0.05
 
 
 @dataclass
 class Trajectory:
     times_s: np.ndarray     # snapshot times
-    h: np.ndarray           # [n_snap, C]
-    hmax: np.ndarray        # [n_snap, C] window maxima
+    h: object               # [n_snap, C] device tensors
+    hmax: object            # [n_snap, C] window maxima
+    hu: object              # [n_snap, C]
+    hv: object              # [n_snap, C]
     storm: object           # RainfallEvent
     duration_s: float
 
@@ -43,22 +49,21 @@ class Trajectory:
 class MeshFeatures:
     """Static per-cell inputs and the dual graph of one mesh (device-resident)."""
 
-    def __init__(self, topo, device: str = "cuda"):
+    def __init__(self, topo, device: str = "cuda", infiltration_state=None):
         import torch
 
         self.topo = topo
         self.C = int(topo.cell_count)
         bed = np.asarray(topo.bed_elevation_m, np.float64)
         area = np.asarray(topo.cell_area_m2, np.float64)
-        cl = np.asarray(topo.characteristic_length_m, np.float64)
         boundary = np.zeros(self.C, np.float32)
         right = np.asarray(topo.edge_right_cell)
         boundary[np.asarray(topo.edge_left_cell)[right < 0]] = 1.0
         st = np.zeros((self.C, FIN), np.float32)
-        st[:, 3] = bed - bed.mean()
-        st[:, 4] = 10.0 * np.asarray(topo.manning_n, np.float64)
-        st[:, 5] = np.log(area) - np.log(area).mean()
-        st[:, 6] = cl / cl.mean()
+        st[:, 4] = bed - bed.mean()
+        st[:, 5] = 10.0 * np.asarray(topo.manning_n, np.float64)
+        if infiltration_state is not None:
+            st[:, 6] = np.asarray(infiltration_state, np.float32)
         st[:, 7] = boundary
         self.area = area.astype(np.float32)
         self.active = np.asarray(topo.active_mask) > 0 if topo.active_mask is not None else np.ones(self.C, bool)
@@ -67,20 +72,35 @@ class MeshFeatures:
         self.static = torch.as_tensor(st, device=device)
         self.active_dev = torch.as_tensor(self.active, device=device)
 
-    def inputs(self, h, h_prev, hmax, rain_next_mm, peak_next_mmhr, rain_prev_mm, window_h):
-        """bf16 [C, 64] network inputs from device depth vectors and window scalars."""
+    def inputs(self, h, hu, hv, hmax, rain_next_mm, peak_next_mmhr, rain_prev_mm, window_h):
+        """bf16 [C, 64] network inputs from device state vectors and window scalars."""
 
         import torch
 
         x = self.static.clone()
         x[:, 0] = SCALE * h
-        x[:, 1] = SCALE * h_prev
-        x[:, 2] = SCALE * hmax
+        x[:, 1] = SCALE * hu
+        x[:, 2] = SCALE * hv
+        x[:, 3] = SCALE * hmax
         x[:, 8] = rain_next_mm / 100.0
         x[:, 9] = rain_prev_mm / 100.0
         x[:, 10] = peak_next_mmhr / 100.0
         x[:, 11] = window_h
         return x.to(torch.bfloat16).contiguous()
+
+
+def advance(y, h, act):
+    """The state after a window from the network outputs y [C, >=4] and the
+    depth h at its start: (h, hmax, hu, hv), dry and inactive cells zeroed."""
+
+    import torch
+
+    hn = torch.clamp(h + y[:, 0] / SCALE, min=0.0) * act
+    hmn = torch.maximum(hn + torch.clamp(y[:, 1], min=0.0) / SCALE, torch.maximum(h, hn)) * act
+    wet = (hn > 1.0e-4) & act
+    hun = torch.where(wet, y[:, 2] / SCALE, torch.zeros_like(hn))
+    hvn = torch.where(wet, y[:, 3] / SCALE, torch.zeros_like(hn))
+    return hn, hmn, hun, hvn
 
 
 def rain_window(event, t0_s: float, t1_s: float) -> tuple[float, float]:
@@ -103,10 +123,12 @@ def windows(duration_s: float) -> list[tuple[float, float]]:
 
 
 # ------------------------------------------------------------------ data
-def solve_members(city, cfg, storms, durations_s, batch_size: int = 64, shape=None, device: str = "cuda"):
-    """Solver trajectories (hourly snapshots + window maxima, kept on the
-    device) of storms on one mesh, batched; returns (trajectories, solver
-    seconds, scenario hours)."""
+def solve_members(city, cfg, storms, durations_s, batch_size: int = 64, shape=None, device: str = "cuda",
+                  stream=None):
+    """Solver trajectories (hourly snapshots, window maxima and momenta, kept
+    on the device) of storms on one mesh, batched; returns (trajectories,
+    solver seconds, scenario hours).  With `stream` the solver runs on that
+    stream (and only it is synchronised), so other work can overlap it."""
 
     import torch
 
@@ -114,18 +136,19 @@ def solve_members(city, cfg, storms, durations_s, batch_size: int = 64, shape=No
 
     out = []
     seconds = 0.0
+    sync = stream.synchronize if stream is not None else torch.cuda.synchronize
     for k0 in range(0, len(storms), batch_size):
         members = [Member(city, storms[k], cfg, durations_s[k]) for k in range(k0, min(len(storms), k0 + batch_size))]
         with BatchSolver(members, shape=shape) as b:
-            torch.cuda.synchronize()
+            sync()
             t = time.perf_counter()
-            b.run()
-            torch.cuda.synchronize()
+            b.run(stream=stream)
+            sync()
             seconds += time.perf_counter() - t
             for j, m in enumerate(members):
-                ts, h, hm = b.snapshots(j)
-                out.append(Trajectory(ts, torch.as_tensor(h, device=device), torch.as_tensor(hm, device=device),
-                                      m.rainfall, m.duration_s))
+                ts, h, hm, hu, hv = b.snapshots(j, momentum=True)
+                dev = lambda a: torch.as_tensor(a, device=device)  # noqa: E731
+                out.append(Trajectory(ts, dev(h), dev(hm), dev(hu), dev(hv), m.rainfall, m.duration_s))
     return out, seconds, float(sum(durations_s)) / 3600.0
 
 
@@ -144,33 +167,60 @@ def transitions(tr: Trajectory):
     return out
 
 
-def sample_tensors(mf: MeshFeatures, tr: Trajectory, w):
-    """(inputs bf16 [C, 64], targets fp32 [C, 2]) of one training window."""
+def sample_tensors(mf: MeshFeatures, tr: Trajectory, w, state=None):
+    """(inputs bf16 [C, 64], targets fp32 [C, 4], target depths for the loss
+    weights [C, 2]) of one training window; `state` = (h, hu, hv, hmax) at its
+    start replaces the solver's (the network's own prediction)."""
 
     import torch
 
     j, rn, pk, rp, wh = w
-    h = tr.h[j]
-    hp = tr.h[j - 1] if j > 0 else h
-    hm = tr.hmax[j] if j > 0 else h
-    x = mf.inputs(h, hp, hm, rn, pk, rp, wh)
-    y = torch.stack([SCALE * (tr.h[j + 1] - h), SCALE * (tr.hmax[j + 1] - tr.h[j + 1])], dim=1).contiguous()
-    return x, y
+    if state is None:
+        h, hu, hv = tr.h[j], tr.hu[j], tr.hv[j]
+        hm = tr.hmax[j] if j > 0 else h
+    else:
+        h, hu, hv, hm = state
+    x = mf.inputs(h, hu, hv, hm, rn, pk, rp, wh)
+    y = torch.stack([SCALE * (tr.h[j + 1] - h), SCALE * (tr.hmax[j + 1] - tr.h[j + 1]), SCALE * tr.hu[j + 1],
+                     SCALE * tr.hv[j + 1]], dim=1).contiguous()
+    return x, y, torch.stack([tr.h[j + 1], tr.hmax[j + 1]], dim=1)
 
 
 # ------------------------------------------------------------------ training
+CHANNEL_WEIGHTS = (1.0, 1.0, 0.5, 0.5)
+
+
+def loss_weights(mf: MeshFeatures, depths, extent_weight: float):
+    """Per-cell, per-output loss weights: active cells; the depth and window
+    maximum channels weigh cells near the 0.05 m extent threshold
+    1 + extent_weight x exp(-((d - 0.05) / 0.025)^2) of their target depth d."""
+
+    import torch
+
+    act = mf.active_dev[:, None].float()
+    w = torch.tensor(CHANNEL_WEIGHTS, device=mf.device)[None, :].repeat(mf.C, 1)
+    if extent_weight > 0.0:
+        near = 1.0 + extent_weight * torch.exp(-((depths - THRESHOLD_M) / 0.025) ** 2)
+        w[:, :2] = w[:, :2] * near
+    return w * act
+
+
 def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: float = 1e-3, seed: int = 0,
-          log=None, max_seconds: float | None = None):
-    """Full-graph steps over every window of every trajectory; MSE on active cells."""
+          log=None, max_seconds: float | None = None, extent_weight: float = 3.0, pushforward: float = 0.5):
+    """Full-graph steps over every window of every trajectory; weighted MSE on
+    active cells.  From the second epoch, a window after the first starts
+    with probability `pushforward` from the network's own one-window
+    prediction (from the solver's state a window earlier) instead of the
+    solver's state, so the network learns to correct its own errors in a
+    rollout."""
 
     import torch
 
     rng = np.random.default_rng(seed)
     g = mf.graph
-    mask = mf.active_dev[:, None].float()
-    n_act = float(mask.sum().item()) * 2.0
     samples = [(tr, w) for tr in trajectories for w in transitions(tr)]
     dy = torch.zeros(g.C, FOUT, device=mf.device)
+    act = mf.active_dev
     history = []
     steps = epochs * len(samples)
     k = 0
@@ -179,11 +229,22 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
         total = torch.zeros((), device=mf.device)
         for i in rng.permutation(len(samples)):
             rate = lr * 0.5 * (1.0 + math.cos(math.pi * k / max(steps, 1)))  # cosine decay
-            x, yt = sample_tensors(mf, *samples[i])
+            tr, w = samples[i]
+            state = None
+            if ep > 0 and w[0] > 0 and rng.random() < pushforward:
+                j = w[0] - 1
+                xp, _, _ = sample_tensors(mf, tr, transitions(tr)[j])
+                with torch.no_grad():
+                    yp = model.forward(g, xp, train=False)
+                    hn, hmn, hun, hvn = advance(yp, tr.h[j], act)
+                state = (hn.clone(), hun.clone(), hvn.clone(), hmn.clone())
+            x, yt, depths = sample_tensors(mf, tr, w, state)
+            wts = loss_weights(mf, depths, extent_weight)
+            norm = wts.sum()
             y = model.forward(g, x)
-            diff = (y[:, :2] - yt) * mask
-            total += (diff * diff).sum() / n_act
-            dy[:, :2] = diff * (2.0 / n_act)
+            diff = y[:, :N_OUT] - yt
+            total += (wts * diff * diff).sum() / norm
+            dy[:, :N_OUT] = wts * diff * (2.0 / norm)
             model.zero_grad()
             model.backward(g, x, dy)
             model.step(rate)
@@ -207,18 +268,17 @@ def rollout(model: MPNN, mf: MeshFeatures, storm, duration_s: float):
     g = mf.graph
     act = mf.active_dev
     h = torch.zeros(mf.C, device=mf.device)
-    hp, hm = h.clone(), h.clone()
+    hu, hv, hm = h.clone(), h.clone(), h.clone()
     rp = 0.0
     ends, hs, hms = [], [], []
     for t0, t1 in windows(duration_s):
         rn, pk = rain_window(storm, t0, t1)
-        y = model.forward(g, mf.inputs(h, hp, hm, rn, pk, rp, (t1 - t0) / 3600.0), train=False)
-        hn = torch.clamp(h + y[:, 0] / SCALE, min=0.0) * act
-        hmn = torch.maximum(hn + torch.clamp(y[:, 1], min=0.0) / SCALE, torch.maximum(h, hn)) * act
+        y = model.forward(g, mf.inputs(h, hu, hv, hm, rn, pk, rp, (t1 - t0) / 3600.0), train=False)
+        hn, hmn, hun, hvn = advance(y, h, act)
         ends.append(t1)
         hs.append(hn)
         hms.append(hmn)
-        hp, h, hm, rp = h, hn, hmn, rn
+        h, hu, hv, hm, rp = hn, hun, hvn, hmn, rn
     return np.asarray(ends), torch.stack(hs).cpu().numpy(), torch.stack(hms).cpu().numpy()
 
 
@@ -244,7 +304,7 @@ def rollout_batch(model: MPNN, mf: MeshFeatures, storms, durations_s, copies: in
         wins = [windows(durations_s[i]) for i in idx]
         n_w = max(len(w) for w in wins)
         h = torch.zeros(B * mf.C, device=mf.device)
-        hp, hm = h.clone(), h.clone()
+        hu, hv, hm = h.clone(), h.clone(), h.clone()
         rp = np.zeros(B)
         hs, hms = [], []
         for w in range(n_w):
@@ -256,21 +316,42 @@ def rollout_batch(model: MPNN, mf: MeshFeatures, storms, durations_s, copies: in
             col = torch.as_tensor(sc, device=mf.device).repeat_interleave(mf.C, dim=0)
             x = static.clone()
             x[:, 0] = SCALE * h
-            x[:, 1] = SCALE * hp
-            x[:, 2] = SCALE * hm
+            x[:, 1] = SCALE * hu
+            x[:, 2] = SCALE * hv
+            x[:, 3] = SCALE * hm
             x[:, 8:12] = col[:, :4]
             y = model.forward(g, x.to(torch.bfloat16).contiguous(), train=False)
-            hn = torch.clamp(h + y[:, 0] / SCALE, min=0.0) * act
-            hmn = torch.maximum(hn + torch.clamp(y[:, 1], min=0.0) / SCALE, torch.maximum(h, hn)) * act
+            hn, hmn, hun, hvn = advance(y, h, act)
             hs.append(hn.view(B, mf.C))
             hms.append(hmn.view(B, mf.C))
-            hp, h, hm, rp = h, hn, hmn, sc[:, 4]
+            h, hu, hv, hm, rp = hn, hun, hvn, hmn, sc[:, 4]
         H = torch.stack(hs, 1).cpu().numpy()
         HM = torch.stack(hms, 1).cpu().numpy()
         for b, i in enumerate(idx):
             n = len(wins[b])
             out[i] = (np.asarray([w[1] for w in wins[b]]), H[b, :n], HM[b, :n])
     return out
+
+
+def ensemble_rollouts(models, mf: MeshFeatures, storms, durations_s, copies: int = 32):
+    """Rollouts of every member by each network: (mean prediction (ends, h,
+    hmax) per member, disagreement per member = RMS over windows and active
+    cells of the networks' window-maximum spread about their mean)."""
+
+    runs = [rollout_batch(m, mf, storms, durations_s, copies=copies) for m in models]
+    act = mf.active
+    preds, spread = [], []
+    for i in range(len(storms)):
+        ends = runs[0][i][0]
+        hs = np.mean([r[i][1] for r in runs], axis=0)
+        hms = np.mean([r[i][2] for r in runs], axis=0)
+        preds.append((ends, hs, hms))
+        if len(runs) > 1:
+            dev = np.stack([r[i][2][:, act] for r in runs]) - hms[None, :, act]
+            spread.append(float(np.sqrt(np.mean(dev ** 2))))
+        else:
+            spread.append(0.0)
+    return preds, np.asarray(spread)
 
 
 # ------------------------------------------------------------------ scoring
@@ -295,12 +376,26 @@ def score(mf: MeshFeatures, pred, tr: Trajectory, threshold: float = 0.05) -> di
     return {"rmse_h_m": rm_h, "rmse_hmax_m": rm_max, "csi": csi, "volume_error": (vp - vs) / max(abs(vs), 1.0)}
 
 
-def flags(mf: MeshFeatures, storm, pred, limits: dict) -> bool:
-    """Members the surrogate should not be trusted on: storms outside the
-    training range (peak or total depth), or a predicted envelope deeper than
-    anything seen in training."""
+def flags(spread: np.ndarray, threshold: float) -> np.ndarray:
+    """Members the surrogate should not be trusted on: the networks of the
+    ensemble disagree on the window maxima by more than `threshold` (RMS, m),
+    a level calibrated on held-out training storms (calibrate_flags)."""
 
-    depth = float(np.sum(np.asarray(storm.intensity_mmhr) * (np.asarray(storm.end_min) - np.asarray(storm.start_min))) / 60.0)
-    peak = float(np.max(storm.intensity_mmhr))
-    deepest = float(pred[2].max())
-    return peak > limits["peak_mmhr"] or depth > limits["depth_mm"] or deepest > limits["max_depth_m"]
+    return np.asarray(spread) > threshold
+
+
+def calibrate_flags(spread: np.ndarray, errors: np.ndarray, flag_fraction: float = 0.04) -> dict:
+    """Flag threshold from held-out training storms: the disagreement level
+    above which the `flag_fraction` most uncertain members lie; also reports
+    how well disagreement ranks the true window-maximum errors there."""
+
+    spread = np.asarray(spread, np.float64)
+    errors = np.asarray(errors, np.float64)
+    thr = float(np.quantile(spread, 1.0 - flag_fraction)) if spread.size else float("inf")
+    rank = lambda a: np.argsort(np.argsort(a))  # noqa: E731
+    rho = float(np.corrcoef(rank(spread), rank(errors))[0, 1]) if spread.size > 2 else float("nan")
+    sel = spread > thr
+    return {"threshold_m": thr, "flag_fraction": flag_fraction, "spearman_spread_vs_error": rho,
+            "validation_members": int(spread.size),
+            "mean_error_flagged_m": float(errors[sel].mean()) if sel.any() else None,
+            "mean_error_accepted_m": float(errors[~sel].mean()) if (~sel).any() else None}

@@ -137,11 +137,30 @@ def test_surrogate_trains_and_screens_small_ensemble():
     native.load()
     if native.device_count() < 1:
         pytest.skip("no CUDA device")
-    res = experiment.run(grid_n=16, n_train=48, n_eval=24, seed=5, epochs=30, lr=2e-3, n_layers=4,
-                         plain_sample=4, duration_cap_h=2.0, log=lambda *_: None, baselines=True)
-    loss = res["train"]["loss"]
-    assert loss[-1] < 0.5 * loss[0]
+    res = experiment.run(grid_n=16, n_train=56, n_eval=24, seed=5, epochs=30, lr=2e-3, n_layers=4,
+                         plain_sample=4, duration_cap_h=2.0, log=lambda *_: None, baselines=True, n_val=8,
+                         flag_fraction=0.25)
+    for loss in res["train"]["loss"]:  # one history per network of the ensemble
+        assert loss[-1] < 0.5 * loss[0]
     acc = res["surrogate_accepted"]
     assert acc is not None and acc["rmse_hmax_m"] < 0.10
     trained = float(np.mean([acc["rmse_hmax_m"]]))
     assert trained < 0.7 * res["no_change"] and trained < 0.7 * res["untrained"]
+    # the two networks' disagreement flags members, and every flagged member is re-solved and scored
+    assert res["ensemble_networks"] == 2 and res["calibration"]["validation_members"] == 8
+    assert res["flagged"] >= 1 and res["surrogate_flagged"]["members"] == res["flagged"]
+    assert res["re_solved"] >= res["flagged"]
+
+
+def test_flag_calibration_on_held_out_storms():
+    from floodgb.surrogate.pipeline import calibrate_flags, flags
+
+    rng = np.random.default_rng(3)
+    spread = rng.uniform(0.0, 0.02, 100)
+    errors = 0.01 + 2.0 * spread + rng.normal(0.0, 1e-3, 100)  # disagreement tracks the true error
+    cal = calibrate_flags(spread, errors, flag_fraction=0.1)
+    f = flags(spread, cal["threshold_m"])
+    assert 8 <= f.sum() <= 11
+    assert cal["spearman_spread_vs_error"] > 0.9
+    assert cal["mean_error_flagged_m"] > cal["mean_error_accepted_m"]
+    assert not flags(np.zeros(5), cal["threshold_m"]).any()
