@@ -28,6 +28,8 @@
 // millimetre-scale head differences exact at 200 m elevations; node storage
 // volume is a float-float pair so small exchanges are not lost against large
 // stored volumes.  No FP64 arithmetic is used on this path.
+#include <algorithm>
+
 #include "fl_device.cuh"
 
 namespace fl {
@@ -304,7 +306,63 @@ __device__ __forceinline__ void group_item(const NetArgs &a, const StepCtrl &s, 
     }
 }
 
-__global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs a, int slot) {
+// Ensemble members: a batched launch runs member blockIdx.y; these move the
+// per-member pointers of the arguments to that member's arrays (the static
+// tables are shared).  A single run uses the arguments as they are.
+__device__ __forceinline__ NodeArgs member_args(NodeArgs a, int m) {
+    const MemberStrides &z = a.ms;
+    a.state0 += m * z.cells;
+    a.state1 += m * z.cells;
+    a.capsur += m * z.inlets;
+    a.Va += m * z.nodes;
+    a.Vb += m * z.nodes;
+    a.inl.Va += m * z.nodes;
+    a.ctrl += 2 * m;
+    a.ledger += m * z.led1;
+    return a;
+}
+
+__device__ __forceinline__ LinkArgs member_args(LinkArgs a, int m) {
+    const MemberStrides &z = a.ms;
+    a.Vb += m * z.nodes;
+    a.Q0 += m * z.links;
+    a.Q1 += m * z.links;
+    a.T += m * z.links;
+    a.ctrl += 2 * m;
+    return a;
+}
+
+__device__ __forceinline__ DonorArgs member_args(DonorArgs a, int m) {
+    const MemberStrides &z = a.ms;
+    a.Vb += m * z.nodes;
+    a.T += m * z.links;
+    a.fac += m * z.nodes;
+    a.ctrl += 2 * m;
+    return a;
+}
+
+__device__ __forceinline__ NetArgs member_args(NetArgs a, int m) {
+    const MemberStrides &z = a.ms;
+    a.capsur += m * z.inlets;
+    a.T += m * z.links;
+    a.fac += m * z.nodes;
+    a.state0 += m * z.cells;
+    a.state1 += m * z.cells;
+    a.Vb += m * z.nodes;
+    a.Va += m * z.nodes;
+    a.Q0 += m * z.links;
+    a.Q1 += m * z.links;
+    a.wet += m * z.cells;
+    a.snap_h += m * z.snap_h;
+    a.snap_v += m * z.snap_v;
+    a.ctrl += 2 * m;
+    a.ledger += m * z.led2;
+    return a;
+}
+
+template <bool MEM>
+__global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs a0, int slot) {
+    const NodeArgs a = MEM ? member_args(a0, (int)blockIdx.y) : a0;
     pdl_launch_dependents();
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = n < a.N;
@@ -319,7 +377,9 @@ __global__ void __launch_bounds__(128) k_nodes(const __grid_constant__ NodeArgs 
 
 // Link l: the transfer volume from the end volumes after the inlet exchange
 // (all inputs loaded before the step record; the flow of the step's parity).
-__global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a, int slot) {
+template <bool MEM>
+__global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs a0, int slot) {
+    const LinkArgs a = MEM ? member_args(a0, (int)blockIdx.y) : a0;
     pdl_launch_dependents();
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     const bool in = l < a.L;
@@ -348,7 +408,9 @@ __global__ void __launch_bounds__(128) k_links(const __grid_constant__ LinkArgs 
 
 // The donor factor depends on nothing the step record selects: it is formed
 // while the record loads and stored only on an active step.
-__global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs a, int slot) {
+template <bool MEM>
+__global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs a0, int slot) {
+    const DonorArgs a = MEM ? member_args(a0, (int)blockIdx.y) : a0;
     pdl_launch_dependents();
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const StepCtrl s = a.ctrl[slot];
@@ -360,7 +422,9 @@ __global__ void __launch_bounds__(128) k_donor(const __grid_constant__ DonorArgs
     a.fac[n] = fac;
 }
 
-__global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs a, int slot) {
+template <bool MEM>
+__global__ void __launch_bounds__(128) k_network(const __grid_constant__ NetArgs a0, int slot) {
+    const NetArgs a = MEM ? member_args(a0, (int)blockIdx.y) : a0;
     pdl_launch_dependents();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int4 gr = g < a.G ? a.grp[g] : make_int4(-1, -1, 0, 0);
@@ -520,7 +584,9 @@ int node_blocks(int32_t N) { return (N + 127) / 128 > 0 ? (N + 127) / 128 : 1; }
 int network_blocks(int32_t G) { return (G + 127) / 128 > 0 ? (G + 127) / 128 : 1; }
 
 cudaError_t launch_nodes(const NodeArgs &a, int slot, cudaStream_t stream) {
-    k_nodes<<<node_blocks(a.N), 128, 0, stream>>>(a, slot);
+    const dim3 grid((unsigned)node_blocks(a.N), (unsigned)std::max(a.ms.n, 1));
+    if (a.ms.n > 1) k_nodes<true><<<grid, 128, 0, stream>>>(a, slot);
+    else k_nodes<false><<<grid, 128, 0, stream>>>(a, slot);
     return cudaGetLastError();
 }
 
@@ -531,7 +597,7 @@ template <class Args>
 static cudaError_t launch_dependent(void (*kernel)(Args, int), int blocks, const Args &a, int slot,
                                     cudaStream_t stream) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.gridDim = dim3((unsigned)blocks, (unsigned)std::max(a.ms.n, 1));
     cfg.blockDim = dim3(128);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = stream;
@@ -544,15 +610,15 @@ static cudaError_t launch_dependent(void (*kernel)(Args, int), int blocks, const
 }
 
 cudaError_t launch_links(const LinkArgs &a, int slot, cudaStream_t stream) {
-    return launch_dependent(k_links, link_blocks(a.L), a, slot, stream);
+    return launch_dependent(a.ms.n > 1 ? k_links<true> : k_links<false>, link_blocks(a.L), a, slot, stream);
 }
 
 cudaError_t launch_donor(const DonorArgs &a, int slot, cudaStream_t stream) {
-    return launch_dependent(k_donor, node_blocks(a.N), a, slot, stream);
+    return launch_dependent(a.ms.n > 1 ? k_donor<true> : k_donor<false>, node_blocks(a.N), a, slot, stream);
 }
 
 cudaError_t launch_network(const NetArgs &a, int slot, cudaStream_t stream) {
-    return launch_dependent(k_network, network_blocks(a.G), a, slot, stream);
+    return launch_dependent(a.ms.n > 1 ? k_network<true> : k_network<false>, network_blocks(a.G), a, slot, stream);
 }
 
 }  // namespace fl

@@ -110,6 +110,19 @@ constexpr uint32_t NL_NODE_MASK = 0x3FFFFFFFu;
 constexpr uint32_t NL_FROM = 1u << 30;
 constexpr uint32_t NL_TO = 1u << 31;
 
+// Ensemble members on one mesh: every per-member array is laid out member
+// after member with these strides (elements); a batched drainage launch runs
+// member blockIdx.y.  A single run has n = 1 and uses none of them.
+struct MemberStrides {
+    int32_t n;                    // members (the launch's gridDim.y)
+    int64_t cells;                // state / wet: Cp
+    int64_t nodes;                // Va, Vb, fac
+    int64_t links;                // Q, T
+    int64_t inlets;               // capsur
+    int64_t led1, led2;           // drainage ledger slots
+    int64_t snap_h, snap_v;       // snapshot arrays: max_snapshots x C, max_snapshots x N
+};
+
 // What k_nodes needs to evaluate the inlet requests of a node's inlets.
 struct InletReqView {
     const int32_t *in_node;       // [I] cell order
@@ -235,6 +248,7 @@ struct NodeArgs {
     StepCtrl *ctrl;
     float2 *ledger;               // [warps * D1_TERMS] float-float running sums
     int32_t N;
+    MemberStrides ms;
 };
 
 // k_links: one thread per link, its transfer volume from the end volumes.
@@ -248,6 +262,7 @@ struct LinkArgs {
     StepCtrl *ctrl;
     int32_t L;
     float g, wave_speed;
+    MemberStrides ms;
 };
 
 // k_donor: one thread per node, its donor limit factor.
@@ -259,6 +274,7 @@ struct DonorArgs {
     float *fac;
     StepCtrl *ctrl;
     int32_t N;
+    MemberStrides ms;
 };
 
 // k_network: one thread per group (a surface cell with the nodes that overflow
@@ -294,6 +310,7 @@ struct NetArgs {
     const int32_t *tcell;         // [U] table cells (new order, ascending)
     double *s2;                   // [U] fallback return depth of table cells that are group cells
     int32_t U;
+    MemberStrides ms;
 };
 
 // Weighted surcharge return into the table cells, after k_network:

@@ -145,8 +145,53 @@ struct FlSolver {
     bool has_table() const { return sur.U > 0; }
     bool has_recharge() const { return rch.U > 0; }
     int launches_per_step() const {
-        return (li_mode ? 2 : 1) + (has_drain() ? 4 : 0) + (has_table() ? 1 : 0) + (has_inflow() ? 1 : 0) +
+        return (li_mode ? 2 : 1) * members + (has_drain() ? 4 : 0) + (has_table() ? 1 : 0) + (has_inflow() ? 1 : 0) +
                (has_recharge() ? 1 : 0);
+    }
+
+    // Ensemble members (fl_create_members; 1 for fl_create): every per-member
+    // array is allocated member after member, starting at the pointers in
+    // `mb`; the fields above (state, wet, ctrl, run, run_h, snapshots,
+    // ledgers, dt_out, vol_out, Va, Vb, Q, hy) address the selected member.
+    int32_t members = 1, cur = 0;
+    struct MemberBase {
+        float4 *state[2] = {nullptr, nullptr};
+        float *wet = nullptr;
+        StepCtrl *ctrl = nullptr;
+        RunCtrl *run = nullptr, *run_h = nullptr;
+        double *snap_t = nullptr;
+        float *snap_h = nullptr, *snap_hu = nullptr, *snap_hv = nullptr, *snap_v = nullptr;
+        float2 *led_s = nullptr, *led_1 = nullptr, *led_2 = nullptr;
+        double *dt_out = nullptr, *vol_out = nullptr;
+        float2 *Va = nullptr, *Vb = nullptr;
+        float *Q[2] = {nullptr, nullptr};
+    } mb;
+    std::vector<HyetoView> hys;  // [members]
+    size_t snap_stride_h() const { return (size_t)params.max_snapshots * (size_t)C; }
+    size_t snap_stride_v() const { return (size_t)params.max_snapshots * (size_t)(N > 0 ? N : 1); }
+    void select(int32_t m) {
+        cur = m;
+        for (int b = 0; b < 2; ++b) {
+            state[b] = mb.state[b] + (size_t)m * Cp;
+            Q[b] = mb.Q[b] ? mb.Q[b] + (size_t)m * NL : nullptr;
+        }
+        wet = mb.wet + (size_t)m * Cp;
+        ctrl = mb.ctrl + 2 * (size_t)m;
+        run = mb.run + m;
+        run_h = mb.run_h + m;
+        snap_t = mb.snap_t + (size_t)m * params.max_snapshots;
+        snap_h = mb.snap_h + m * snap_stride_h();
+        snap_hu = mb.snap_hu + m * snap_stride_h();
+        snap_hv = mb.snap_hv + m * snap_stride_h();
+        snap_v = mb.snap_v + m * snap_stride_v();
+        led_s = mb.led_s + (size_t)m * n_led_s;
+        led_1 = mb.led_1 ? mb.led_1 + (size_t)m * n_led_1 : nullptr;
+        led_2 = mb.led_2 ? mb.led_2 + (size_t)m * n_led_2 : nullptr;
+        dt_out = mb.dt_out + m;
+        vol_out = mb.vol_out + 2 * (size_t)m;
+        Va = mb.Va ? mb.Va + (size_t)m * N : nullptr;
+        Vb = mb.Vb ? mb.Vb + (size_t)m * N : nullptr;
+        hy = hys[m];
     }
 
     // Drainage tables live in one arena so one L2 access-policy window can
@@ -193,11 +238,42 @@ static int push_run(FlSolver *s, cudaStream_t st) {
     return FL_OK;
 }
 
-// One step: [CFL reduction + plan] surface [inlets network]
+// The surface / CFL kernel arguments of member m: the solver's arguments
+// (the shared tables and settings) with that member's arrays.
+static SurfArgs surf_args(const FlSolver *s, int m) {
+    SurfArgs a = s->sa;
+    a.state0 = s->mb.state[0] + (size_t)m * s->Cp;
+    a.state1 = s->mb.state[1] + (size_t)m * s->Cp;
+    a.wet = s->mb.wet + (size_t)m * s->Cp;
+    a.ctrl = s->mb.ctrl + 2 * (size_t)m;
+    a.run = s->mb.run + m;
+    a.hy = s->hys[m];
+    a.ledger = s->mb.led_s + (size_t)m * s->n_led_s;
+    a.snap_h = s->mb.snap_h + m * s->snap_stride_h();
+    a.snap_hu = s->mb.snap_hu + m * s->snap_stride_h();
+    a.snap_hv = s->mb.snap_hv + m * s->snap_stride_h();
+    a.snap_t = s->mb.snap_t + (size_t)m * s->params.max_snapshots;
+    return a;
+}
+
+static DtArgs dt_args(const FlSolver *s, int m) {
+    DtArgs d = s->da;
+    d.state0 = s->mb.state[0] + (size_t)m * s->Cp;
+    d.state1 = s->mb.state[1] + (size_t)m * s->Cp;
+    d.ctrl = s->mb.ctrl + 2 * (size_t)m;
+    d.run = s->mb.run + m;
+    d.hy = s->hys[m];
+    d.snap_t = s->mb.snap_t + (size_t)m * s->params.max_snapshots;
+    return d;
+}
+
+// One step: [CFL reduction + plan] surface [inlets network], the CFL and
+// surface launches once per member, each drainage kernel once for all
+// members.
 static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStream_t st) {
     if (eval) {
-        FL_CUDA(launch_dt(s->da, s->dt_blocks, slot, 1, st));
-        g_launches++;
+        for (int m = 0; m < s->members; ++m) FL_CUDA(launch_dt(dt_args(s, m), s->dt_blocks, slot, 1, st));
+        g_launches += s->members;
     }
     if (s->has_inflow()) {
         FL_CUDA(launch_inflow(s->ext, slot, st));
@@ -207,8 +283,9 @@ static int launch_step(FlSolver *s, int slot, bool eval, bool plan_next, cudaStr
         FL_CUDA(launch_li(s->li, s->kind, slot, plan_next ? 1 : 0, s->sms, st));
         g_launches += 2;
     } else {
-        FL_CUDA(launch_surface(s->sa, s->kind, slot, plan_next ? 1 : 0, s->surf_grid, s->surf_smem, st));
-        g_launches++;
+        for (int m = 0; m < s->members; ++m)
+            FL_CUDA(launch_surface(surf_args(s, m), s->kind, slot, plan_next ? 1 : 0, s->surf_grid, s->surf_smem, st));
+        g_launches += s->members;
     }
     if (s->has_drain()) {
         FL_CUDA(launch_nodes(s->nd, slot, st));
@@ -302,7 +379,7 @@ static int capture_graph(FlSolver *s) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_error(FL_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
     // the launches above were captured, not executed
-    g_launches -= (int64_t)s->chunk * s->launches_per_step() + (s->chunk + interval - 1) / interval;
+    g_launches -= (int64_t)s->chunk * s->launches_per_step() + (int64_t)s->members * ((s->chunk + interval - 1) / interval);
     return FL_OK;
 }
 
@@ -397,9 +474,14 @@ FL_API void fl_destroy(FlSolver *s) {
     delete s;
 }
 
-static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcing,
+// forcings: M entries (the members' rainfall); the per-cell fields come from
+// forcings[0].
+static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcings, int32_t M,
                        const FlParams *params, int32_t device, FlSolver *s) {
+    const FlForcingDesc *forcing = forcings;
     if (!mesh || !forcing || !params) return set_error(FL_E_INVALID, "fl_create needs mesh, forcing and params");
+    if (M < 1 || M > 1024) return set_error(FL_E_INVALID, "members must be in [1, 1024], got %d", M);
+    s->members = M;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return set_error(FL_E_NO_DEVICE, "no CUDA device is visible; CPU fallback is disabled");
@@ -415,9 +497,15 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     if (forcing->kind == 1 && (!forcing->rain_multiplier || !forcing->horton_f0_mps || !forcing->horton_fc_mps ||
                                !forcing->horton_k_per_s))
         return set_error(FL_E_INVALID, "per-cell forcing needs rain_multiplier and Horton f0/fc/k arrays");
-    if (forcing->hyetograph_count < 0 || (forcing->hyetograph_count > 0 &&
-                                          (!forcing->hyeto_start_s || !forcing->hyeto_end_s || !forcing->hyeto_rate_mps)))
-        return set_error(FL_E_INVALID, "hyetograph arrays are missing");
+    for (int32_t m = 0; m < M; ++m) {
+        const FlForcingDesc &f = forcings[m];
+        if (f.hyetograph_count < 0 || (f.hyetograph_count > 0 && (!f.hyeto_start_s || !f.hyeto_end_s || !f.hyeto_rate_mps)))
+            return set_error(FL_E_INVALID, "hyetograph arrays of member %d are missing", m);
+    }
+    if (M > 1 && p.surface_step_mode != 0)
+        return set_error(FL_E_UNSUPPORTED, "ensemble members run the full_swe surface step only");
+    if (M > 1 && drain && drain->surcharge_entry_count > 0)
+        return set_error(FL_E_UNSUPPORTED, "ensemble members do not support the weighted surcharge table");
     s->device = device;
     FL_CUDA(cudaSetDevice(device));
     s->params = p;
@@ -461,37 +549,46 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         }
         if ((rc = s->upload(&horton, hz))) return rc;
     }
-    if ((rc = s->alloc(&s->wet, Cp))) return rc;
-    FL_CUDA(cudaMemset(s->wet, 0, sizeof(float) * Cp));
+    // per-member arrays (member after member)
+    const size_t Mz = (size_t)M;
+    if ((rc = s->alloc(&s->wet, Mz * Cp))) return rc;
+    FL_CUDA(cudaMemset(s->wet, 0, sizeof(float) * Mz * Cp));
     for (int b = 0; b < 2; ++b) {
-        if ((rc = s->alloc(&s->state[b], Cp))) return rc;
+        if ((rc = s->alloc(&s->state[b], Mz * Cp))) return rc;
     }
     {
         std::vector<float4> st0(Cp, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         for (int32_t i = 0; i < C; ++i) st0[i] = make_float4(0.0f, 0.0f, 0.0f, L.bed[i]);
-        FL_CUDA(cudaMemcpy(s->state[0], st0.data(), sizeof(float4) * Cp, cudaMemcpyHostToDevice));
-        FL_CUDA(cudaMemcpy(s->state[1], st0.data(), sizeof(float4) * Cp, cudaMemcpyHostToDevice));
+        for (size_t m = 0; m < Mz; ++m)
+            for (int b = 0; b < 2; ++b)
+                FL_CUDA(cudaMemcpy(s->state[b] + m * Cp, st0.data(), sizeof(float4) * Cp, cudaMemcpyHostToDevice));
     }
-    if ((rc = s->alloc(&s->ctrl, 2)) || (rc = s->alloc(&s->run, 1)) || (rc = s->alloc(&s->snap_t, p.max_snapshots)))
+    if ((rc = s->alloc(&s->ctrl, 2 * Mz)) || (rc = s->alloc(&s->run, Mz)) ||
+        (rc = s->alloc(&s->snap_t, Mz * p.max_snapshots)))
         return rc;
-    FL_CUDA(cudaMemset(s->ctrl, 0, sizeof(StepCtrl) * 2));
+    FL_CUDA(cudaMemset(s->ctrl, 0, sizeof(StepCtrl) * 2 * Mz));
     const size_t snap_cells = (size_t)p.max_snapshots * (size_t)C;
-    if ((rc = s->alloc(&s->snap_h, snap_cells)) || (rc = s->alloc(&s->snap_hu, snap_cells)) ||
-        (rc = s->alloc(&s->snap_hv, snap_cells)) || (rc = s->alloc(&s->snap_v, (size_t)p.max_snapshots * (s->N > 0 ? s->N : 1))))
+    const size_t snap_nodes = (size_t)p.max_snapshots * (s->N > 0 ? s->N : 1);
+    if ((rc = s->alloc(&s->snap_h, Mz * snap_cells)) || (rc = s->alloc(&s->snap_hu, Mz * snap_cells)) ||
+        (rc = s->alloc(&s->snap_hv, Mz * snap_cells)) || (rc = s->alloc(&s->snap_v, Mz * snap_nodes)))
         return rc;
-    // hyetograph
-    const int nh = forcing->hyetograph_count;
-    double *hy = nullptr;
-    if ((rc = s->alloc(&hy, 3 * (size_t)(nh > 0 ? nh : 1)))) return rc;
-    if (nh > 0) {
-        FL_CUDA(cudaMemcpy(hy, forcing->hyeto_start_s, sizeof(double) * nh, cudaMemcpyHostToDevice));
-        FL_CUDA(cudaMemcpy(hy + nh, forcing->hyeto_end_s, sizeof(double) * nh, cudaMemcpyHostToDevice));
-        FL_CUDA(cudaMemcpy(hy + 2 * nh, forcing->hyeto_rate_mps, sizeof(double) * nh, cudaMemcpyHostToDevice));
+    // hyetographs, one per member
+    s->hys.resize(M);
+    for (int32_t m = 0; m < M; ++m) {
+        const int nh = forcings[m].hyetograph_count;
+        double *hy = nullptr;
+        if ((rc = s->alloc(&hy, 3 * (size_t)(nh > 0 ? nh : 1)))) return rc;
+        if (nh > 0) {
+            FL_CUDA(cudaMemcpy(hy, forcings[m].hyeto_start_s, sizeof(double) * nh, cudaMemcpyHostToDevice));
+            FL_CUDA(cudaMemcpy(hy + nh, forcings[m].hyeto_end_s, sizeof(double) * nh, cudaMemcpyHostToDevice));
+            FL_CUDA(cudaMemcpy(hy + 2 * nh, forcings[m].hyeto_rate_mps, sizeof(double) * nh, cudaMemcpyHostToDevice));
+        }
+        s->hys[m].start_s = hy;
+        s->hys[m].end_s = hy + nh;
+        s->hys[m].rate = hy + 2 * nh;
+        s->hys[m].n = nh;
     }
-    s->hy.start_s = hy;
-    s->hy.end_s = hy + nh;
-    s->hy.rate = hy + 2 * nh;
-    s->hy.n = nh;
+    s->hy = s->hys[0];
     // scratch
     s->sa.n_tiles = (int32_t)L.tile_info.size();
     s->sa.e_cap = L.e_cap;
@@ -508,8 +605,8 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     s->dt_blocks = std::max(1, std::min(sms * 4, (C + 255) / 256));
     float *dt_partial = nullptr;
     unsigned int *counter = nullptr;
-    if ((rc = s->alloc(&dt_partial, s->dt_blocks)) || (rc = s->alloc(&counter, 1)) || (rc = s->alloc(&s->dt_out, 1)) ||
-        (rc = s->alloc(&s->vol_out, 2)) || (rc = s->alloc(&s->led_s, s->n_led_s)))
+    if ((rc = s->alloc(&dt_partial, s->dt_blocks)) || (rc = s->alloc(&counter, 1)) || (rc = s->alloc(&s->dt_out, Mz)) ||
+        (rc = s->alloc(&s->vol_out, 2 * Mz)) || (rc = s->alloc(&s->led_s, Mz * s->n_led_s)))
         return rc;
     FL_CUDA(cudaMemset(counter, 0, sizeof(unsigned int)));
     for (int b = 0; b < 3; ++b)
@@ -528,7 +625,10 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
                                  (size_t)(node_blocks(s->N) * 4 * D1_TERMS + network_blocks(s->G) * 4 * D2_TERMS) * 8 +
                                  (L.node_tstart.size() + L.node_tw.size()) * 4 + N * 8 +
                                  (L.tcell.size() + L.tcell_start.size()) * 4 + L.tcell_ent.size() * 8 +
-                                 L.tcell.size() * 8 + 64 * 256;
+                                 L.tcell.size() * 8 + 64 * 256 +
+                                 // the other members' node / link / inlet arrays and ledgers
+                                 (Mz - 1) * (N * (8 * 2 + 4) + NL * (4 * 3) + I * 8 +
+                                             (size_t)(node_blocks(s->N) * 4 * D1_TERMS + network_blocks(s->G) * 4 * D2_TERMS) * 8);
             void *q = nullptr;
             cudaError_t e = cudaMalloc(&q, bytes);
             if (e != cudaSuccess) return set_error(FL_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
@@ -551,23 +651,34 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
             (rc = s->upload(&lk0, L.lk0)) || (rc = s->upload(&lk1, L.lk1)) || (rc = s->upload(&lk2, L.lk2)) ||
             (rc = s->upload(&s->node_perm, L.node_perm)))
             return rc;
-        if ((rc = s->alloc(&s->Va, s->N)) || (rc = s->alloc(&s->Vb, s->N)) || (rc = s->alloc(&s->Q[0], s->NL)) ||
-            (rc = s->alloc(&s->Q[1], s->NL)) || (rc = s->alloc(&s->stage_n, s->N)))
+        const size_t MN = Mz * (size_t)s->N, ML = Mz * (size_t)std::max(s->NL, 1);
+        if ((rc = s->alloc(&s->Va, MN)) || (rc = s->alloc(&s->Vb, MN)) || (rc = s->alloc(&s->Q[0], ML)) ||
+            (rc = s->alloc(&s->Q[1], ML)) || (rc = s->alloc(&s->stage_n, s->N)))
             return rc;
-        FL_CUDA(cudaMemset(s->Va, 0, sizeof(float2) * s->N));
-        FL_CUDA(cudaMemset(s->Vb, 0, sizeof(float2) * s->N));
-        FL_CUDA(cudaMemset(s->Q[0], 0, sizeof(float) * std::max(s->NL, 1)));
-        FL_CUDA(cudaMemset(s->Q[1], 0, sizeof(float) * std::max(s->NL, 1)));
+        FL_CUDA(cudaMemset(s->Va, 0, sizeof(float2) * MN));
+        FL_CUDA(cudaMemset(s->Vb, 0, sizeof(float2) * MN));
+        FL_CUDA(cudaMemset(s->Q[0], 0, sizeof(float) * ML));
+        FL_CUDA(cudaMemset(s->Q[1], 0, sizeof(float) * ML));
         s->d1_blocks = node_blocks(s->N);
         s->d2_blocks = network_blocks(s->G);
         s->n_led_1 = (size_t)s->d1_blocks * 4 * D1_TERMS;
         s->n_led_2 = (size_t)s->d2_blocks * 4 * D2_TERMS;
         float *T, *fac;
         float2 *capsur;
-        if ((rc = s->alloc(&s->led_1, s->n_led_1)) || (rc = s->alloc(&s->led_2, s->n_led_2)) ||
-            (rc = s->alloc(&T, s->NL)) || (rc = s->alloc(&fac, s->N)) || (rc = s->alloc(&capsur, s->I)))
+        if ((rc = s->alloc(&s->led_1, Mz * s->n_led_1)) || (rc = s->alloc(&s->led_2, Mz * s->n_led_2)) ||
+            (rc = s->alloc(&T, ML)) || (rc = s->alloc(&fac, MN)) || (rc = s->alloc(&capsur, Mz * std::max(s->I, 1))))
             return rc;
-        FL_CUDA(cudaMemset(capsur, 0, sizeof(float2) * std::max(s->I, 1)));
+        FL_CUDA(cudaMemset(capsur, 0, sizeof(float2) * Mz * std::max(s->I, 1)));
+        MemberStrides ms{};
+        ms.n = M;
+        ms.cells = Cp;
+        ms.nodes = s->N;
+        ms.links = s->NL;
+        ms.inlets = s->I;
+        ms.led1 = (int64_t)s->n_led_1;
+        ms.led2 = (int64_t)s->n_led_2;
+        ms.snap_h = (int64_t)snap_cells;
+        ms.snap_v = (int64_t)snap_nodes;
         InletReqView &v = s->nd.inl;
         v.in_node = in_node;
         v.in_par = in_par;
@@ -590,6 +701,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         a.ctrl = s->ctrl;
         a.ledger = s->led_1;
         a.N = s->N;
+        a.ms = ms;
         LinkArgs &la = s->lk;
         la.link_from = lf;
         la.link_to = lt;
@@ -605,6 +717,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         la.L = s->NL;
         la.g = (float)p.gravity_mps2;
         la.wave_speed = drain->pressurized_wave_speed_mps;
+        la.ms = ms;
         DonorArgs &dn = s->dn;
         dn.node_link_start = nls;
         dn.nl = nl;
@@ -613,6 +726,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         dn.fac = fac;
         dn.ctrl = s->ctrl;
         dn.N = s->N;
+        dn.ms = ms;
         NetArgs &b = s->nw;
         b.grp = grp;
         b.kcell_start = kcell_start;
@@ -644,6 +758,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
         b.has_recharge = 0;
         b.table = 0;
         b.U = 0;
+        b.ms = ms;
         if (!L.node_tstart.empty()) {
             int32_t *tstart, *tcell, *tcs;
             float *tw;
@@ -844,26 +959,54 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     }
 
     // host side
-    FL_CUDA(cudaHostAlloc((void **)&s->run_h, sizeof(RunCtrl), cudaHostAllocDefault));
-    FL_CUDA(cudaHostAlloc((void **)&s->poll_h, 2 * sizeof(RunCtrl), cudaHostAllocDefault));
-    memset(s->run_h, 0, sizeof(RunCtrl));
+    FL_CUDA(cudaHostAlloc((void **)&s->run_h, Mz * sizeof(RunCtrl), cudaHostAllocDefault));
+    FL_CUDA(cudaHostAlloc((void **)&s->poll_h, 2 * Mz * sizeof(RunCtrl), cudaHostAllocDefault));
+    memset(s->run_h, 0, Mz * sizeof(RunCtrl));
     FL_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
     FL_CUDA(cudaEventCreateWithFlags(&s->ev[0], cudaEventDisableTiming));
     FL_CUDA(cudaEventCreateWithFlags(&s->ev[1], cudaEventDisableTiming));
     const int interval = p.cfl_update_interval_steps;
     s->chunk = interval % 2 == 0 ? interval : 2 * interval;
     while (s->chunk < 16) s->chunk *= 2;  // short CFL cycles: several per graph
+    // member 0's arrays start every per-member allocation
+    FlSolver::MemberBase &b0 = s->mb;
+    b0.state[0] = s->state[0];
+    b0.state[1] = s->state[1];
+    b0.wet = s->wet;
+    b0.ctrl = s->ctrl;
+    b0.run = s->run;
+    b0.run_h = s->run_h;
+    b0.snap_t = s->snap_t;
+    b0.snap_h = s->snap_h;
+    b0.snap_hu = s->snap_hu;
+    b0.snap_hv = s->snap_hv;
+    b0.snap_v = s->snap_v;
+    b0.led_s = s->led_s;
+    b0.led_1 = s->led_1;
+    b0.led_2 = s->led_2;
+    b0.dt_out = s->dt_out;
+    b0.vol_out = s->vol_out;
+    b0.Va = s->Va;
+    b0.Vb = s->Vb;
+    b0.Q[0] = s->Q[0];
+    b0.Q[1] = s->Q[1];
+    s->select(0);
     FL_CUDA(cudaDeviceSynchronize());
     return fl_reset_clock(s, nullptr);
 }
 
 FL_API int fl_create(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcing,
                      const FlParams *params, int32_t device, FlSolver **out) {
+    return fl_create_members(mesh, drain, forcing, 1, params, device, out);
+}
+
+FL_API int fl_create_members(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcings,
+                             int32_t n_members, const FlParams *params, int32_t device, FlSolver **out) {
     if (!out) return set_error(FL_E_INVALID, "out is NULL");
     *out = nullptr;
     FlSolver *s = new (std::nothrow) FlSolver();
     if (!s) return set_error(FL_E_NOMEM, "out of host memory");
-    int rc = create_impl(mesh, drain, forcing, params, device, s);
+    int rc = create_impl(mesh, drain, forcings, n_members, params, device, s);
     if (rc != FL_OK) {
         std::string msg = g_error;
         fl_destroy(s);
@@ -874,10 +1017,42 @@ FL_API int fl_create(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlF
     return FL_OK;
 }
 
+FL_API int fl_member_select(FlSolver *s, int32_t member) {
+    if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    if (member < 0 || member >= s->members)
+        return set_error(FL_E_INVALID, "member %d is out of range (%d members)", member, s->members);
+    s->select(member);
+    return FL_OK;
+}
+
+FL_API int fl_member_count(FlSolver *s, int32_t *members) {
+    if (!s || !members) return set_error(FL_E_INVALID, "solver or output is NULL");
+    *members = s->members;
+    return FL_OK;
+}
+
+static int reset_member_clock(FlSolver *s, cudaStream_t st);
+
 FL_API int fl_reset_clock(FlSolver *s, void *stream) {
     if (!s) return set_error(FL_E_INVALID, "solver is NULL");
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
+    const int32_t keep = s->cur;
+    for (int32_t m = 0; m < s->members; ++m) {
+        s->select(m);
+        const int rc = reset_member_clock(s, st);
+        if (rc) {
+            s->select(keep);
+            return rc;
+        }
+    }
+    s->select(keep);
+    s->slot = 0;
+    return FL_OK;
+}
+
+// The clock reset of the selected member.
+static int reset_member_clock(FlSolver *s, cudaStream_t st) {
     const int32_t parity = s->run_h ? s->run_h->parity : 0;
     RunCtrl r;
     memset(&r, 0, sizeof(r));
@@ -915,7 +1090,6 @@ FL_API int fl_reset_clock(FlSolver *s, void *stream) {
         FL_CUDA(cudaMemsetAsync(s->rch.led, 0, sizeof(float2) * 2 * (size_t)s->R, st));
     }
     FL_CUDA(cudaStreamSynchronize(st));
-    s->slot = 0;
     return FL_OK;
 }
 
@@ -992,10 +1166,96 @@ FL_API int fl_get_state(FlSolver *s, float *h, float *hu, float *hv, double *nod
     return FL_OK;
 }
 
+// fl_run with several members: every member runs to the end of the run, all
+// of them stepping together (each with its own dt) until the last one ends.
+static int run_members(FlSolver *s, double t_target_s, int64_t max_steps, cudaStream_t st) {
+    const int32_t M = s->members, keep = s->cur;
+    if (max_steps > 0 || t_target_s < s->params.duration_s)
+        return set_error(FL_E_UNSUPPORTED, "with several members fl_run runs every member to the end of the run "
+                                           "(t_target >= duration, no step cap)");
+    FL_CUDA(cudaMemcpyAsync(s->mb.run_h, s->mb.run, sizeof(RunCtrl) * M, cudaMemcpyDeviceToHost, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    int64_t step0 = -1;
+    for (int32_t m = 0; m < M; ++m) {
+        RunCtrl &r = s->mb.run_h[m];
+        if (r.error) {
+            s->select(m);
+            const int rc = error_code_message(s);
+            s->select(keep);
+            return rc;
+        }
+        if (r.t < r.final_t) {
+            if (step0 < 0) step0 = r.step;
+            else if (r.step != step0) return set_error(FL_E_UNSUPPORTED, "members are at different steps");
+        }
+        r.stop_t = r.final_t;
+        r.max_step = std::numeric_limits<int64_t>::max();
+    }
+    if (step0 < 0) return FL_OK;  // every member has ended
+    const int interval = s->params.cfl_update_interval_steps;
+    if (step0 % interval != 0)
+        return set_error(FL_E_UNSUPPORTED, "members resume at step %lld, not a multiple of the CFL interval",
+                         (long long)step0);
+    FL_CUDA(cudaMemcpyAsync(s->mb.run, s->mb.run_h, sizeof(RunCtrl) * M, cudaMemcpyHostToDevice, st));
+    // the first launch (a CFL step) plans every member's step from its run state
+    for (int32_t m = 0; m < M; ++m)
+        FL_CUDA(cudaMemsetAsync(&s->mb.ctrl[2 * m + s->slot], 0, sizeof(StepCtrl), st));
+    int rc = capture_graph(s);
+    if (rc) return rc;
+    int64_t launched = 0, last_total = -1;
+    int stalled = 0;
+    const int per_chunk = s->chunk * s->launches_per_step() + M * ((s->chunk + interval - 1) / interval);
+    while (true) {
+        FL_CUDA(cudaGraphLaunch(s->graph, st));
+        g_launches += per_chunk;
+        FL_CUDA(cudaMemcpyAsync(&s->poll_h[(launched & 1) * M], s->mb.run, sizeof(RunCtrl) * M,
+                                cudaMemcpyDeviceToHost, st));
+        FL_CUDA(cudaEventRecord(s->ev[launched & 1], st));
+        ++launched;
+        if (launched >= 2) {
+            FL_CUDA(cudaEventSynchronize(s->ev[launched & 1]));
+            const RunCtrl *p = &s->poll_h[(launched & 1) * M];
+            bool done = true, failed = false;
+            int64_t total = 0;
+            for (int32_t m = 0; m < M; ++m) {
+                failed = failed || p[m].error != 0;
+                if (p[m].t < p[m].stop_t) done = false;
+                total += p[m].step;
+            }
+            if (failed || done) break;
+            stalled = (total == last_total) ? stalled + 1 : 0;
+            last_total = total;
+            if (stalled >= 3) {
+                FL_CUDA(cudaStreamSynchronize(st));
+                return set_error(FL_E_CUDA, "device loop stopped advancing at %lld member steps", (long long)total);
+            }
+        }
+    }
+    s->slot = 0;
+    FL_CUDA(cudaMemcpyAsync(s->mb.run_h, s->mb.run, sizeof(RunCtrl) * M, cudaMemcpyDeviceToHost, st));
+    FL_CUDA(cudaStreamSynchronize(st));
+    for (int32_t m = 0; m < M; ++m) {
+        s->select(m);
+        const RunCtrl &e = *s->run_h;
+        if (!e.error && e.finite_interval > 0 && e.step > 0 && e.step % e.finite_interval == 0) {
+            FL_CUDA(launch_finite(s->state[0], s->state[1], s->run, s->C, st));
+            g_launches++;
+            if ((rc = sync_run(s, st))) break;
+        }
+        if (s->run_h->error) {
+            rc = error_code_message(s);
+            break;
+        }
+    }
+    s->select(keep);
+    return rc;
+}
+
 FL_API int fl_run(FlSolver *s, double t_target_s, int64_t max_steps, void *stream) {
     if (!s) return set_error(FL_E_INVALID, "solver is NULL");
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
+    if (s->members > 1) return run_members(s, t_target_s, max_steps, st);
     int rc = sync_run(s, st);
     if (rc) return rc;
     if (s->run_h->error) return error_code_message(s);
@@ -1025,7 +1285,7 @@ FL_API int fl_run(FlSolver *s, double t_target_s, int64_t max_steps, void *strea
     int64_t launched = 0;
     int64_t last_step = -1;
     int stalled = 0;
-    const int per_chunk = s->chunk * s->launches_per_step() + (s->chunk + interval - 1) / interval;
+    const int per_chunk = s->chunk * s->launches_per_step() + s->members * ((s->chunk + interval - 1) / interval);
     while (true) {
         FL_CUDA(cudaGraphLaunch(s->graph, st));
         g_launches += per_chunk;
@@ -1061,6 +1321,7 @@ FL_API int fl_run(FlSolver *s, double t_target_s, int64_t max_steps, void *strea
 
 FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mps, void *stream) {
     if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    if (s->members > 1) return set_error(FL_E_UNSUPPORTED, "fl_step runs a single-member solver");
     if (!(dt_s > 0.0)) return set_error(FL_E_INVALID, "timestep_s must be positive.");
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
@@ -1124,6 +1385,7 @@ FL_API int fl_step(FlSolver *s, double dt_s, int32_t phases, double rain_rate_mp
 
 FL_API int fl_time_kernel(FlSolver *s, int32_t kernel, int32_t reps, void *stream, double *ms_per_launch) {
     if (!s || !ms_per_launch || reps < 1) return set_error(FL_E_INVALID, "bad fl_time_kernel arguments");
+    if (s->members > 1) return set_error(FL_E_UNSUPPORTED, "fl_time_kernel times a single-member solver");
     if ((kernel == 1 || kernel == 2 || kernel == 4 || kernel == 5) && !s->has_drain())
         return set_error(FL_E_INVALID, "solver has no drainage");
     if (kernel < 0 || kernel > 5) return set_error(FL_E_INVALID, "kernel must be 0..5");
@@ -1199,7 +1461,7 @@ FL_API int fl_stable_timestep(FlSolver *s, double *dt_s, void *stream) {
     if (!s || !dt_s) return set_error(FL_E_INVALID, "solver or output is NULL");
     cudaStream_t st = (cudaStream_t)stream;
     FL_CUDA(cudaSetDevice(s->device));
-    DtArgs a = s->da;
+    DtArgs a = dt_args(s, s->cur);
     a.dt_out = s->dt_out;
     FL_CUDA(launch_dt(a, s->dt_blocks, 0, 0, st));
     g_launches++;
@@ -1369,6 +1631,7 @@ static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 FL_API int fl_set_boundary_inflow(FlSolver *s, int32_t J, const int32_t *cells, int32_t T, const double *times,
                                   const float *q) {
     if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    if (s->members > 1 && J > 0) return set_error(FL_E_UNSUPPORTED, "external inflow needs a single-member solver");
     if (J < 0) return set_error(FL_E_INVALID, "receiver_count must be >= 0");
     if (J > 0 && (!cells || !times || !q || T < 1))
         return set_error(FL_E_INVALID, "external inflow needs receiver cells, at least one time and the flow table");
@@ -1447,6 +1710,7 @@ FL_API int fl_set_boundary_inflow(FlSolver *s, int32_t J, const int32_t *cells, 
 FL_API int fl_set_recharge(FlSolver *s, int32_t R, const int32_t *cells, const float *storage_cap,
                            const float *capture_cap, const float *recharge_cap, const float *stop_depth) {
     if (!s) return set_error(FL_E_INVALID, "solver is NULL");
+    if (s->members > 1 && R > 0) return set_error(FL_E_UNSUPPORTED, "surface recharge needs a single-member solver");
     if (R < 0) return set_error(FL_E_INVALID, "row_count must be >= 0");
     if (R > 0 && (!cells || !storage_cap || !capture_cap || !recharge_cap || !stop_depth))
         return set_error(FL_E_INVALID, "recharge needs cells and the four per-row arrays");

@@ -140,6 +140,10 @@ _SIGNATURES = {
     "fl_device_count": (C.c_int, [i32p]),
     "fl_create": (C.c_int, [C.POINTER(FlMeshDesc), C.POINTER(FlDrainDesc), C.POINTER(FlForcingDesc),
                             C.POINTER(FlParams), C.c_int32, C.POINTER(C.c_void_p)]),
+    "fl_create_members": (C.c_int, [C.POINTER(FlMeshDesc), C.POINTER(FlDrainDesc), C.POINTER(FlForcingDesc),
+                                    C.c_int32, C.POINTER(FlParams), C.c_int32, C.POINTER(C.c_void_p)]),
+    "fl_member_select": (C.c_int, [C.c_void_p, C.c_int32]),
+    "fl_member_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "fl_destroy": (None, [C.c_void_p]),
     "fl_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_int32, C.c_void_p]),

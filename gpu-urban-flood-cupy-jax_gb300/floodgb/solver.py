@@ -57,6 +57,27 @@ class Descriptors:
     kind: int
 
 
+def forcing_desc(rainfall, infiltration_fields, infiltration_mps: float, keep) -> "N.FlForcingDesc":
+    """Forcing descriptor: the hyetograph of `rainfall` and the per-cell
+    Horton fields (or the scalar infiltration capacity)."""
+
+    if rainfall is not None:
+        hs, he, hr = hyetograph_arrays(rainfall)
+    else:
+        hs = he = hr = np.zeros(0)
+    kind = 1 if infiltration_fields is not None else 0
+    return N.FlForcingDesc(
+        kind=kind,
+        rain_multiplier=keep.f32(infiltration_fields.rainfall_multiplier if kind else None),
+        horton_f0_mps=keep.f32(infiltration_fields.horton_f0_mps if kind else None),
+        horton_fc_mps=keep.f32(infiltration_fields.horton_fc_mps if kind else None),
+        horton_k_per_s=keep.f32(infiltration_fields.horton_k_per_s if kind else None),
+        infiltration_mps=float(np.float32(infiltration_mps)),
+        hyetograph_count=int(np.asarray(hs).size),
+        hyeto_start_s=keep.f64(hs), hyeto_end_s=keep.f64(he), hyeto_rate_mps=keep.f64(hr),
+    )
+
+
 def build_descriptors(surface_topology, coupling_topology=None, pipe_topology=None, *, rainfall=None,
                       infiltration_fields=None, infiltration_mps: float = 0.0, cfg: RunConfig | None = None,
                       duration_s: float | None = None, centroids=None, boundary_stage_m: float | None = None,
@@ -84,21 +105,8 @@ def build_descriptors(surface_topology, coupling_topology=None, pipe_topology=No
         drain = N.drain_desc(coupling_topology, pipe_topology, keep, ph.inlet_capture_rule,
                              ph.inlet_orifice_area_m2, ph.inlet_orifice_coefficient,
                              ph.inlet_weir_perimeter_m, ph.inlet_weir_coefficient)
-    if rainfall is not None:
-        hs, he, hr = hyetograph_arrays(rainfall)
-    else:
-        hs = he = hr = np.zeros(0)
     kind = 1 if infiltration_fields is not None else 0
-    forcing = N.FlForcingDesc(
-        kind=kind,
-        rain_multiplier=keep.f32(infiltration_fields.rainfall_multiplier if kind else None),
-        horton_f0_mps=keep.f32(infiltration_fields.horton_f0_mps if kind else None),
-        horton_fc_mps=keep.f32(infiltration_fields.horton_fc_mps if kind else None),
-        horton_k_per_s=keep.f32(infiltration_fields.horton_k_per_s if kind else None),
-        infiltration_mps=float(np.float32(infiltration_mps)),
-        hyetograph_count=int(np.asarray(hs).size),
-        hyeto_start_s=keep.f64(hs), hyeto_end_s=keep.f64(he), hyeto_rate_mps=keep.f64(hr),
-    )
+    forcing = forcing_desc(rainfall, infiltration_fields, infiltration_mps, keep)
     if max_snapshots is None:
         max_snapshots = int(math.ceil(duration_s / (s.snapshot_interval_min * 60.0))) + 2
     params = N.FlParams(
@@ -372,5 +380,76 @@ def solver_for_city(city, rainfall, cfg: RunConfig, duration_s: float | None = N
         s.set_boundary_inflow(city.external_boundary)
     if getattr(city, "recharge_topology", None) is not None:
         s.set_recharge(city.recharge_topology)
+    s.reset_clock()
+    return s
+
+
+class MemberSolver(FloodSolver):
+    """Ensemble members on one city (fl_create_members): the same mesh,
+    drainage network, infiltration fields and parameters, one rainfall event
+    per member; each member its own state, adaptive dt, snapshots and ledger.
+    run() advances every member to the end of the run; the other methods
+    address the member chosen with select() (member 0 at first)."""
+
+    def __init__(self, surface_topology, coupling_topology=None, pipe_topology=None, *, rainfalls,
+                 infiltration_fields=None, infiltration_mps: float = 0.0, cfg: RunConfig | None = None,
+                 duration_s: float | None = None, centroids=None, max_snapshots: int | None = None, device: int = 0,
+                 gravity_mps2: float = 9.80665, min_depth_m: float = 1.0e-5):
+        lib = N.load()
+        cfg = cfg or load_config()
+        rainfalls = list(rainfalls)
+        if not rainfalls:
+            raise ValueError("at least one member is needed")
+        d = build_descriptors(surface_topology, coupling_topology, pipe_topology, rainfall=rainfalls[0],
+                              infiltration_fields=infiltration_fields, infiltration_mps=infiltration_mps, cfg=cfg,
+                              duration_s=duration_s, centroids=centroids, max_snapshots=max_snapshots,
+                              gravity_mps2=gravity_mps2, min_depth_m=min_depth_m)
+        forcings = (N.FlForcingDesc * len(rainfalls))()
+        forcings[0] = d.forcing
+        for m, r in enumerate(rainfalls[1:], start=1):
+            forcings[m] = forcing_desc(r, infiltration_fields, infiltration_mps, d.keep)
+        self.cfg = cfg
+        self.duration_s = d.duration_s
+        self.cell_count = surface_topology.cell_count
+        self.node_count = coupling_topology.node_count if coupling_topology is not None else 0
+        self.link_count = pipe_topology.link_count if pipe_topology is not None else 0
+        self.kind = d.kind
+        self.max_snapshots = d.max_snapshots
+        self.members = len(rainfalls)
+        handle = C.c_void_p()
+        rc = lib.fl_create_members(C.byref(d.mesh), C.byref(d.drain) if d.drain is not None else None, forcings,
+                                   len(rainfalls), C.byref(d.params), int(device), C.byref(handle))
+        N.check(rc, "fl_create_members")
+        self._h = handle
+        self._lib = lib
+        self._keep = None
+
+    def select(self, member: int) -> "MemberSolver":
+        N.check(self._lib.fl_member_select(self._h, int(member)), "fl_member_select")
+        return self
+
+    def run(self, t_target_s: float | None = None, max_steps: int = 0, stream=None):
+        """Every member to the end of the run."""
+
+        return super().run(None, 0, stream=stream)
+
+
+def members_for_city(city, rainfalls, cfg: RunConfig, duration_s: float | None = None, device: int = 0,
+                     max_snapshots: int | None = None) -> MemberSolver:
+    """MemberSolver for a CityDomain and one rainfall event per member, each
+    member starting from the city's initial state."""
+
+    topo = city.topologies
+    if getattr(city, "external_boundary", None) is not None or getattr(city, "recharge_topology", None) is not None:
+        raise ValueError("ensemble members support neither external inflow nor surface recharge")
+    fields, simple = city_infiltration(city, cfg)
+    s = MemberSolver(topo.surface_topology, topo.coupling_topology, topo.pipe_topology, rainfalls=rainfalls,
+                     infiltration_fields=fields, infiltration_mps=simple, cfg=cfg, duration_s=duration_s,
+                     centroids=city.mesh.centroids_xy, device=device, max_snapshots=max_snapshots)
+    for m in range(s.members):
+        s.select(m).set_state(topo.surface_state.h_m, topo.surface_state.hu_m2ps, topo.surface_state.hv_m2ps,
+                              topo.pipe_state.node_volume_m3 if s.node_count else None,
+                              topo.pipe_state.link_flow_m3ps if s.link_count else None)
+    s.select(0)
     s.reset_clock()
     return s

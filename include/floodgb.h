@@ -175,6 +175,27 @@ FL_API int fl_create(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlF
                      const FlParams *params, int32_t device, FlSolver **out);
 FL_API void fl_destroy(FlSolver *solver);
 
+/* Ensemble members on one mesh.  No counterpart in the reference, which runs
+ * one scenario per process.  n_members runs of the same mesh, drainage
+ * network and parameters that differ in their rainfall: member m takes the
+ * hyetograph of forcings[m], and the per-cell fields (Horton f0 / fc / k,
+ * rain multiplier, scalar infiltration) of forcings[0] apply to every
+ * member.  Each member has its own state, adaptive dt, snapshots and
+ * ledger and follows exactly the single-instance step of fl_run; per step
+ * the surface kernel runs once per member and each drainage kernel once for
+ * all members (the members share the static tables).  The calls that take a
+ * solver address the selected member (fl_member_select; member 0 after
+ * creation), except fl_run, which runs every member to the end of the run
+ * (t_target >= the duration, no step cap), and fl_reset_clock, which resets
+ * every member.  Not available with several members: the local-inertial
+ * step, external inflow, surface recharge, the weighted surcharge table,
+ * fl_step and fl_time_kernel (FL_E_UNSUPPORTED).  fl_create is
+ * fl_create_members with one member. */
+FL_API int fl_create_members(const FlMeshDesc *mesh, const FlDrainDesc *drain, const FlForcingDesc *forcings,
+                             int32_t n_members, const FlParams *params, int32_t device, FlSolver **out);
+FL_API int fl_member_select(FlSolver *solver, int32_t member);
+FL_API int fl_member_count(FlSolver *solver, int32_t *members);
+
 /* State transfer in reference order: TriangularSurfaceState,
  * TriangularPipeNetworkState (:49-55, :203-208) and the Horton wet time.
  * Any pointer may be NULL to leave that field unchanged / unread. */
