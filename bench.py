@@ -436,9 +436,10 @@ def our_arm(args):
     ensemble = None
     if world == 1 and not args.no_ensemble:
         ensemble = ensemble_measure()
-    long_run = None
+    long_run = members = None
     if world == 1 and not args.no_long_run:
         long_run = long_single(24.0)
+        members = members_measure(3.0, 8)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / len(ms), "higher_is_better": True, "scaling": "weak",
@@ -468,6 +469,7 @@ def our_arm(args):
         "parity": parity,
         "ensemble": ensemble,
         "long_run_24h": long_run,
+        "members_config4": members,
     }
     print(json.dumps(line), flush=True)
 
@@ -591,6 +593,58 @@ def long_single(hours: float = 24.0) -> dict:
             "reference_hardware": "RTX PRO 4000 Blackwell, real 981,880-tri city, 321,645 steps"}
 
 
+def members_measure(hours: float = 3.0, members: int = 8) -> dict:
+    """Config-4 ensemble: `members` production-sized coupled members on the
+    981,880-triangle city with seeded variants of the 160 mm / 24 h event
+    (intensity x U(0.7, 1.3), peak shifted by up to +-3 h), run for `hours`
+    simulated hours as one member solver (the surface kernel once per member
+    and each drainage kernel once for all members per step), against the
+    same members run one after another by the single-instance solver."""
+
+    import numpy as np
+    import torch
+
+    from floodgb.config import load_config
+    from floodgb.rainfall import hourly_rainfall
+    from floodgb.solver import members_for_city, solver_for_city
+    from floodgb.synthetic import FRONT_LOADED_24H_MMHR, production_workload
+
+    sc = production_workload()
+    cfg = load_config(None, dict(sc.overrides, **{"solver.duration_min": hours * 60.0}))
+    C = sc.city.topologies.surface_topology.cell_count
+    rng = np.random.default_rng(24)
+    rains = [hourly_rainfall(np.roll(FRONT_LOADED_24H_MMHR * rng.uniform(0.7, 1.3), int(rng.integers(-3, 4))))
+             for _ in range(members)]
+    seq_s, seq_steps = 0.0, []
+    for r in rains:
+        s = solver_for_city(sc.city, r, cfg)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s.run()
+        torch.cuda.synchronize()
+        seq_s += time.perf_counter() - t
+        seq_steps.append(s.progress().step_count)
+        s.close()
+    ens = members_for_city(sc.city, rains, cfg)
+    try:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ens.run()
+        torch.cuda.synchronize()
+        batched_s = time.perf_counter() - t
+        steps = [ens.select(m).progress().step_count for m in range(members)]
+    finally:
+        ens.close()
+    return {"members": members, "hours_each": hours, "cells": C, "steps": steps,
+            "steps_match_single_runs": steps == seq_steps,
+            "batched_s": batched_s, "batched_scenario_h_per_s": members * hours / batched_s,
+            "batched_cell_steps_per_s": C * sum(steps) / batched_s,
+            "single_instance_s": seq_s, "single_instance_scenario_h_per_s": members * hours / seq_s,
+            "batched_over_single": seq_s / batched_s,
+            "workload": "production-shaped coupled city, seeded variants of the 160 mm / 24 h front-loaded event, "
+                        f"hours 0-{hours:g}"}
+
+
 def long_arm(args):
     """The 24 h single instance (long_single), then `long_members` members
     with seeded variants of the event (intensity x U(0.7, 1.3), peak shifted
@@ -648,7 +702,8 @@ def long_arm(args):
                 "scenario_h_per_s": len(solvers) * args.long_hours / ens_s, "steps": steps,
                 "cell_steps_per_s": C * sum(steps) / ens_s, "errors": errors,
                 "single_instance_scenario_h_per_s": args.long_hours / solve_s}
-    print(json.dumps({"long_run": single, "concurrent_members": ensemble}))
+    batched = members_measure(args.long_hours, args.long_members)
+    print(json.dumps({"long_run": single, "concurrent_members": ensemble, "batched_members": batched}))
 
 
 def main():
