@@ -469,7 +469,9 @@ FL_API void fl_destroy(FlSolver *s) {
     for (void *p : s->allocs) cudaFree(p);
     if (s->ext_mem) cudaFree(s->ext_mem);
     if (s->rch_mem) cudaFree(s->rch_mem);
-    if (s->run_h) cudaFreeHost(s->run_h);
+    // the pinned run records start at member 0's (run_h addresses the selected member)
+    RunCtrl *run_h = s->mb.run_h ? s->mb.run_h : s->run_h;
+    if (run_h) cudaFreeHost(run_h);
     if (s->poll_h) cudaFreeHost(s->poll_h);
     delete s;
 }
