@@ -7,8 +7,9 @@ storms held out), the flag threshold on the networks' disagreement is
 calibrated on the held-out storms, then a held-out ensemble is screened --
 ensemble rollouts for every member, flags where the networks disagree, a
 random audit -- and the solver re-runs the flagged and audited members and
-scores the surrogate on them (or on every member).  The audit is drawn before
-the rollouts, so its re-runs overlap them on a second stream.  Throughput is
+scores the surrogate on them (or on every member).  The re-runs follow the
+rollouts as one set of batches, or the audit (drawn before the rollouts) runs
+on a second stream beside them.  Throughput is
 scenario-hours per second of the whole screening (surrogate + re-runs)
 against the plain single-instance solver (one FloodSolver run per member,
 sequentially) and the batched solver.
@@ -46,12 +47,22 @@ def _mesh(grid_n: int, seed: int):
 
 def screen(models, mf, city, cfg, threshold: float, storms, durations, *, audit: float = 0.05, seed: int = 0,
            plain_sample: int = 8, batch_size: int = 64, baselines: bool = False, n_layers: int = 8,
-           score_all: bool = True, overlap: bool = True) -> dict:
-    """Screen an ensemble: a random audit, ensemble rollouts of every member
-    (the audit re-runs overlapping them on a second stream), flags where the
-    networks disagree, solver re-runs of the flagged members; the solver
-    judges the re-run members (or, with score_all, every member); the plain
-    single-instance solver is timed on a sample."""
+           score_all: bool = True, rerun: str = "after", rerun_batch: int = 128,
+           extent_threshold: float | None = None) -> dict:
+    """Screen an ensemble: a random audit, ensemble rollouts of every member,
+    flags where the networks disagree, solver re-runs of the flagged and
+    audited members; the solver judges the re-run members (or, with
+    score_all, every member); the plain single-instance solver is timed on a
+    sample.
+
+    rerun="after": the rollouts first, then the flagged and audited members
+    in batches of up to `rerun_batch`.  rerun="overlap": the audit re-runs on
+    a second stream while the rollouts run, then the flagged members that
+    were not audited.  `extent_threshold` (calibrate_extent) adds each
+    member's CSI of the surrogate's envelope at that depth."""
+
+    if rerun not in ("after", "overlap"):
+        raise ValueError(f"rerun must be 'after' or 'overlap', not {rerun!r}")
 
     import threading
 
@@ -80,45 +91,46 @@ def screen(models, mf, city, cfg, threshold: float, storms, durations, *, audit:
                                        batch_size, stream=side)
 
     t = time.perf_counter()
-    worker = threading.Thread(target=run_audit) if overlap else None
+    worker = threading.Thread(target=run_audit) if rerun == "overlap" else None
     if worker is not None:
         worker.start()
-    else:
-        run_audit()
     main = torch.cuda.Stream()
     with torch.cuda.stream(main):
         preds, spread = ensemble_rollouts(models, mf, storms, durations, copies=copies)
     main.synchronize()
     surr_s = time.perf_counter() - t
+    audit_trajs, audit_solver_s = [], None
     if worker is not None:
         worker.join()
-    audit_trajs, audit_solver_s, audit_h = audit_out["r"]
+        audit_trajs, audit_solver_s, _ = audit_out["r"]
     overlap_s = time.perf_counter() - t
     ops.status()
     hours = float(sum(durations)) / 3600.0
     flagged = flags(spread, threshold)
-    f_idx = np.flatnonzero(flagged & ~audited)
+    # the members the solver re-runs now: with the audit already re-run, the flagged rest
+    f_idx = np.flatnonzero(flagged & ~audited) if worker is not None else np.flatnonzero(flagged | audited)
     t = time.perf_counter()
-    flag_trajs = []
+    flag_trajs, flag_solver_s = [], 0.0
     if f_idx.size:
-        flag_trajs, _, _ = solve_members(city, cfg, [storms[i] for i in f_idx], [durations[i] for i in f_idx],
-                                         batch_size)
+        flag_trajs, flag_solver_s, _ = solve_members(city, cfg, [storms[i] for i in f_idx],
+                                                     [durations[i] for i in f_idx],
+                                                     batch_size if worker is not None else rerun_batch)
     torch.cuda.synchronize()
     flag_s = time.perf_counter() - t
-    rerun = {int(i): tr for i, tr in zip(a_idx, audit_trajs)}
-    rerun.update({int(i): tr for i, tr in zip(f_idx, flag_trajs)})
-    rerun_h = float(sum(durations[i] for i in rerun)) / 3600.0
+    re_solved = {int(i): tr for i, tr in zip(a_idx, audit_trajs)}
+    re_solved.update({int(i): tr for i, tr in zip(f_idx, flag_trajs)})
+    rerun_h = float(sum(durations[i] for i in re_solved)) / 3600.0
     if score_all:
         truth, batched_s, _ = solve_members(city, cfg, storms, durations, batch_size)
-        scores = [score(mf, p, tr) for p, tr in zip(preds, truth)]
+        scores = [score(mf, p, tr, extent_threshold=extent_threshold) for p, tr in zip(preds, truth)]
         scored = np.ones(n, bool)
     else:
         truth, batched_s = None, None
         scores = [None] * n
-        for i, tr in rerun.items():
-            scores[i] = score(mf, preds[i], tr)
+        for i, tr in re_solved.items():
+            scores[i] = score(mf, preds[i], tr, extent_threshold=extent_threshold)
         scored = flagged | audited
-    del rerun, audit_trajs, flag_trajs
+    del re_solved, audit_trajs, flag_trajs
 
     def agg(mask):
         mask = mask & scored
@@ -154,13 +166,13 @@ def screen(models, mf, city, cfg, threshold: float, storms, durations, *, audit:
     screen_s = overlap_s + flag_s
     res["throughput_scenario_h_per_s"] = {
         "plain_single_instance": plain_rate,
-        "batched_solver": hours / batched_s if batched_s else (audit_h / audit_solver_s if audit_solver_s else None),
+        "batched_solver": hours / batched_s if batched_s else None,
         "surrogate_only": hours / surr_s,
         "screening": hours / screen_s,
         "screening_over_plain": (hours / screen_s) / plain_rate,
-        "surrogate_s": surr_s, "audit_rerun_solver_s": audit_solver_s, "surrogate_and_audit_wall_s": overlap_s,
-        "flag_rerun_s": flag_s, "rerun_scenario_h": rerun_h,
-        "audit_overlapped_with_rollouts": bool(overlap),
+        "surrogate_s": surr_s, "audit_rerun_solver_s": audit_solver_s, "rollout_wall_s": overlap_s,
+        "rerun_wall_s": flag_s, "rerun_solver_s": flag_solver_s, "rerun_scenario_h": rerun_h,
+        "rerun": rerun, "rerun_batch": rerun_batch if rerun == "after" else batch_size,
     }
     return res
 
@@ -177,7 +189,8 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
     import torch
 
     from .model import MPNN
-    from .pipeline import MeshFeatures, calibrate_flags, ensemble_rollouts, score, solve_members, train
+    from .pipeline import (MeshFeatures, calibrate_extent, calibrate_flags, ensemble_rollouts, score, solve_members,
+                           train)
 
     city, cfg = _mesh(grid_n, seed)
     mf = MeshFeatures(city.topologies.surface_topology)
@@ -191,21 +204,24 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
     res["train_data"] = {"solver_s": solve_s, "scenario_hours": tr_hours, "wall_s": time.perf_counter() - t}
     log(f"training trajectories: {tr_hours:.1f} scenario-h in {solve_s:.1f} s")
     fit, val = trajs[:n_train - n_val], trajs[n_train - n_val:]
-    models, hists = [], []
+    models, hists, forced = [], [], []
     torch.cuda.synchronize()
     t = time.perf_counter()
     for k in range(n_models):
         m = MPNN(n_layers=n_layers, seed=seed + 1000 * k)
+        forced.append([])
         hists.append(train(m, mf, fit, epochs=epochs, lr=lr, seed=seed + k, log=log, max_seconds=train_seconds,
-                           extent_weight=extent_weight, pushforward=pushforward))
+                           extent_weight=extent_weight, pushforward=pushforward, teacher=forced[-1]))
         models.append(m)
     torch.cuda.synchronize()
     res["train"] = {"seconds": time.perf_counter() - t, "epochs": [len(h) for h in hists], "loss": hists,
+                    "teacher_forced_loss": forced,
                     "windows": sum(len(tr.times_s) - 1 for tr in fit)}
     # flag threshold: the networks' disagreement on the held-out training storms
     preds, spread = ensemble_rollouts(models, mf, tr_storms[n_train - n_val:], tr_dur[n_train - n_val:])
     errors = [score(mf, p, tr)["rmse_hmax_m"] for p, tr in zip(preds, val)]
     cal = calibrate_flags(spread, np.asarray(errors), flag_fraction)
+    cal.update(calibrate_extent(mf, preds, val))
     res["calibration"] = cal
     log(f"calibration: {cal}")
     depth = lambda e: float(np.sum(e.intensity_mmhr * (e.end_min - e.start_min)) / 60.0)  # noqa: E731
@@ -214,9 +230,11 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
     res["limits"] = limits
     del trajs, fit, val
     res.update(screen(models, mf, city, cfg, cal["threshold_m"], ev_storms, ev_dur, audit=audit, seed=seed,
-                      plain_sample=plain_sample, batch_size=batch_size, baselines=baselines, n_layers=n_layers))
+                      plain_sample=plain_sample, batch_size=batch_size, baselines=baselines, n_layers=n_layers,
+                      extent_threshold=cal["extent_threshold_m"]))
     if weights_out:
-        save(weights_out, models, cal, limits, {"grid_n": grid_n, "seed": seed, "n_layers": n_layers})
+        save(weights_out, models, cal, limits, {"grid_n": grid_n, "seed": seed, "n_layers": n_layers,
+                                                "n_train": n_train, "n_val": n_val})
     log(json.dumps(res["throughput_scenario_h_per_s"]))
     return res
 
@@ -248,7 +266,7 @@ def load(path):
 
 
 def screen_saved(path, n_eval: int = 64, plain_sample: int = 2, audit: float = 0.05, duration_cap_h=None,
-                 score_all: bool = True) -> dict:
+                 score_all: bool = True, rerun: str = "after", rerun_batch: int = 128) -> dict:
     """Screen the first n_eval held-out storms of the saved ensemble's mesh and seed."""
 
     from .pipeline import MeshFeatures
@@ -258,10 +276,34 @@ def screen_saved(path, n_eval: int = 64, plain_sample: int = 2, audit: float = 0
     mf = MeshFeatures(city.topologies.surface_topology)
     storms, dur = _storms(n_eval, int(meta["seed"]) + 2, duration_cap_h)
     res = screen(models, mf, city, cfg, float(cal["threshold_m"]), storms, dur, audit=audit, seed=int(meta["seed"]),
-                 plain_sample=plain_sample, score_all=score_all)
+                 plain_sample=plain_sample, score_all=score_all, rerun=rerun, rerun_batch=rerun_batch,
+                 extent_threshold=cal.get("extent_threshold_m"))
     res["mesh_cells"] = mf.C
     res["calibration"] = cal
     return res
+
+
+def recalibrate(path, batch_size: int = 64) -> dict:
+    """Recompute the extent threshold of a saved ensemble on its held-out
+    training storms (the last n_val of the n_train seeded training storms)
+    and write it into the file's calibration; returns the calibration."""
+
+    from .pipeline import MeshFeatures, calibrate_extent, ensemble_rollouts, solve_members
+
+    models, cal, meta = load(path)
+    n_train = int(meta.get("n_train", 512))
+    n_val = int(meta.get("n_val", cal["validation_members"]))
+    city, cfg = _mesh(int(meta["grid_n"]), int(meta["seed"]))
+    mf = MeshFeatures(city.topologies.surface_topology)
+    storms, dur = _storms(n_train, int(meta["seed"]) + 1)
+    storms, dur = storms[n_train - n_val:], dur[n_train - n_val:]
+    val, _, _ = solve_members(city, cfg, storms, dur, batch_size)
+    preds, _ = ensemble_rollouts(models, mf, storms, dur)
+    cal.update(calibrate_extent(mf, preds, val))
+    with np.load(path) as z:
+        limits = json.loads(str(z["limits"]))
+    save(path, models, cal, limits, dict(meta, n_train=n_train, n_val=n_val))
+    return cal
 
 
 def main():
@@ -279,9 +321,17 @@ def main():
     p.add_argument("--networks", type=int, default=2)
     p.add_argument("--flag-fraction", type=float, default=0.04)
     p.add_argument("--screen-only", default=None, help="screen with saved weights (no training)")
+    p.add_argument("--rerun", choices=("after", "overlap"), default="after")
+    p.add_argument("--rerun-batch", type=int, default=128)
+    p.add_argument("--score-all", action="store_true", help="with --screen-only: solve and score every member")
+    p.add_argument("--recalibrate", default=None, help="recompute a saved ensemble's extent threshold in place")
     a = p.parse_args()
+    if a.recalibrate:
+        print(json.dumps(recalibrate(a.recalibrate), indent=1))
+        return
     if a.screen_only:
-        res = screen_saved(a.screen_only, n_eval=a.eval, plain_sample=8, duration_cap_h=a.duration_cap_h)
+        res = screen_saved(a.screen_only, n_eval=a.eval, plain_sample=8, duration_cap_h=a.duration_cap_h,
+                           score_all=a.score_all, rerun=a.rerun, rerun_batch=a.rerun_batch)
         text = json.dumps(res, indent=1)
         if a.out:
             with open(a.out, "w") as f:

@@ -126,29 +126,33 @@ def windows(duration_s: float) -> list[tuple[float, float]]:
 def solve_members(city, cfg, storms, durations_s, batch_size: int = 64, shape=None, device: str = "cuda",
                   stream=None):
     """Solver trajectories (hourly snapshots, window maxima and momenta, kept
-    on the device) of storms on one mesh, batched; returns (trajectories,
-    solver seconds, scenario hours).  With `stream` the solver runs on that
-    stream (and only it is synchronised), so other work can overlap it."""
+    on the device) of storms on one mesh, batched; returns (trajectories in
+    the order of `storms`, solver seconds, scenario hours).  A batch runs
+    until its longest member ends, so members go into batches longest storm
+    first.  With `stream` the solver runs on that stream (and only it is
+    synchronised), so other work can overlap it."""
 
     import torch
 
     from ..batch import BatchSolver, Member
 
-    out = []
+    out = [None] * len(storms)
     seconds = 0.0
     sync = stream.synchronize if stream is not None else torch.cuda.synchronize
+    order = sorted(range(len(storms)), key=lambda k: (-float(durations_s[k]), k))
+    dev = lambda a: torch.as_tensor(a, device=device)  # noqa: E731
     for k0 in range(0, len(storms), batch_size):
-        members = [Member(city, storms[k], cfg, durations_s[k]) for k in range(k0, min(len(storms), k0 + batch_size))]
+        idx = order[k0:k0 + batch_size]
+        members = [Member(city, storms[k], cfg, durations_s[k]) for k in idx]
         with BatchSolver(members, shape=shape) as b:
             sync()
             t = time.perf_counter()
             b.run(stream=stream)
             sync()
             seconds += time.perf_counter() - t
-            for j, m in enumerate(members):
+            for j, (k, m) in enumerate(zip(idx, members)):
                 ts, h, hm, hu, hv = b.snapshots(j, momentum=True)
-                dev = lambda a: torch.as_tensor(a, device=device)  # noqa: E731
-                out.append(Trajectory(ts, dev(h), dev(hm), dev(hu), dev(hv), m.rainfall, m.duration_s))
+                out[k] = Trajectory(ts, dev(h), dev(hm), dev(hu), dev(hv), m.rainfall, m.duration_s)
     return out, seconds, float(sum(durations_s)) / 3600.0
 
 
@@ -206,13 +210,20 @@ def loss_weights(mf: MeshFeatures, depths, extent_weight: float):
 
 
 def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: float = 1e-3, seed: int = 0,
-          log=None, max_seconds: float | None = None, extent_weight: float = 3.0, pushforward: float = 0.5):
+          log=None, max_seconds: float | None = None, extent_weight: float = 3.0, pushforward: float = 0.5,
+          teacher: list | None = None):
     """Full-graph steps over every window of every trajectory; weighted MSE on
     active cells.  From the second epoch, a window after the first starts
     with probability `pushforward` from the network's own one-window
     prediction (from the solver's state a window earlier) instead of the
     solver's state, so the network learns to correct its own errors in a
-    rollout."""
+    rollout.
+
+    Returns the mean loss of each epoch over all its windows.  The first
+    epoch has no pushforward windows, so that figure rises when they start;
+    `teacher`, when given, receives each epoch's mean loss over the windows
+    that started from the solver's state, which is comparable across
+    epochs."""
 
     import torch
 
@@ -227,6 +238,8 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
     t_start = time.perf_counter()
     for ep in range(epochs):
         total = torch.zeros((), device=mf.device)
+        forced = torch.zeros((), device=mf.device)
+        n_forced = 0
         for i in rng.permutation(len(samples)):
             rate = lr * 0.5 * (1.0 + math.cos(math.pi * k / max(steps, 1)))  # cosine decay
             tr, w = samples[i]
@@ -243,13 +256,19 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
             norm = wts.sum()
             y = model.forward(g, x)
             diff = y[:, :N_OUT] - yt
-            total += (wts * diff * diff).sum() / norm
+            loss = (wts * diff * diff).sum() / norm
+            total += loss
+            if state is None:
+                forced += loss
+                n_forced += 1
             dy[:, :N_OUT] = wts * diff * (2.0 / norm)
             model.zero_grad()
             model.backward(g, x, dy)
             model.step(rate)
             k += 1
         history.append(float(total.item()) / len(samples))
+        if teacher is not None:
+            teacher.append(float(forced.item()) / max(n_forced, 1))
         if log:
             log(f"epoch {ep}: loss {history[-1]:.5f}")
         if max_seconds is not None and time.perf_counter() - t_start > max_seconds:
@@ -286,12 +305,30 @@ def rollout_batch(model: MPNN, mf: MeshFeatures, storms, durations_s, copies: in
     """Rollouts of many members, `copies` at a time in one forward pass over
     the replicated graph; same results as rollout() member by member."""
 
+    return ensemble_rollouts([model], mf, storms, durations_s, copies=copies)[0]
+
+
+def ensemble_rollouts(models, mf: MeshFeatures, storms, durations_s, copies: int = 32):
+    """Rollouts of every member by each network of an ensemble, `copies`
+    members per forward pass over the replicated graph: (mean prediction
+    (window ends, h [n, C], hmax [n, C]) per member as host arrays, and the
+    disagreement per member = RMS over the member's windows, the networks and
+    the active cells of the networks' window maxima about their mean).
+
+    All networks advance the same members window by window, so the mean and
+    the disagreement are formed on the device and only the mean comes back;
+    members of one pass run for the longest one's windows, so members are
+    grouped by window count and the padding windows are left out of the
+    disagreement."""
+
     import torch
 
     out = [None] * len(storms)
+    spread = np.zeros(len(storms))
     graphs = {}
-    # members of one forward pass run for the longest one's windows: group
-    # members of equal window count so few passes are padding
+    M = len(models)
+    C = mf.C
+    n_act = max(int(mf.active.sum()), 1)
     order = sorted(range(len(storms)), key=lambda i: (len(windows(durations_s[i])), i))
     for k0 in range(0, len(storms), copies):
         idx = order[k0:k0 + copies]
@@ -303,62 +340,58 @@ def rollout_batch(model: MPNN, mf: MeshFeatures, storms, durations_s, copies: in
         act = mf.active_dev.repeat(B)
         wins = [windows(durations_s[i]) for i in idx]
         n_w = max(len(w) for w in wins)
-        h = torch.zeros(B * mf.C, device=mf.device)
-        hu, hv, hm = h.clone(), h.clone(), h.clone()
+        zero = torch.zeros(B * C, device=mf.device)
+        states = [(zero, zero, zero, zero) for _ in range(M)]  # (h, hu, hv, hmax) per network
         rp = np.zeros(B)
         hs, hms = [], []
+        d2 = torch.zeros(B, dtype=torch.float64, device=mf.device)
         for w in range(n_w):
             sc = np.zeros((B, 5), np.float32)
+            live = np.zeros(B, np.float64)
             for b, i in enumerate(idx):
                 t0, t1 = wins[b][min(w, len(wins[b]) - 1)]
                 rn, pk = rain_window(storms[i], t0, t1) if w < len(wins[b]) else (0.0, 0.0)
                 sc[b] = (rn / 100.0, rp[b] / 100.0, pk / 100.0, (t1 - t0) / 3600.0, rn)
-            col = torch.as_tensor(sc, device=mf.device).repeat_interleave(mf.C, dim=0)
-            x = static.clone()
-            x[:, 0] = SCALE * h
-            x[:, 1] = SCALE * hu
-            x[:, 2] = SCALE * hv
-            x[:, 3] = SCALE * hm
-            x[:, 8:12] = col[:, :4]
-            y = model.forward(g, x.to(torch.bfloat16).contiguous(), train=False)
-            hn, hmn, hun, hvn = advance(y, h, act)
-            hs.append(hn.view(B, mf.C))
-            hms.append(hmn.view(B, mf.C))
-            h, hu, hv, hm, rp = hn, hun, hvn, hmn, sc[:, 4]
+                live[b] = 1.0 if w < len(wins[b]) else 0.0
+            col = torch.as_tensor(sc, device=mf.device).repeat_interleave(C, dim=0)
+            nxt = []
+            for model, (h, hu, hv, hm) in zip(models, states):
+                x = static.clone()
+                x[:, 0] = SCALE * h
+                x[:, 1] = SCALE * hu
+                x[:, 2] = SCALE * hv
+                x[:, 3] = SCALE * hm
+                x[:, 8:12] = col[:, :4]
+                y = model.forward(g, x.to(torch.bfloat16).contiguous(), train=False)
+                hn, hmn, hun, hvn = advance(y, h, act)
+                nxt.append((hn, hun, hvn, hmn))
+            states = nxt
+            h_mean = states[0][0] if M == 1 else sum(st[0] for st in states) / M
+            hm_mean = states[0][3] if M == 1 else sum(st[3] for st in states) / M
+            hs.append(h_mean.view(B, C))
+            hms.append(hm_mean.view(B, C))
+            if M > 1:
+                dev2 = sum((st[3] - hm_mean) ** 2 for st in states).view(B, C)
+                d2 += dev2.sum(1, dtype=torch.float64) * torch.as_tensor(live, device=mf.device)
+            rp = sc[:, 4]
         H = torch.stack(hs, 1).cpu().numpy()
         HM = torch.stack(hms, 1).cpu().numpy()
+        D2 = d2.cpu().numpy()
         for b, i in enumerate(idx):
             n = len(wins[b])
             out[i] = (np.asarray([w[1] for w in wins[b]]), H[b, :n], HM[b, :n])
-    return out
-
-
-def ensemble_rollouts(models, mf: MeshFeatures, storms, durations_s, copies: int = 32):
-    """Rollouts of every member by each network: (mean prediction (ends, h,
-    hmax) per member, disagreement per member = RMS over windows and active
-    cells of the networks' window-maximum spread about their mean)."""
-
-    runs = [rollout_batch(m, mf, storms, durations_s, copies=copies) for m in models]
-    act = mf.active
-    preds, spread = [], []
-    for i in range(len(storms)):
-        ends = runs[0][i][0]
-        hs = np.mean([r[i][1] for r in runs], axis=0)
-        hms = np.mean([r[i][2] for r in runs], axis=0)
-        preds.append((ends, hs, hms))
-        if len(runs) > 1:
-            dev = np.stack([r[i][2][:, act] for r in runs]) - hms[None, :, act]
-            spread.append(float(np.sqrt(np.mean(dev ** 2))))
-        else:
-            spread.append(0.0)
-    return preds, np.asarray(spread)
+            spread[i] = float(np.sqrt(D2[b] / (M * n * n_act))) if M > 1 else 0.0
+    return out, spread
 
 
 # ------------------------------------------------------------------ scoring
-def score(mf: MeshFeatures, pred, tr: Trajectory, threshold: float = 0.05) -> dict:
+def score(mf: MeshFeatures, pred, tr: Trajectory, threshold: float = 0.05,
+          extent_threshold: float | None = None) -> dict:
     """Surrogate vs solver over the member's hourly windows: depth and window
-    maximum RMSE (m), flood-extent CSI of the max-depth envelope, and the
-    final surface-volume error."""
+    maximum RMSE (m), flood-extent CSI of the max-depth envelopes (both at
+    `threshold`), and the final surface-volume error; with
+    `extent_threshold`, also "csi_calibrated": the surrogate's envelope at
+    that depth against the solver's at `threshold`."""
 
     ends, hp, hmp = pred
     # solver snapshot k (k >= 1) closes window k - 1
@@ -367,13 +400,43 @@ def score(mf: MeshFeatures, pred, tr: Trajectory, threshold: float = 0.05) -> di
     act = mf.active
     rm_h = float(np.sqrt(np.mean((hp[:, act] - hs[:, act]) ** 2)))
     rm_max = float(np.sqrt(np.mean((hmp[:, act] - hms[:, act]) ** 2)))
-    env_p = hmp.max(0)[act] >= threshold
+    env_p = hmp.max(0)[act]
     env_s = hms.max(0)[act] >= threshold
-    union = int((env_p | env_s).sum())
-    csi = float((env_p & env_s).sum() / union) if union else 1.0
     vp = float(np.sum(hp[-1] * mf.area))
     vs = float(np.sum(hs[-1] * mf.area))
-    return {"rmse_h_m": rm_h, "rmse_hmax_m": rm_max, "csi": csi, "volume_error": (vp - vs) / max(abs(vs), 1.0)}
+    out = {"rmse_h_m": rm_h, "rmse_hmax_m": rm_max, "csi": csi(env_p >= threshold, env_s),
+           "volume_error": (vp - vs) / max(abs(vs), 1.0)}
+    if extent_threshold is not None:
+        out["csi_calibrated"] = csi(env_p >= extent_threshold, env_s)
+    return out
+
+
+def csi(pred: np.ndarray, truth: np.ndarray) -> float:
+    """Critical success index hits / (hits + misses + false alarms) of two
+    boolean extents; 1 when both are empty."""
+
+    union = int((pred | truth).sum())
+    return float((pred & truth).sum() / union) if union else 1.0
+
+
+EXTENT_CANDIDATES_M = tuple(round(0.02 + 0.0025 * k, 4) for k in range(25))  # 0.02 .. 0.08 m
+
+
+def calibrate_extent(mf: MeshFeatures, preds, trajectories, threshold: float = 0.05) -> dict:
+    """Depth at which the surrogate's max-depth envelope best matches the
+    solver's extent at `threshold`: the candidate (0.02-0.08 m) with the
+    highest mean CSI over held-out training storms."""
+
+    act = mf.active
+    env_p, env_s = [], []
+    for (ends, _, hmp), tr in zip(preds, trajectories):
+        env_p.append(hmp.max(0)[act])
+        env_s.append(tr.hmax[1:1 + len(ends)].cpu().numpy().max(0)[act] >= threshold)
+    mean_csi = [float(np.mean([csi(p >= t, s) for p, s in zip(env_p, env_s)])) for t in EXTENT_CANDIDATES_M]
+    best = int(np.argmax(mean_csi))
+    at = EXTENT_CANDIDATES_M.index(threshold) if threshold in EXTENT_CANDIDATES_M else None
+    return {"extent_threshold_m": EXTENT_CANDIDATES_M[best], "validation_csi_calibrated": mean_csi[best],
+            "validation_csi_at_threshold": mean_csi[at] if at is not None else None}
 
 
 def flags(spread: np.ndarray, threshold: float) -> np.ndarray:
