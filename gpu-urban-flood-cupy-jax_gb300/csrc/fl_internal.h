@@ -378,6 +378,7 @@ struct HostLayout {
     std::vector<int32_t> kcell_cell, kcell_start;
     std::vector<int32_t> node_in_start;
     std::vector<int32_t> node_perm, node_inv;  // node_perm[new] = reference node
+    std::vector<int32_t> link_perm, link_inv;  // link_perm[new] = reference link
     std::vector<float> node_area, nd_capv;
     std::vector<float4> nd0;
     std::vector<int4> grp;

@@ -522,27 +522,44 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     for (; ni < N; ++ni) L.grp.push_back(make_int4(-1, -1, ni, ni + 1));  // nodes without a surface cell
     L.G = (int32_t)L.grp.size();
 
-    // links (reference order, renumbered end nodes) and each node's link slots
+    // links in the order of their renumbered (from, to) nodes, so a node's
+    // links and a link's end nodes lie close together; each node's slot list
+    // keeps the reference link order, so every per-node sum runs in the same
+    // order as with links in reference order
     L.link_from.resize(NL);
     L.link_to.resize(NL);
     L.lk0.resize(NL);
     L.lk1.resize(NL);
     L.lk2.resize(NL);
     L.node_link_start.assign(N + 1, 0);
-    const bool rect = d.link_geometry_code && d.link_rect_width_m && d.link_rect_height_m;
+    std::vector<int32_t> lfn(NL), ltn(NL);
     for (int32_t l = 0; l < NL; ++l) {
         const int32_t f = d.link_from_node_index[l], t = d.link_to_node_index[l];
         if (f < 0 || f >= N || t < 0 || t >= N)
             return set_error(FL_E_INVALID, "link %d has a node index out of range", l);
-        const int32_t fn = L.node_inv[f], tn = L.node_inv[t];
-        L.link_from[l] = fn;
-        L.link_to[l] = tn;
+        lfn[l] = L.node_inv[f];
+        ltn[l] = L.node_inv[t];
+    }
+    L.link_perm.resize(NL);
+    std::iota(L.link_perm.begin(), L.link_perm.end(), 0);
+    std::stable_sort(L.link_perm.begin(), L.link_perm.end(), [&](int32_t a, int32_t b) {
+        return lfn[a] != lfn[b] ? lfn[a] < lfn[b] : ltn[a] < ltn[b];
+    });
+    L.link_inv.assign(NL, 0);
+    for (int32_t k = 0; k < NL; ++k) L.link_inv[L.link_perm[k]] = k;
+    const bool rect = d.link_geometry_code && d.link_rect_width_m && d.link_rect_height_m;
+    for (int32_t k = 0; k < NL; ++k) {
+        const int32_t l = L.link_perm[k];
+        const int32_t f = d.link_from_node_index[l], t = d.link_to_node_index[l];
+        const int32_t fn = lfn[l], tn = ltn[l];
+        L.link_from[k] = fn;
+        L.link_to[k] = tn;
         const double invf = d.node_invert_elevation_m[f], invt = d.node_invert_elevation_m[t];
         const double inv = d.link_invert_elevation_m ? (double)d.link_invert_elevation_m[l] : std::min(invf, invt);
-        L.lk0[l] = f4(d.link_length_m[l], (float)(invf - invt), (float)(0.5 * (invf + invt) - inv),
+        L.lk0[k] = f4(d.link_length_m[l], (float)(invf - invt), (float)(0.5 * (invf + invt) - inv),
                       std::max(d.link_manning_n[l], 0.0f));
         const float km = d.link_minor_loss_coefficient ? std::max(d.link_minor_loss_coefficient[l], 0.0f) : 0.0f;
-        L.lk1[l] = f4(d.link_diameter_m ? d.link_diameter_m[l] : 0.0f, d.link_area_m2[l], d.link_hydraulic_radius_m[l], km);
+        L.lk1[k] = f4(d.link_diameter_m ? d.link_diameter_m[l] : 0.0f, d.link_area_m2[l], d.link_hydraulic_radius_m[l], km);
         int flags = 0;
         if (d.link_diameter_m) flags |= 1;
         float W = 0.0f, H = 0.0f;
@@ -552,7 +569,7 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
             H = d.link_rect_height_m[l];
         }
         const float capq = d.link_flow_capacity_m3ps ? std::max(d.link_flow_capacity_m3ps[l], 0.0f) : INF;
-        L.lk2[l] = f4(capq, W, H, (float)flags);
+        L.lk2[k] = f4(capq, W, H, (float)flags);
         L.node_link_start[fn + 1]++;
         if (tn != fn) L.node_link_start[tn + 1]++;
     }
@@ -560,13 +577,14 @@ int build_drain_layout(const FlMeshDesc &m, const FlDrainDesc &d, HostLayout &L)
     L.nl.assign(L.node_link_start[N], make_int2(0, 0));
     {
         std::vector<int32_t> fill(L.node_link_start.begin(), L.node_link_start.end() - 1);
-        for (int32_t l = 0; l < NL; ++l) {  // ascending link order in every node's list
-            const int32_t f = L.link_from[l], t = L.link_to[l];
+        for (int32_t l = 0; l < NL; ++l) {  // reference link order in every node's list
+            const int32_t k = L.link_inv[l];
+            const int32_t f = L.link_from[k], t = L.link_to[k];
             if (t == f) {
-                L.nl[fill[f]++] = make_int2(l, (int32_t)((uint32_t)f | NL_FROM | NL_TO));
+                L.nl[fill[f]++] = make_int2(k, (int32_t)((uint32_t)f | NL_FROM | NL_TO));
             } else {
-                L.nl[fill[f]++] = make_int2(l, (int32_t)((uint32_t)t | NL_FROM));
-                L.nl[fill[t]++] = make_int2(l, (int32_t)((uint32_t)f | NL_TO));
+                L.nl[fill[f]++] = make_int2(k, (int32_t)((uint32_t)t | NL_FROM));
+                L.nl[fill[t]++] = make_int2(k, (int32_t)((uint32_t)f | NL_TO));
             }
         }
     }

@@ -55,8 +55,8 @@ cudaError_t launch_permute_f32(const float *src, float *dst, const int32_t *perm
                                cudaStream_t stream);
 cudaError_t launch_f64_to_ff(const double *src, float2 *dst, int32_t n, cudaStream_t stream);
 cudaError_t launch_ff_to_f64(const float2 *src, double *dst, int32_t n, cudaStream_t stream);
-cudaError_t launch_f64_to_f32(const double *src, float *dst, int32_t n, cudaStream_t stream);
-cudaError_t launch_f32_to_f64(const float *src, double *dst, int32_t n, cudaStream_t stream);
+cudaError_t launch_f64_to_f32_perm(const double *src, float *dst, const int32_t *perm, int32_t n, cudaStream_t stream);
+cudaError_t launch_f32_to_f64_perm(const float *src, double *dst, const int32_t *perm, int32_t n, cudaStream_t stream);
 cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *g1, const float2 *V, RunCtrl *run,
                            int32_t C, int32_t N, double *out2, cudaStream_t stream);
 cudaError_t launch_nodes(const NodeArgs &a, int slot, cudaStream_t stream);
@@ -116,6 +116,7 @@ struct FlSolver {
     DonorArgs dn{};
     NetArgs nw{};
     int32_t *node_perm = nullptr;  // node_perm[new] = reference node
+    int32_t *link_perm = nullptr;  // link_perm[new] = reference link
     float *stage_n = nullptr;      // [N] node-order staging
     char *drain_base = nullptr;    // the drainage arena (L2 access-policy window)
     size_t drain_bytes = 0;
@@ -623,11 +624,11 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
             const size_t I = (size_t)std::max(s->I, 1), N = (size_t)std::max(s->N, 1), NL = (size_t)std::max(s->NL, 1);
             const size_t K = (size_t)std::max(s->K, 1), G = (size_t)std::max(s->G, 1), S = L.nl.size() + 1;
             const size_t bytes = I * (4 + 8 + 16 + 8 + 8) + (K + 1) * 4 + K * 4 + (N + 1) * 4 * 2 + N * (4 + 16 + 4) +
-                                 G * 16 + S * 8 + NL * (4 * 2 + 16 * 3 + 4 * 3) + N * (8 * 2 + 4 + 4 + 4) +
+                                 G * 16 + S * 8 + NL * (4 * 3 + 16 * 3 + 4 * 3) + N * (8 * 2 + 4 + 4 + 4) +
                                  (size_t)(node_blocks(s->N) * 4 * D1_TERMS + network_blocks(s->G) * 4 * D2_TERMS) * 8 +
                                  (L.node_tstart.size() + L.node_tw.size()) * 4 + N * 8 +
                                  (L.tcell.size() + L.tcell_start.size()) * 4 + L.tcell_ent.size() * 8 +
-                                 L.tcell.size() * 8 + 64 * 256 +
+                                 L.tcell.size() * 8 + 80 * 256 +
                                  // the other members' node / link / inlet arrays and ledgers
                                  (Mz - 1) * (N * (8 * 2 + 4) + NL * (4 * 3) + I * 8 +
                                              (size_t)(node_blocks(s->N) * 4 * D1_TERMS + network_blocks(s->G) * 4 * D2_TERMS) * 8);
@@ -651,7 +652,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
             (rc = s->upload(&nd0, L.nd0)) || (rc = s->upload(&nd_capv, L.nd_capv)) || (rc = s->upload(&grp, L.grp)) ||
             (rc = s->upload(&nls, L.node_link_start)) || (rc = s->upload(&nl, L.nl)) ||
             (rc = s->upload(&lk0, L.lk0)) || (rc = s->upload(&lk1, L.lk1)) || (rc = s->upload(&lk2, L.lk2)) ||
-            (rc = s->upload(&s->node_perm, L.node_perm)))
+            (rc = s->upload(&s->node_perm, L.node_perm)) || (rc = s->upload(&s->link_perm, L.link_perm)))
             return rc;
         const size_t MN = Mz * (size_t)s->N, ML = Mz * (size_t)std::max(s->NL, 1);
         if ((rc = s->alloc(&s->Va, MN)) || (rc = s->alloc(&s->Vb, MN)) || (rc = s->alloc(&s->Q[0], ML)) ||
@@ -1126,7 +1127,7 @@ FL_API int fl_set_state(FlSolver *s, const float *h, const float *hu, const floa
     if (link_flow && s->NL > 0) {
         FL_CUDA(cudaStreamSynchronize(st));
         FL_CUDA(cudaMemcpyAsync(s->stage_d, link_flow, sizeof(double) * s->NL, k, st));
-        FL_CUDA(launch_f64_to_f32(s->stage_d, s->Q[s->run_h->parity], s->NL, st));
+        FL_CUDA(launch_f64_to_f32_perm(s->stage_d, s->Q[s->run_h->parity], s->link_perm, s->NL, st));
     }
     g_launches += (mask ? 1 : 0) + (wet_time ? 1 : 0) + (node_volume && s->N ? 1 : 0) + (link_flow && s->NL ? 1 : 0);
     FL_CUDA(cudaStreamSynchronize(st));
@@ -1161,7 +1162,7 @@ FL_API int fl_get_state(FlSolver *s, float *h, float *hu, float *hv, double *nod
         FL_CUDA(cudaStreamSynchronize(st));
     }
     if (link_flow && s->NL > 0) {
-        FL_CUDA(launch_f32_to_f64(s->Q[s->run_h->parity], s->stage_d, s->NL, st));
+        FL_CUDA(launch_f32_to_f64_perm(s->Q[s->run_h->parity], s->stage_d, s->link_perm, s->NL, st));
         FL_CUDA(cudaMemcpyAsync(link_flow, s->stage_d, sizeof(double) * s->NL, k, st));
         FL_CUDA(cudaStreamSynchronize(st));
     }

@@ -397,12 +397,14 @@ __global__ void k_ff_to_f64_perm(const float2 *src, double *dst, const int32_t *
     }
 }
 
-__global__ void k_f64_to_f32(const double *src, float *dst, int32_t n) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = (float)src[i];
+// Link flows between the reference's link order (host side) and the
+// solver's (perm[new] = reference link).
+__global__ void k_f64_to_f32_perm(const double *src, float *dst, const int32_t *perm, int32_t n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = (float)src[perm[i]];
 }
 
-__global__ void k_f32_to_f64(const float *src, double *dst, int32_t n) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = (double)src[i];
+__global__ void k_f32_to_f64_perm(const float *src, double *dst, const int32_t *perm, int32_t n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[perm[i]] = (double)src[i];
 }
 
 // Current surface volume sum(h * area) and node volume (float64 partials).
@@ -525,13 +527,13 @@ cudaError_t launch_ff_to_f64_perm(const float2 *src, double *dst, const int32_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_f64_to_f32(const double *src, float *dst, int32_t n, cudaStream_t stream) {
-    k_f64_to_f32<<<304, 256, 0, stream>>>(src, dst, n);
+cudaError_t launch_f64_to_f32_perm(const double *src, float *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
+    k_f64_to_f32_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_f32_to_f64(const float *src, double *dst, int32_t n, cudaStream_t stream) {
-    k_f32_to_f64<<<304, 256, 0, stream>>>(src, dst, n);
+cudaError_t launch_f32_to_f64_perm(const float *src, double *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
+    k_f32_to_f64_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
     return cudaGetLastError();
 }
 

@@ -181,7 +181,7 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
         lr: float = 1e-3, audit: float = 0.05, n_layers: int = 8, plain_sample: int = 8, batch_size: int = 64,
         duration_cap_h: float | None = None, train_seconds: float | None = None, log=print, weights_out=None,
         baselines: bool = False, n_models: int = 2, n_val: int = 32, flag_fraction: float = 0.04,
-        extent_weight: float = 3.0, pushforward: float = 0.5):
+        extent_weight: float = 3.0, pushforward: float = 0.5, train_batch: int = 1):
     """Train an ensemble of n_models networks on n_train - n_val solver
     trajectories, calibrate the flag threshold on the other n_val, then screen
     n_eval held-out storms."""
@@ -198,7 +198,7 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
     ev_storms, ev_dur = _storms(n_eval, seed + 2, duration_cap_h)
     res = {"mesh_cells": mf.C, "dual_edges": mf.graph.E, "train_members": n_train - n_val, "validation_members": n_val,
            "eval_members": n_eval, "layers": n_layers, "hidden": 128, "ensemble_networks": n_models,
-           "extent_weight": extent_weight, "pushforward": pushforward}
+           "extent_weight": extent_weight, "pushforward": pushforward, "train_batch": train_batch, "lr": lr}
     t = time.perf_counter()
     trajs, solve_s, tr_hours = solve_members(city, cfg, tr_storms, tr_dur, batch_size)
     res["train_data"] = {"solver_s": solve_s, "scenario_hours": tr_hours, "wall_s": time.perf_counter() - t}
@@ -211,7 +211,8 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
         m = MPNN(n_layers=n_layers, seed=seed + 1000 * k)
         forced.append([])
         hists.append(train(m, mf, fit, epochs=epochs, lr=lr, seed=seed + k, log=log, max_seconds=train_seconds,
-                           extent_weight=extent_weight, pushforward=pushforward, teacher=forced[-1]))
+                           extent_weight=extent_weight, pushforward=pushforward, teacher=forced[-1],
+                           batch=train_batch))
         models.append(m)
     torch.cuda.synchronize()
     res["train"] = {"seconds": time.perf_counter() - t, "epochs": [len(h) for h in hists], "loss": hists,
@@ -312,6 +313,8 @@ def main():
     p.add_argument("--train", type=int, default=512)
     p.add_argument("--eval", type=int, default=1024)
     p.add_argument("--epochs", type=int, default=8)
+    p.add_argument("--lr", type=float, default=1e-3)
+    p.add_argument("--train-batch", type=int, default=1, help="windows per optimizer step")
     p.add_argument("--layers", type=int, default=8)
     p.add_argument("--seed", type=int, default=11)
     p.add_argument("--duration-cap-h", type=float, default=None)
@@ -338,9 +341,9 @@ def main():
                 f.write(text)
         print(text)
         return
-    res = run(a.grid_n, a.train, a.eval, a.seed, a.epochs, n_layers=a.layers, duration_cap_h=a.duration_cap_h,
-              train_seconds=a.train_seconds, weights_out=a.weights, n_models=a.networks,
-              flag_fraction=a.flag_fraction)
+    res = run(a.grid_n, a.train, a.eval, a.seed, a.epochs, lr=a.lr, n_layers=a.layers,
+              duration_cap_h=a.duration_cap_h, train_seconds=a.train_seconds, weights_out=a.weights,
+              n_models=a.networks, flag_fraction=a.flag_fraction, train_batch=a.train_batch)
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:

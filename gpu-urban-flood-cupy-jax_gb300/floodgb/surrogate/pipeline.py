@@ -211,7 +211,7 @@ def loss_weights(mf: MeshFeatures, depths, extent_weight: float):
 
 def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: float = 1e-3, seed: int = 0,
           log=None, max_seconds: float | None = None, extent_weight: float = 3.0, pushforward: float = 0.5,
-          teacher: list | None = None):
+          teacher: list | None = None, batch: int = 1):
     """Full-graph steps over every window of every trajectory; weighted MSE on
     active cells.  From the second epoch, a window after the first starts
     with probability `pushforward` from the network's own one-window
@@ -223,7 +223,16 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
     epoch has no pushforward windows, so that figure rises when they start;
     `teacher`, when given, receives each epoch's mean loss over the windows
     that started from the solver's state, which is comparable across
-    epochs."""
+    epochs.
+
+    With batch > 1 every optimizer step takes `batch` windows in one pass
+    over the replicated graph (the mean of their losses, each normalised by
+    its own weights); the single-window step is launch-bound on a mesh of
+    this size, so a batch costs little more than one window."""
+
+    if batch > 1:
+        return _train_batched(model, mf, trajectories, epochs, lr, seed, log, max_seconds, extent_weight,
+                              pushforward, teacher, batch)
 
     import torch
 
@@ -262,6 +271,94 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
                 forced += loss
                 n_forced += 1
             dy[:, :N_OUT] = wts * diff * (2.0 / norm)
+            model.zero_grad()
+            model.backward(g, x, dy)
+            model.step(rate)
+            k += 1
+        history.append(float(total.item()) / len(samples))
+        if teacher is not None:
+            teacher.append(float(forced.item()) / max(n_forced, 1))
+        if log:
+            log(f"epoch {ep}: loss {history[-1]:.5f}")
+        if max_seconds is not None and time.perf_counter() - t_start > max_seconds:
+            break
+    ops.status()
+    return history
+
+
+def _train_batched(model: MPNN, mf: MeshFeatures, trajectories, epochs, lr, seed, log, max_seconds, extent_weight,
+                   pushforward, teacher, batch):
+    import torch
+
+    rng = np.random.default_rng(seed)
+    C = mf.C
+    samples = [(tr, w) for tr in trajectories for w in transitions(tr)]
+    trans = {id(tr): transitions(tr) for tr in trajectories}
+    act = mf.active_dev
+    graphs, grads = {}, {}
+
+    def graph(b):
+        if b not in graphs:
+            graphs[b] = mf.graph.replicate(b)
+            grads[b] = torch.zeros(b * C, FOUT, device=mf.device)
+        return graphs[b], grads[b]
+
+    history = []
+    per_epoch = (len(samples) + batch - 1) // batch
+    steps = epochs * per_epoch
+    k = 0
+    t_start = time.perf_counter()
+    for ep in range(epochs):
+        total = torch.zeros((), device=mf.device)
+        forced = torch.zeros((), device=mf.device)
+        n_forced = 0
+        order = rng.permutation(len(samples))
+        for b0 in range(0, len(samples), batch):
+            idx = order[b0:b0 + batch]
+            B = len(idx)
+            rate = lr * 0.5 * (1.0 + math.cos(math.pi * k / max(steps, 1)))  # cosine decay
+            push = [bool(ep > 0 and samples[i][1][0] > 0 and rng.random() < pushforward) for i in idx]
+            states = [None] * B
+            if any(push):
+                # the network's own one-window predictions from the solver's
+                # state a window earlier, in one pass at the batch's size (the
+                # windows that start from the solver's state repeat a pushed one)
+                src = [j if push[j] else push.index(True) for j in range(B)]
+                xs = []
+                for j in src:
+                    tr, w = samples[idx[j]]
+                    xs.append(sample_tensors(mf, tr, trans[id(tr)][w[0] - 1])[0])
+                gp, _ = graph(B)
+                with torch.no_grad():
+                    yp = model.forward(gp, torch.cat(xs), train=False)
+                    for j in range(B):
+                        if push[j]:
+                            tr, w = samples[idx[j]]
+                            hn, hmn, hun, hvn = advance(yp[j * C:(j + 1) * C], tr.h[w[0] - 1], act)
+                            states[j] = (hn.clone(), hun.clone(), hvn.clone(), hmn.clone())
+            xs, ys, ws, norms = [], [], [], []
+            for j in range(B):
+                tr, w = samples[idx[j]]
+                x, yt, depths = sample_tensors(mf, tr, w, states[j])
+                wt = loss_weights(mf, depths, extent_weight)
+                xs.append(x)
+                ys.append(yt)
+                ws.append(wt)
+                norms.append(wt.sum())
+            g, dy = graph(B)
+            x = torch.cat(xs)
+            wts = torch.cat(ws)
+            norm = torch.stack(norms)
+            y = model.forward(g, x)
+            diff = y[:, :N_OUT] - torch.cat(ys)
+            per = (wts * diff * diff).view(B, C, N_OUT).sum((1, 2)) / norm
+            total += per.sum()
+            keep = [j for j in range(B) if not push[j]]
+            if keep:
+                forced += per[keep].sum()
+                n_forced += len(keep)
+            scale = (2.0 / (norm * B)).repeat_interleave(C)[:, None]
+            dy[:, :N_OUT] = wts * diff * scale
             model.zero_grad()
             model.backward(g, x, dy)
             model.step(rate)

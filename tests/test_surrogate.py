@@ -264,3 +264,54 @@ def test_ensemble_rollouts_equal_member_rollouts():
         want = np.sqrt(np.mean([(a[2][:, act] - mean[:, act]) ** 2 for a in alone]))
         assert abs(spread[i] - want) <= 1e-6 + 1e-4 * want, (i, spread[i], want)
         assert spread[i] > 0
+
+
+@pytest.mark.gpu
+def test_replicated_graph_gradient_is_the_sum_of_window_gradients():
+    """The batched training step: one forward and backward pass over two
+    copies of the graph gives each parameter the sum of the two windows'
+    gradients taken one by one."""
+
+    torch = pytest.importorskip("torch")
+    from floodgb import native
+    from floodgb.build import build_library
+    from floodgb.surrogate.model import MPNN, DualGraph
+    from floodgb.synthetic import make_grid_city
+
+    build_library()
+    native.load()
+    if native.device_count() < 1:
+        pytest.skip("no CUDA device")
+    topo = make_grid_city(n=9, size_m=90.0, seed=4).city.topologies.surface_topology
+    g = DualGraph(topo)
+    g2 = g.replicate(2)
+    net = MPNN(n_layers=2, seed=7)
+    rng = np.random.default_rng(2)
+    xs, dys = [], []
+    for _ in range(2):
+        x = np.zeros((g.C, SO.FIN), np.float32)
+        x[:, :12] = rng.normal(size=(g.C, 12))
+        xs.append(torch.as_tensor(x, device="cuda").to(torch.bfloat16).contiguous())
+        dy = torch.zeros(g.C, SO.FOUT, device="cuda")
+        dy[:, :4] = torch.as_tensor(rng.normal(0, 1e-2, (g.C, 4)).astype(np.float32), device="cuda")
+        dys.append(dy)
+    single = []
+    for x, dy in zip(xs, dys):
+        net.zero_grad()
+        net.forward(g, x)
+        net.backward(g, x, dy)
+        single.append([(d.gw.clone(), d.gb.clone()) for d in net.layers()])
+    net.zero_grad()
+    xb = torch.cat(xs).contiguous()
+    yb = net.forward(g2, xb).clone()
+    net.backward(g2, xb, torch.cat(dys))
+    torch.cuda.synchronize()
+    for k, d in enumerate(net.layers()):
+        for got, a, b in ((d.gw, single[0][k][0], single[1][k][0]), (d.gb, single[0][k][1], single[1][k][1])):
+            want = (a + b).cpu().numpy()
+            err = np.linalg.norm(got.cpu().numpy() - want) / max(np.linalg.norm(want), 1e-12)
+            assert err < 1e-3, (k, err)
+    # and the forward pass of each copy is the window's own
+    for j, x in enumerate(xs):
+        y = net.forward(g, x, train=False)
+        np.testing.assert_allclose(yb[j * g.C:(j + 1) * g.C].cpu().numpy(), y.cpu().numpy(), atol=1e-5, rtol=1e-5)
