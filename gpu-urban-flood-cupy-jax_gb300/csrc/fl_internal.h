@@ -94,6 +94,7 @@ struct HyetoView {
 
 // Ledger slots of the per-warp running sums (float-float pairs).
 constexpr int SURF_TERMS = 4;   // rain, infil, boundary in, boundary out
+constexpr int VOL_BLOCKS = 304;  // blocks of the volume reduction (each writes one partial pair)
 constexpr int D1_TERMS = 2;     // capture, surcharge
 constexpr int D2_TERMS = 4;     // outfall, overflow, unreturned, link |transfer|
 

