@@ -82,12 +82,14 @@ __global__ void __launch_bounds__(256) k_segment_sum(const float *__restrict__ s
             const float4 v = *(const float4 *)(src + row * lds + col0 + c);
             acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
         }
-        float4 *d = (float4 *)(dst + (int64_t)warp * ldd + c);
-        if (accumulate) {
-            const float4 o = *d;
-            acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
+        if (dst) {  // (null: the bf16 copy only, for inference)
+            float4 *d = (float4 *)(dst + (int64_t)warp * ldd + c);
+            if (accumulate) {
+                const float4 o = *d;
+                acc.x += o.x; acc.y += o.y; acc.z += o.z; acc.w += o.w;
+            }
+            *d = acc;
         }
-        *d = acc;
         if (dst_bf16) {
             __nv_bfloat162 h0 = __floats2bfloat162_rn(acc.x, acc.y), h1 = __floats2bfloat162_rn(acc.z, acc.w);
             uint2 w;
@@ -209,9 +211,10 @@ FL_API int fl_transpose_bf16(const FlGemmSegment *segs, int32_t n_seg, int32_t m
 FL_API int fl_segment_sum(const float *src, int64_t lds, int32_t col0, const int32_t *start, const int32_t *order,
                           int32_t n_out, int32_t width, float *dst, int64_t ldd, void *dst_bf16, int64_t ldb,
                           int32_t accumulate, void *stream) {
-    FM_CHECK(src && start && dst && n_out >= 1 && width > 0 && width % 4 == 0 && lds % 4 == 0 && ldd % 4 == 0 &&
-                 col0 % 4 == 0 && (!dst_bf16 || ldb % 4 == 0),
-             "fl_segment_sum: bad arguments (widths and strides must be multiples of 4)");
+    FM_CHECK(src && start && (dst || (dst_bf16 && !accumulate)) && n_out >= 1 && width > 0 && width % 4 == 0 &&
+                 lds % 4 == 0 && ldd % 4 == 0 && col0 % 4 == 0 && (!dst_bf16 || ldb % 4 == 0),
+             "fl_segment_sum: bad arguments (widths and strides must be multiples of 4; a null dst needs "
+             "dst_bf16 and no accumulation)");
     const int64_t threads = (int64_t)n_out * 32;
     k_segment_sum<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
         src, lds, col0, start, order, n_out, width, dst, ldd, (__nv_bfloat16 *)dst_bf16, ldb, accumulate);

@@ -181,7 +181,6 @@ class Workspace:
         self.zd = bf(C, H)
         self.y = f32(C, FOUT)
         self.m_f32 = f32(E, H)
-        self.agg_f32 = f32(C, H)
         if not train:
             return
         # backward scratch
@@ -257,7 +256,8 @@ class MPNN:
             ops.gemm([(hb, g.dst, H), (hb, g.src, H), (ws.e_bf, None, H)], e1.w_bf, bias=e1.b, out_bf16=ws.z1e[k],
                      relu=True)
             ops.gemm([(ws.z1e[k], None, H)], e2.w_bf, bias=e2.b, out_f32=ws.m_f32)
-            ops.segment_sum(ws.m_f32, 0, g.recv_start, None, C, H, ws.agg_f32, dst_bf16=ws.agg_bf[k])
+            # aggregation, written as bf16 only: both the next GEMM and backward read that copy
+            ops.segment_sum(ws.m_f32, 0, g.recv_start, None, C, H, None, dst_bf16=ws.agg_bf[k])
             ops.gemm([(hb, None, H), (ws.agg_bf[k], None, H)], n1.w_bf, bias=n1.b, out_bf16=ws.z1n[k], relu=True)
             ops.gemm([(ws.z1n[k], None, H)], n2.w_bf, bias=n2.b, residual=ws.h_f32[cur], out_f32=ws.h_f32[cur ^ 1],
                      out_bf16=ws.h_bf[(l + 1) % nh])

@@ -89,8 +89,9 @@ def transpose(segments, m, dst):
 
 
 def segment_sum(src, col0, start, order, n_out, width, dst, dst_bf16=None, accumulate=False):
+    """Fixed-order row sums; dst None (with dst_bf16, no accumulation) writes the bf16 copy only."""
     N.check(N.load().fl_segment_sum(C.c_void_p(src.data_ptr()), src.stride(0), int(col0), C.c_void_p(start.data_ptr()),
-                                    _ptr(order), int(n_out), int(width), C.c_void_p(dst.data_ptr()), dst.stride(0),
+                                    _ptr(order), int(n_out), int(width), _ptr(dst), dst.stride(0) if dst is not None else 4,
                                     _ptr(dst_bf16), dst_bf16.stride(0) if dst_bf16 is not None else 0,
                                     int(bool(accumulate)), _stream()), "fl_segment_sum")
 

@@ -412,7 +412,8 @@ FL_API int fl_gemm_status(void *stream);
  * fl_transpose_bf16: dst[k, r] = A[r, k] for the segment concatenation A
  *   (as fl_gemm_bf16's A), columns m..ldd-1 of dst set to 0.
  * fl_segment_sum: dst[i, :width] (+)= sum over p in [start[i], start[i+1]) of
- *   src[order ? order[p] : p, col0 : col0+width]; optional bf16 copy.
+ *   src[order ? order[p] : p, col0 : col0+width]; optional bf16 copy (with
+ *   the bf16 copy and no accumulation, dst may be NULL: bf16 only).
  * fl_relu_bwd: out = dx * (z > 0) (z NULL: no mask), bf16 (+ fp32).
  * fl_colsum: out[c] (+)= sum_r x[r, c]; scratch holds 256 x n floats.
  * fl_adam: Adam step on fp32 w[rows, cols]; refreshes w_bf16 and its
