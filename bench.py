@@ -157,8 +157,10 @@ def measured_peak_hbm():
 # from; a kernel whose sources changed since its capture reports null.
 SURFACE_SOURCES = ("fl_surface.cu", "fl_device.cuh", "fl_internal.h")
 SURFACE_TRAFFIC_CAPTURES = {
-    # two launches at the wet state after 900 s: 74.78 + 2.93 MB and 74.78 + 2.50 MB
+    # two launches at the wet state after 900 s: 74.78 + 2.93 MB and 74.78 + 2.50 MB (549-CTA grid)
     "8643f7e5e23436c8": 77_498_240,
+    # the same with the grid over every CTA slot: 74.80 + 2.54 MB and 74.80 + 2.83 MB
+    "c4a68efc35e9b1cd": 77_481_984,
 }
 
 

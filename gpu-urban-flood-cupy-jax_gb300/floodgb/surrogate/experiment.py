@@ -88,7 +88,7 @@ def screen(models, mf, city, cfg, threshold: float, storms, durations, *, audit:
     def run_audit():
         side = torch.cuda.Stream()
         audit_out["r"] = solve_members(city, cfg, [storms[i] for i in a_idx], [durations[i] for i in a_idx],
-                                       batch_size, stream=side)
+                                       batch_size, stream=side, device="cpu")
 
     t = time.perf_counter()
     worker = threading.Thread(target=run_audit) if rerun == "overlap" else None
@@ -108,20 +108,21 @@ def screen(models, mf, city, cfg, threshold: float, storms, durations, *, audit:
     hours = float(sum(durations)) / 3600.0
     flagged = flags(spread, threshold)
     # the members the solver re-runs now: with the audit already re-run, the flagged rest
+    # (re-run trajectories stay in host memory: they are only scored)
     f_idx = np.flatnonzero(flagged & ~audited) if worker is not None else np.flatnonzero(flagged | audited)
     t = time.perf_counter()
     flag_trajs, flag_solver_s = [], 0.0
     if f_idx.size:
         flag_trajs, flag_solver_s, _ = solve_members(city, cfg, [storms[i] for i in f_idx],
                                                      [durations[i] for i in f_idx],
-                                                     batch_size if worker is not None else rerun_batch)
+                                                     batch_size if worker is not None else rerun_batch, device="cpu")
     torch.cuda.synchronize()
     flag_s = time.perf_counter() - t
     re_solved = {int(i): tr for i, tr in zip(a_idx, audit_trajs)}
     re_solved.update({int(i): tr for i, tr in zip(f_idx, flag_trajs)})
     rerun_h = float(sum(durations[i] for i in re_solved)) / 3600.0
     if score_all:
-        truth, batched_s, _ = solve_members(city, cfg, storms, durations, batch_size)
+        truth, batched_s, _ = solve_members(city, cfg, storms, durations, batch_size, device="cpu")
         scores = [score(mf, p, tr, extent_threshold=extent_threshold) for p, tr in zip(preds, truth)]
         scored = np.ones(n, bool)
     else:

@@ -125,8 +125,8 @@ def windows(duration_s: float) -> list[tuple[float, float]]:
 # ------------------------------------------------------------------ data
 def solve_members(city, cfg, storms, durations_s, batch_size: int = 64, shape=None, device: str = "cuda",
                   stream=None):
-    """Solver trajectories (hourly snapshots, window maxima and momenta, kept
-    on the device) of storms on one mesh, batched; returns (trajectories in
+    """Solver trajectories (hourly snapshots, window maxima and momenta, as
+    tensors on `device`) of storms on one mesh, batched; returns (trajectories in
     the order of `storms`, solver seconds, scenario hours).  A batch runs
     until its longest member ends, so members go into batches longest storm
     first.  With `stream` the solver runs on that stream (and only it is
