@@ -502,56 +502,68 @@ cudaError_t launch_replan(RunCtrl *run, double *snap_t, HyetoView hy, StepCtrl *
     return cudaGetLastError();
 }
 
+// Grid of the grid-stride helper kernels below: enough 256-thread blocks for
+// n elements, at most `per_sm` blocks per SM of the current device.
+static int helper_grid(int64_t n, int per_sm) {
+    static int sms[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    if (sms[dev] == 0 && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms[dev] = 1;
+    const int64_t want = std::max<int64_t>(1, (n + 255) / 256);
+    return (int)std::min<int64_t>(want, (int64_t)std::max(sms[dev], 1) * per_sm);
+}
+
 cudaError_t launch_finite(const float4 *s0, const float4 *s1, RunCtrl *run, int32_t C, cudaStream_t stream) {
-    k_finite<<<608, 256, 0, stream>>>(s0, s1, run, C);
+    k_finite<<<helper_grid(C, 4), 256, 0, stream>>>(s0, s1, run, C);
     return cudaGetLastError();
 }
 
 cudaError_t launch_load_state(float4 *state, const float *h, const float *hu, const float *hv, const float *bed,
                               const int32_t *perm, int32_t C, int mask, cudaStream_t stream) {
-    k_load_state<<<608, 256, 0, stream>>>(state, h, hu, hv, bed, perm, C, mask);
+    k_load_state<<<helper_grid(C, 4), 256, 0, stream>>>(state, h, hu, hv, bed, perm, C, mask);
     return cudaGetLastError();
 }
 
 cudaError_t launch_store_state(const float4 *state, float *h, float *hu, float *hv, const int32_t *perm, int32_t C,
                                cudaStream_t stream) {
-    k_store_state<<<608, 256, 0, stream>>>(state, h, hu, hv, perm, C);
+    k_store_state<<<helper_grid(C, 4), 256, 0, stream>>>(state, h, hu, hv, perm, C);
     return cudaGetLastError();
 }
 
 cudaError_t launch_permute_f32(const float *src, float *dst, const int32_t *perm, int32_t C, int to_reference,
                                cudaStream_t stream) {
-    k_permute_f32<<<608, 256, 0, stream>>>(src, dst, perm, C, to_reference);
+    k_permute_f32<<<helper_grid(C, 4), 256, 0, stream>>>(src, dst, perm, C, to_reference);
     return cudaGetLastError();
 }
 
 cudaError_t launch_f64_to_ff(const double *src, float2 *dst, int32_t n, cudaStream_t stream) {
-    k_f64_to_ff<<<304, 256, 0, stream>>>(src, dst, n);
+    k_f64_to_ff<<<helper_grid(n, 2), 256, 0, stream>>>(src, dst, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ff_to_f64(const float2 *src, double *dst, int32_t n, cudaStream_t stream) {
-    k_ff_to_f64<<<304, 256, 0, stream>>>(src, dst, n);
+    k_ff_to_f64<<<helper_grid(n, 2), 256, 0, stream>>>(src, dst, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_f64_to_ff_perm(const double *src, float2 *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
-    k_f64_to_ff_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
+    k_f64_to_ff_perm<<<helper_grid(n, 2), 256, 0, stream>>>(src, dst, perm, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ff_to_f64_perm(const float2 *src, double *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
-    k_ff_to_f64_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
+    k_ff_to_f64_perm<<<helper_grid(n, 2), 256, 0, stream>>>(src, dst, perm, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_f64_to_f32_perm(const double *src, float *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
-    k_f64_to_f32_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
+    k_f64_to_f32_perm<<<helper_grid(n, 2), 256, 0, stream>>>(src, dst, perm, n);
     return cudaGetLastError();
 }
 
 cudaError_t launch_f32_to_f64_perm(const float *src, double *dst, const int32_t *perm, int32_t n, cudaStream_t stream) {
-    k_f32_to_f64_perm<<<304, 256, 0, stream>>>(src, dst, perm, n);
+    k_f32_to_f64_perm<<<helper_grid(n, 2), 256, 0, stream>>>(src, dst, perm, n);
     return cudaGetLastError();
 }
 
