@@ -161,6 +161,8 @@ SURFACE_TRAFFIC_CAPTURES = {
     "8643f7e5e23436c8": 77_498_240,
     # the same with the grid over every CTA slot: 74.80 + 2.54 MB and 74.80 + 2.83 MB
     "c4a68efc35e9b1cd": 77_481_984,
+    # helper kernels sized from the SM count (k_surface unchanged): 74.80 + 2.55 MB and 74.80 + 2.82 MB
+    "f8cff34baccfde73": 77_484_672,
 }
 
 
