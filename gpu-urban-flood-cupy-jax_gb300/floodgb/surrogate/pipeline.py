@@ -209,6 +209,16 @@ def loss_weights(mf: MeshFeatures, depths, extent_weight: float):
     return w * act
 
 
+def cosine(progress: float, t_start: float, max_seconds: float | None) -> float:
+    """Cosine learning-rate factor at the larger of the step progress and,
+    with a time budget, the fraction of it spent: training stopped by the
+    budget ends with the rate decayed as if its last epoch were planned."""
+
+    if max_seconds:
+        progress = max(progress, (time.perf_counter() - t_start) / max_seconds)
+    return 0.5 * (1.0 + math.cos(math.pi * min(progress, 1.0)))
+
+
 def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: float = 1e-3, seed: int = 0,
           log=None, max_seconds: float | None = None, extent_weight: float = 3.0, pushforward: float = 0.5,
           teacher: list | None = None, batch: int = 1):
@@ -223,7 +233,8 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
     epoch has no pushforward windows, so that figure rises when they start;
     `teacher`, when given, receives each epoch's mean loss over the windows
     that started from the solver's state, which is comparable across
-    epochs.
+    epochs.  With `max_seconds` training stops when that much time is
+    spent (within an epoch too), the cosine rate decaying over the budget.
 
     With batch > 1 every optimizer step takes `batch` windows in one pass
     over the replicated graph (the mean of their losses, each normalised by
@@ -248,9 +259,11 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
     for ep in range(epochs):
         total = torch.zeros((), device=mf.device)
         forced = torch.zeros((), device=mf.device)
-        n_forced = 0
+        n_forced = n_done = 0
         for i in rng.permutation(len(samples)):
-            rate = lr * 0.5 * (1.0 + math.cos(math.pi * k / max(steps, 1)))  # cosine decay
+            if max_seconds is not None and time.perf_counter() - t_start > max_seconds:
+                break
+            rate = lr * cosine(k / max(steps, 1), t_start, max_seconds)
             tr, w = samples[i]
             state = None
             if ep > 0 and w[0] > 0 and rng.random() < pushforward:
@@ -275,7 +288,10 @@ def train(model: MPNN, mf: MeshFeatures, trajectories, epochs: int = 10, lr: flo
             model.backward(g, x, dy)
             model.step(rate)
             k += 1
-        history.append(float(total.item()) / len(samples))
+            n_done += 1
+        if n_done == 0:
+            break
+        history.append(float(total.item()) / n_done)
         if teacher is not None:
             teacher.append(float(forced.item()) / max(n_forced, 1))
         if log:
@@ -311,12 +327,14 @@ def _train_batched(model: MPNN, mf: MeshFeatures, trajectories, epochs, lr, seed
     for ep in range(epochs):
         total = torch.zeros((), device=mf.device)
         forced = torch.zeros((), device=mf.device)
-        n_forced = 0
+        n_forced = n_done = 0
         order = rng.permutation(len(samples))
         for b0 in range(0, len(samples), batch):
+            if max_seconds is not None and time.perf_counter() - t_start > max_seconds:
+                break
             idx = order[b0:b0 + batch]
             B = len(idx)
-            rate = lr * 0.5 * (1.0 + math.cos(math.pi * k / max(steps, 1)))  # cosine decay
+            rate = lr * cosine(k / max(steps, 1), t_start, max_seconds)
             push = [bool(ep > 0 and samples[i][1][0] > 0 and rng.random() < pushforward) for i in idx]
             states = [None] * B
             if any(push):
@@ -363,7 +381,10 @@ def _train_batched(model: MPNN, mf: MeshFeatures, trajectories, epochs, lr, seed
             model.backward(g, x, dy)
             model.step(rate)
             k += 1
-        history.append(float(total.item()) / len(samples))
+            n_done += B
+        if n_done == 0:
+            break
+        history.append(float(total.item()) / n_done)
         if teacher is not None:
             teacher.append(float(forced.item()) / max(n_forced, 1))
         if log:
