@@ -316,3 +316,19 @@ def test_replicated_graph_gradient_is_the_sum_of_window_gradients():
     for j, x in enumerate(xs):
         y = net.forward(g, x, train=False)
         np.testing.assert_allclose(yb[j * g.C:(j + 1) * g.C].cpu().numpy(), y.cpu().numpy(), atol=1e-5, rtol=1e-5)
+
+
+def test_cosine_schedule_with_and_without_a_time_budget():
+    import time
+
+    from floodgb.surrogate.pipeline import cosine
+
+    t0 = time.perf_counter()
+    assert cosine(0.0, t0, None) == 1.0
+    assert abs(cosine(0.5, t0, None) - 0.5) < 1e-12
+    assert abs(cosine(1.0, t0, None)) < 1e-12
+    # a budget already spent: the rate has decayed whatever the step progress
+    assert abs(cosine(0.1, t0 - 10.0, 5.0)) < 1e-12
+    # half the budget spent, a tenth of the steps done: the later of the two sets the rate
+    r = cosine(0.1, time.perf_counter() - 5.0, 10.0)
+    assert 0.45 < r < 0.5
