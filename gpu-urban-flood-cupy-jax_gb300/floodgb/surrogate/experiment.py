@@ -182,7 +182,7 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
         lr: float = 1e-3, audit: float = 0.05, n_layers: int = 8, plain_sample: int = 8, batch_size: int = 64,
         duration_cap_h: float | None = None, train_seconds: float | None = None, log=print, weights_out=None,
         baselines: bool = False, n_models: int = 2, n_val: int = 32, flag_fraction: float = 0.04,
-        extent_weight: float = 3.0, pushforward: float = 0.5, train_batch: int = 1):
+        extent_weight: float = 3.0, pushforward: float = 0.5, train_batch: int = 1, score_all: bool = True):
     """Train an ensemble of n_models networks on n_train - n_val solver
     trajectories, calibrate the flag threshold on the other n_val, then screen
     n_eval held-out storms."""
@@ -233,7 +233,7 @@ def run(grid_n: int = 224, n_train: int = 512, n_eval: int = 1024, seed: int = 1
     del trajs, fit, val
     res.update(screen(models, mf, city, cfg, cal["threshold_m"], ev_storms, ev_dur, audit=audit, seed=seed,
                       plain_sample=plain_sample, batch_size=batch_size, baselines=baselines, n_layers=n_layers,
-                      extent_threshold=cal["extent_threshold_m"]))
+                      extent_threshold=cal["extent_threshold_m"], score_all=score_all))
     if weights_out:
         save(weights_out, models, cal, limits, {"grid_n": grid_n, "seed": seed, "n_layers": n_layers,
                                                 "n_train": n_train, "n_val": n_val})
@@ -328,6 +328,9 @@ def main():
     p.add_argument("--rerun", choices=("after", "overlap"), default="after")
     p.add_argument("--rerun-batch", type=int, default=128)
     p.add_argument("--score-all", action="store_true", help="with --screen-only: solve and score every member")
+    p.add_argument("--rerun-scores-only", action="store_true",
+                   help="training run: score only the re-solved (flagged and audited) members")
+    p.add_argument("--plain-sample", type=int, default=8)
     p.add_argument("--recalibrate", default=None, help="recompute a saved ensemble's extent threshold in place")
     a = p.parse_args()
     if a.recalibrate:
@@ -344,7 +347,8 @@ def main():
         return
     res = run(a.grid_n, a.train, a.eval, a.seed, a.epochs, lr=a.lr, n_layers=a.layers,
               duration_cap_h=a.duration_cap_h, train_seconds=a.train_seconds, weights_out=a.weights,
-              n_models=a.networks, flag_fraction=a.flag_fraction, train_batch=a.train_batch)
+              n_models=a.networks, flag_fraction=a.flag_fraction, train_batch=a.train_batch,
+              score_all=not a.rerun_scores_only, plain_sample=a.plain_sample)
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:
