@@ -311,13 +311,13 @@ def _train_batched(model: MPNN, mf: MeshFeatures, trajectories, epochs, lr, seed
     samples = [(tr, w) for tr in trajectories for w in transitions(tr)]
     trans = {id(tr): transitions(tr) for tr in trajectories}
     act = mf.active_dev
-    graphs, grads = {}, {}
+    graphs, dys = {}, {}  # per batch size: the replicated graph and the output-gradient buffer
 
     def graph(b):
         if b not in graphs:
             graphs[b] = mf.graph.replicate(b)
-            grads[b] = torch.zeros(b * C, FOUT, device=mf.device)
-        return graphs[b], grads[b]
+            dys[b] = torch.zeros(b * C, FOUT, device=mf.device)
+        return graphs[b], dys[b]
 
     history = []
     per_epoch = (len(samples) + batch - 1) // batch
