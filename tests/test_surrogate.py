@@ -332,3 +332,57 @@ def test_cosine_schedule_with_and_without_a_time_budget():
     # half the budget spent, a tenth of the steps done: the later of the two sets the rate
     r = cosine(0.1, time.perf_counter() - 5.0, 10.0)
     assert 0.45 < r < 0.5
+
+
+class _FakeNet:
+    """A stand-in network on CPU tensors: depth change from the coming
+    window's rain and the current depth, a fixed window maximum above it,
+    momenta from the depth; enough to check the rollout bookkeeping."""
+
+    def __init__(self, k):
+        self.k = k
+
+    def forward(self, g, x, train=False):
+        import torch
+
+        x = x.float()
+        y = torch.zeros(g.C, 64)
+        y[:, 0] = self.k * x[:, 8] - 0.1 * x[:, 0]
+        y[:, 1] = 0.02 * self.k + 0.01 * x[:, 9]
+        y[:, 2] = 0.5 * x[:, 0]
+        y[:, 3] = -0.25 * x[:, 0]
+        return y
+
+
+def test_ensemble_bookkeeping_against_member_rollouts_on_cpu():
+    """Grouping by window count, padding windows and the device-side mean and
+    disagreement of ensemble_rollouts against each network's rollout() of
+    each member alone (a fake network, CPU tensors)."""
+
+    pytest.importorskip("torch")
+    from floodgb.rainfall import rainfall_event
+    from floodgb.surrogate.pipeline import MeshFeatures, ensemble_rollouts, rollout
+    from floodgb.synthetic import make_grid_city
+
+    mf = MeshFeatures(make_grid_city(n=8, size_m=80.0, seed=2).city.topologies.surface_topology, device="cpu")
+    nets = [_FakeNet(0.8), _FakeNet(1.3)]
+    storms = [rainfall_event([0.0, 20.0], [20.0, 90.0], [80.0, 30.0]),
+              rainfall_event([0.0], [150.0], [45.0]),
+              rainfall_event([10.0, 60.0], [60.0, 100.0], [110.0, 5.0]),
+              rainfall_event([0.0], [40.0], [20.0])]
+    durations = [5400.0, 10800.0, 7200.0, 3000.0]  # 2, 3, 2 and 1 windows
+    preds, spread = ensemble_rollouts(nets, mf, storms, durations, copies=2)
+    act = mf.active
+    for i, (storm, dur) in enumerate(zip(storms, durations)):
+        alone = [rollout(n, mf, storm, dur) for n in nets]
+        ends, h, hm = preds[i]
+        np.testing.assert_array_equal(ends, alone[0][0])
+        np.testing.assert_allclose(h, np.mean([a[1] for a in alone], 0), rtol=1e-6, atol=1e-7)
+        np.testing.assert_allclose(hm, np.mean([a[2] for a in alone], 0), rtol=1e-6, atol=1e-7)
+        mean = np.mean([a[2] for a in alone], 0)
+        want = np.sqrt(np.mean([(a[2][:, act] - mean[:, act]) ** 2 for a in alone]))
+        assert abs(spread[i] - want) <= 1e-6 * max(want, 1e-6), (i, spread[i], want)
+    # one network: the mean is its rollout and there is no disagreement
+    one, sp1 = ensemble_rollouts(nets[:1], mf, storms, durations, copies=3)
+    assert not sp1.any()
+    np.testing.assert_allclose(one[1][2], rollout(nets[0], mf, storms[1], durations[1])[2], rtol=1e-6, atol=1e-7)
